@@ -1,0 +1,215 @@
+"""Lead modes and mode-matching self-energies (host input to the transmission path).
+
+The nested-dissection path takes ``Σ_L``, ``Σ_R`` as inputs (``NestedTwoTerminal::transmission_with``,
+``crates/caroli-green/src/nested.rs:682``); caroli computes them by mode matching
+(``crates/caroli-green/src/modes.rs``).  This module computes the same retarded self-energies on
+the host with LAPACK (numpy/scipy), by a formulation of its own:
+
+- the Bloch problem ``(h01^† λ^-1 + h00 - E + h01 λ) φ = 0`` of a lead cell (``h01 = <j|H|j+1>``)
+  is linearised as the ``2n`` pencil ``A v = λ B v`` with ``v = (ψ_j, ψ_{j+1})``;
+- modes with ``|λ| < 1`` and propagating modes with positive current go right, the others left;
+  the current of a propagating group is ``J_pq = i(λ_q φ_p^† h01 φ_q - λ_p^* φ_p^† h01^† φ_q)``,
+  diagonalised within degenerate groups (the reference's rule, ``modes.rs:400-446``);
+- with ``V`` the right-going vectors, ``Σ_R = h01 V_bot V_top^-1``; with ``W`` the left-going ones,
+  ``Σ_L = h01^† W_top W_bot^-1`` (any basis of the subspaces gives the same ``Σ``);
+- a Hermitian scalar coupling ``h01 = s c 1`` (square and cubic leads) takes the fast path of
+  ``modes.rs:540-710``: one eigen-decomposition of ``h00``, reused at every energy;
+- band edges and surface bound states are retried at ``E + δ``, ``δ`` in ``{0, 1e-9 … 1e-6}``
+  times the bandwidth scale (``modes.rs:49-50``, ``:129-145``).
+
+``Σ`` is the mathematically unique retarded self-energy, so it agrees with the reference's
+``sigma_left``/``sigma_right`` to rounding; the tests pin it against the reference's published
+transmissions and against Lopez-Sancho decimation.
+"""
+from __future__ import annotations
+
+import numpy as np
+import scipy.linalg as sla
+
+UNIT_TOL = 1e-6
+DEGENERATE_TOL = 1e-7
+VELOCITY_TOL = 1e-8
+DEFECTIVE_TOL = 1e-7
+SINGULAR_TOL = 1e-11
+SHIFTS = (0.0, 1e-9, 1e-8, 1e-7, 1e-6)
+
+
+class GreenError(Exception):
+    """Mirror of ``GreenError`` (``crates/caroli-green/src/lib.rs:34-47``)."""
+
+    def __init__(self, kind, detail=""):
+        super().__init__(f"{kind}: {detail}" if detail else kind)
+        self.kind = kind
+
+
+def _row_norm(m):
+    return float(np.abs(m).sum(axis=1).max()) if m.size else 0.0
+
+
+def _hermitian(m, tol=1e-14):
+    return np.abs(m - m.conj().T).max() <= tol * max(np.abs(m).max(), 0.0) if m.size else True
+
+
+def _inv_cond(m):
+    if m.shape[0] == 0:
+        return 1.0
+    s = np.linalg.svd(m, compute_uv=False)
+    return float(s.min() / s.max()) if s.max() > 0 else 0.0
+
+
+class LeadSolver:
+    """Energy-independent part of a lead's mode problem (``ModeSolver``, ``modes.rs:514-538``)."""
+
+    def __init__(self, h00, h01):
+        self.h00 = np.array(h00, dtype=np.complex128)
+        self.h01 = np.array(h01, dtype=np.complex128)
+        n = self.h00.shape[0]
+        self.n = n
+        self.scale = max(_row_norm(self.h00) + 2.0 * _row_norm(self.h01), np.finfo(float).tiny)
+        self.cell = None
+        if n and np.abs(self.h01).max() > 0 and _hermitian(self.h00) and _hermitian(self.h01):
+            c = self.h01[0, 0].real
+            if c != 0 and np.abs(self.h01 - c * np.eye(n)).max() <= 1e-14 * abs(c):
+                s = 1.0 if c > 0 else -1.0
+                theta, y = np.linalg.eigh(0.5 * (self.h00 + self.h00.conj().T))
+                self.cell = (s, abs(c), theta, y)
+
+    def self_energies(self, energy):
+        """``(Σ_L, Σ_R, energy used)`` at the real ``energy`` (shifted off band edges)."""
+        last = GreenError("Eigen")
+        for shift in SHIFTS:
+            e = energy + shift * self.scale
+            try:
+                if self.cell is not None:
+                    return self._definite(e) + (e,)
+                return self._general(e) + (e,)
+            except GreenError as err:
+                last = err
+            except (np.linalg.LinAlgError, ValueError) as err:
+                last = GreenError("Eigen", str(err))
+        raise last
+
+    # -- h01 = s c 1: one Hermitian problem ------------------------------------------------------
+    def _definite(self, e):
+        s, c, theta, y = self.cell
+        mu = -(theta - e) / (s * c)
+        lam_r = np.empty(len(mu), np.complex128)
+        lam_l = np.empty(len(mu), np.complex128)
+        for k, m in enumerate(mu):
+            if abs(m) < 2.0:
+                root = complex(m / 2.0, np.sqrt(4.0 - m * m) / 2.0)
+                if 2.0 * root.imag < DEGENERATE_TOL:
+                    raise GreenError("Singular", f"subband edge near E = {e}")
+                # Current J = -2 s c Im λ: the root with s Im λ < 0 goes right.
+                r, l = (root, root.conjugate()) if s < 0 else (root.conjugate(), root)
+                if abs(2.0 * r.imag / c) < VELOCITY_TOL * self.scale:
+                    raise GreenError("Singular", f"subband edge near E = {e}")
+                lam_r[k], lam_l[k] = r, l
+            else:
+                big = (m + np.sign(m) * np.sqrt(m * m - 4.0)) / 2.0
+                if abs(big) <= 1.0 + UNIT_TOL:
+                    raise GreenError("Singular", f"subband edge near E = {e}")
+                lam_r[k], lam_l[k] = 1.0 / big, big
+        # Σ_R = h01 F_+ with F_+ = Y λ_R Y†;  Σ_L = h01† F_-^-1 with F_-^-1 = Y λ_L^-1 Y†.
+        sig_r = (s * c) * (y * lam_r) @ y.conj().T
+        sig_l = (s * c) * (y * (1.0 / lam_l)) @ y.conj().T
+        return sig_l, sig_r
+
+    # -- general coupling: the 2n pencil ---------------------------------------------------------
+    def _general(self, e):
+        n = self.n
+        h00, h01 = self.h00, self.h01
+        eye = np.eye(n, dtype=np.complex128)
+        zero = np.zeros((n, n), np.complex128)
+        a = np.block([[zero, eye], [-h01.conj().T, e * eye - h00]])
+        b = np.block([[eye, zero], [zero, h01]])
+        w, vr = sla.eig(a, b, homogeneous_eigvals=True, right=True)
+        alpha, beta = w[0], w[1]
+        mod_a, mod_b = np.abs(alpha), np.abs(beta)
+        right_ev = mod_a < (1.0 - UNIT_TOL) * mod_b
+        left_ev = mod_a > (1.0 + UNIT_TOL) * mod_b
+        prop = ~(right_ev | left_ev)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            lam = np.where(mod_b > 0, alpha / np.where(mod_b > 0, beta, 1.0), np.inf)
+        vr = vr / np.linalg.norm(vr, axis=0)
+
+        right_vecs, left_vecs = [], []
+        pidx = np.nonzero(prop)[0]
+        # Degenerate propagating groups by single linkage.
+        groups = []
+        for k in pidx:
+            placed = False
+            for g in groups:
+                if any(abs(lam[k] - lam[j]) < DEGENERATE_TOL for j in g):
+                    g.append(k)
+                    placed = True
+                    break
+            if not placed:
+                groups.append([k])
+        for g in groups:
+            v = vr[:, g]
+            phi = v[:n]
+            lg = lam[g]
+            gram = v.conj().T @ v
+            if _inv_cond(gram) < DEFECTIVE_TOL ** 2:
+                raise GreenError("Singular", f"Jordan block (subband edge) near E = {e}")
+            a_ = phi.conj().T @ (h01 @ phi)
+            b_ = phi.conj().T @ (h01.conj().T @ phi)
+            cur = 1j * (a_ * lg[None, :] - lg.conj()[:, None] * b_)
+            cur = 0.5 * (cur + cur.conj().T)
+            vel, coef = sla.eigh(cur, gram)
+            newv = v @ coef
+            for k in range(len(g)):
+                ph = newv[:n, k]
+                vk = vel[k] / max(np.vdot(ph, ph).real, np.finfo(float).tiny)
+                if not np.isfinite(vk) or abs(vk) < VELOCITY_TOL * self.scale:
+                    raise GreenError("Singular", f"subband edge near E = {e}")
+                (right_vecs if vk > 0 else left_vecs).append(newv[:, k])
+        nr = int(right_ev.sum()) + len(right_vecs)
+        nl = int(left_ev.sum()) + len(left_vecs)
+        if nr != n or nl != n:
+            raise GreenError("ModeCount", f"{nr} right-going and {nl} left-going, expected {n}")
+        vr_right = np.concatenate([vr[:, right_ev]] + [np.array(right_vecs).T.reshape(2 * n, -1)], axis=1)
+        vr_left = np.concatenate([vr[:, left_ev]] + [np.array(left_vecs).T.reshape(2 * n, -1)], axis=1)
+        if _inv_cond(vr_right) < 1e-10 or _inv_cond(vr_left) < 1e-10:
+            vr_right, vr_left = self._schur_bases(a, b, vr_right[:, right_ev.sum():], vr_left[:, left_ev.sum():])
+        top, bot = vr_right[:n], vr_right[n:]
+        if _inv_cond(top) < SINGULAR_TOL:
+            raise GreenError("Singular", f"lead surface bound state near E = {e}")
+        sig_r = h01 @ np.linalg.solve(top.T, bot.T).T
+        top, bot = vr_left[:n], vr_left[n:]
+        if _inv_cond(bot) < SINGULAR_TOL:
+            raise GreenError("Singular", f"lead surface bound state near E = {e}")
+        sig_l = h01.conj().T @ np.linalg.solve(bot.T, top.T).T
+        return sig_l, sig_r
+
+    @staticmethod
+    def _schur_bases(a, b, prop_right, prop_left):
+        """Orthonormal bases of the evanescent subspaces from the ordered QZ decomposition, for
+        pencils whose eigenvectors are too close to parallel."""
+        def first(sort):
+            _, _, alpha, beta, _, z = sla.ordqz(a, b, sort=sort, output="complex")
+            k = int(sum(sort(x, y) for x, y in zip(alpha, beta)))
+            return z[:, :k]
+
+        inside = lambda x, y: abs(x) < (1.0 - UNIT_TOL) * abs(y)
+        outside = lambda x, y: abs(x) > (1.0 + UNIT_TOL) * abs(y)
+        right = np.concatenate([first(inside), prop_right], axis=1)
+        left = np.concatenate([first(outside), prop_left], axis=1)
+        return right, left
+
+
+def broadening(sigma):
+    """``Γ = i(Σ - Σ†)`` (``crates/caroli-green/src/lib.rs:67-71``)."""
+    return 1j * (sigma - sigma.conj().T)
+
+
+def gamma_root(sigma):
+    """``W`` with ``W W† = Γ``: eigenvectors of ``Γ`` with eigenvalues above ``1e-12`` of the
+    largest, scaled by their square roots (``nested.rs:1036-1047``)."""
+    g = broadening(sigma)
+    g = 0.5 * (g + g.conj().T)
+    vals, vecs = np.linalg.eigh(g)
+    top = np.abs(vals).max() if len(vals) else 0.0
+    keep = vals > 1e-12 * top
+    return vecs[:, keep] * np.sqrt(vals[keep])[None, :]
