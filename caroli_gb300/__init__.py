@@ -1,0 +1,19 @@
+"""caroli_gb300 — GB300-native (sm_103a) nested-dissection two-terminal transmission of caroli.
+
+The hot path (front assembly, pivot-block elimination, Schur updates, root solve and Caroli trace)
+runs in ``libcaroli_gb300.so`` (``csrc/``), reached through the C ABI of
+``include/caroli_gb300.h``; this package is the host face that mirrors caroli's Rust API.
+"""
+from .lattice import Lattice, Region, Site
+from .leads import GreenError, LeadSolver, broadening, gamma_root
+from .model import BhzParams, Model, OnSiteMap, SparseMatrix, bhz, bhz_exchange, bhz_spin, cubic, graphene, square
+from .nested import LeadSelfEnergies, NestedTwoTerminal
+from .precision import Precision, PrecisionOptions, PrecisionReport, checked
+from .system import System, build_system
+
+__all__ = [
+    "Lattice", "Region", "Site", "GreenError", "LeadSolver", "broadening", "gamma_root", "BhzParams", "Model",
+    "OnSiteMap", "SparseMatrix", "bhz", "bhz_exchange", "bhz_spin", "cubic", "graphene", "square",
+    "LeadSelfEnergies", "NestedTwoTerminal", "Precision", "PrecisionOptions", "PrecisionReport", "checked",
+    "System", "build_system",
+]

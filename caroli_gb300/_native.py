@@ -1,0 +1,150 @@
+"""ctypes binding of ``libcaroli_gb300.so`` (the C ABI of ``include/caroli_gb300.h``).
+
+The library is built in-tree (``caroli_gb300/_build``) by ``__graft_entry__.build()``. There is no
+fallback: without the library every GPU entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libcaroli_gb300.so")
+
+OK, PIVOT_DELAYED, SINGULAR, NONFINITE, REFINE_STALLED, TIMEOUT = 0, 1, 2, 3, 4, 5
+EINVAL, ENOMEM, ECUDA, EUNAVAILABLE = 16, 17, 18, 19
+DOUBLE, SINGLE, MIXED = 0, 1, 2
+
+# Every symbol the header declares, with its ctypes signature.
+P = ctypes.c_void_p
+I64 = ctypes.c_int64
+SIGNATURES = {
+    "caroli_ctx_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    "caroli_ctx_destroy": (None, [P]),
+    "caroli_last_error": (ctypes.c_char_p, [P]),
+    "caroli_plan_upload": (ctypes.c_int, [P, I64, P, P, I64, ctypes.c_int, P, P, P, P, I64, P, ctypes.c_int, P, P, P,
+                                          P, P, ctypes.POINTER(ctypes.c_int)]),
+    "caroli_plan_info": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P, P]),
+    "caroli_values_upload": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P]),
+    "caroli_sigma_upload": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, ctypes.c_double, P, P]),
+    "caroli_solve_batch": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, ctypes.c_int, P, P, P]),
+    "caroli_last_timing": (ctypes.c_int, [P, P, P]),
+}
+
+_lib = None
+
+
+class NativeError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"caroli_gb300 native error {code}: {msg}")
+        self.code = code
+
+
+def load():
+    """The loaded library; raises if it was not built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise NativeError(EUNAVAILABLE, f"{LIB_PATH} is missing: build the CUDA library first")
+        lib = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+class Context:
+    """A device context (``caroli_ctx``)."""
+
+    def __init__(self, device=0):
+        lib = load()
+        h = ctypes.c_void_p()
+        rc = lib.caroli_ctx_create(device, ctypes.byref(h))
+        if rc != OK:
+            raise NativeError(rc, "no usable CUDA device" if rc == EUNAVAILABLE else "caroli_ctx_create failed")
+        self.h = h
+        self.lib = lib
+
+    def check(self, rc):
+        if rc != OK:
+            raise NativeError(rc, self.lib.caroli_last_error(self.h).decode())
+
+    def close(self):
+        if self.h:
+            self.lib.caroli_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Plan:
+    """A system uploaded to a context (``caroli_plan_upload``) with its values and Σ slots."""
+
+    def __init__(self, ctx: Context, system):
+        self.ctx = ctx
+        s = system
+        self._keep = []
+
+        def arr(x, dt):
+            a = np.ascontiguousarray(x, dtype=dt)
+            self._keep.append(a)
+            return a
+
+        lp = arr(np.cumsum([0] + [len(b.left) for b in s.blocks]), np.int64)
+        rp = arr(np.cumsum([0] + [len(b.right) for b in s.blocks]), np.int64)
+        lf = arr(np.concatenate([b.left for b in s.blocks]) if s.blocks else [], np.int64)
+        rt = arr(np.concatenate([b.right for b in s.blocks]) if s.blocks else [], np.int64)
+        pid = ctypes.c_int()
+        ctx.check(ctx.lib.caroli_plan_upload(
+            ctx.h, s.n, ptr(arr(s.row_ptr, np.int64)), ptr(arr(s.cols, np.uint32)), len(s.site_offsets), s.dim,
+            ptr(arr(s.cells, np.int64)), ptr(arr(s.site_offsets, np.int64)), ptr(arr(s.site_orbitals, np.int64)),
+            ptr(arr(s.range, np.int64)), len(s.interior), ptr(arr(s.interior, np.int64)), len(s.blocks),
+            ptr(arr(s.labels, np.int32)), ptr(lp), ptr(lf), ptr(rp), ptr(rt), ctypes.byref(pid)))
+        self.id = pid.value
+        self._keep = []
+        self.nblocks = len(s.blocks)
+        self.slots = {}
+
+    def info(self, block):
+        vals = [ctypes.c_int64() for _ in range(5)]
+        self.ctx.check(self.ctx.lib.caroli_plan_info(self.ctx.h, self.id, block, *[ctypes.byref(v) for v in vals]))
+        return dict(zip(["fronts", "max_n", "max_ne", "root_n", "arena_elems"], [v.value for v in vals]))
+
+    def upload_values(self, values):
+        v = np.ascontiguousarray(np.stack(values), dtype=np.complex128)
+        self.ctx.check(self.ctx.lib.caroli_values_upload(self.ctx.h, self.id, v.shape[0], ptr(v)))
+
+    def upload_sigma(self, slot, energy, sigmas):
+        ls = [np.asfortranarray(sl, dtype=np.complex128) for sl, _ in sigmas]
+        rs = [np.asfortranarray(sr, dtype=np.complex128) for _, sr in sigmas]
+        pl = np.array([a.ctypes.data for a in ls], dtype=np.uintp)
+        pr = np.array([a.ctypes.data for a in rs], dtype=np.uintp)
+        self.ctx.check(self.ctx.lib.caroli_sigma_upload(self.ctx.h, self.id, slot, energy, ptr(pl), ptr(pr)))
+
+    def solve(self, slots, configs, precision=DOUBLE):
+        slots = np.ascontiguousarray(slots, np.int32)
+        configs = np.ascontiguousarray(configs, np.int32)
+        n = len(slots)
+        t = np.zeros(n)
+        st = np.zeros(n, np.int32)
+        err = np.zeros(n)
+        self.ctx.check(self.ctx.lib.caroli_solve_batch(self.ctx.h, self.id, n, ptr(slots), ptr(configs), precision,
+                                                       ptr(t), ptr(st), ptr(err)))
+        return t, st, err
+
+    def last_timing(self):
+        ms, launches = ctypes.c_double(), ctypes.c_int64()
+        self.ctx.check(self.ctx.lib.caroli_last_timing(self.ctx.h, ctypes.byref(ms), ctypes.byref(launches)))
+        return ms.value, launches.value

@@ -1,0 +1,166 @@
+"""``NestedTwoTerminal``: the drop-in host face of the GB300 transmission path.
+
+Mirrors the public API of ``caroli_green::NestedTwoTerminal`` (``crates/caroli-green/src/nested.rs``):
+
+=============================  ==========================================================
+reference                      here
+=============================  ==========================================================
+``from_model`` :530            ``NestedTwoTerminal.from_model`` (and ``from_models`` for a
+                               batch of disorder configurations of one geometry)
+``block_count`` :613           ``block_count``
+``transmission`` :618          ``transmission``
+``transmissions`` :623         ``transmissions`` (one batched GPU launch sequence)
+``transmissions_checked`` :630 ``transmissions_checked``
+``self_energies`` :652         ``self_energies`` -> ``LeadSelfEnergies``
+``transmission_with`` :682     ``transmission_with``
+``transmission_with_precision``  ``transmission_with_precision``
+  :688
+=============================  ==========================================================
+
+The elimination and the trace run on the GPU through ``libcaroli_gb300.so``; the lead
+self-energies are computed on the host (``leads.py``), once per energy, and reused for every
+configuration as the reference does (``self_energies`` doc, nested.rs:643-651). A failed solve
+raises ``GreenError("Singular", …)`` as ``GreenError::Singular`` (nested.rs:798-800).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _native
+from .leads import GreenError, LeadSolver
+from .precision import Precision, PrecisionOptions, checked
+from .system import System, build_system
+
+
+@dataclass
+class LeadSelfEnergies:
+    """Self-energies of every block at one energy (``nested.rs:436-459``)."""
+
+    energy: float
+    blocks: list  # [(Σ_L, Σ_R)] per block
+
+    def key(self):
+        return id(self)
+
+
+_CONTEXTS = {}
+
+
+def context(device=0):
+    """The shared device context of ``device`` (created on first use)."""
+    if device not in _CONTEXTS:
+        _CONTEXTS[device] = _native.Context(device)
+    return _CONTEXTS[device]
+
+
+class NestedTwoTerminal:
+    def __init__(self, system: System, device: int = 0):
+        self.system = system
+        self.device = device
+        self._solvers = []
+        for b in system.blocks:
+            left = LeadSolver(b.left_h00, b.left_h01)
+            right = left if b.same_lead() else LeadSolver(b.right_h00, b.right_h01)
+            self._solvers.append((left, right))
+        self._plan = None
+        self._slot_of = {}
+
+    # -- construction -------------------------------------------------------------------------
+    @staticmethod
+    def from_model(device_model, lead, region, axis, device=0):
+        return NestedTwoTerminal(build_system([device_model], lead, region, axis), device)
+
+    @staticmethod
+    def from_models(device_models, lead, region, axis, device=0):
+        """One system per disorder configuration of the same geometry and leads."""
+        return NestedTwoTerminal(build_system(list(device_models), lead, region, axis), device)
+
+    def block_count(self):
+        return len(self.system.blocks)
+
+    def config_count(self):
+        return self.system.config_count()
+
+    # -- self-energies ------------------------------------------------------------------------
+    def self_energies(self, energy) -> LeadSelfEnergies:
+        blocks = []
+        for left, right in self._solvers:
+            sl, sr_same, _ = left.self_energies(energy)
+            sr = sr_same if right is left else right.self_energies(energy)[1]
+            blocks.append((sl, sr))
+        return LeadSelfEnergies(float(energy), blocks)
+
+    # -- GPU plumbing -------------------------------------------------------------------------
+    def plan(self):
+        if self._plan is None:
+            self._plan = _native.Plan(context(self.device), self.system)
+            self._plan.upload_values(self.system.values)
+        return self._plan
+
+    def _slot(self, sigma: LeadSelfEnergies):
+        if len(sigma.blocks) != len(self.system.blocks):
+            raise ValueError("self-energies of a system with other blocks")
+        for (sl, sr), b in zip(sigma.blocks, self.system.blocks):
+            if sl.shape != (len(b.left),) * 2 or sr.shape != (len(b.right),) * 2:
+                raise ValueError("self-energies of a system with other leads")
+        key = id(sigma)
+        if key not in self._slot_of or self._slot_of[key][1] is not sigma:
+            slot = len(self._slot_of)
+            self.plan().upload_sigma(slot, sigma.energy, sigma.blocks)
+            self._slot_of[key] = (slot, sigma)
+        return self._slot_of[key][0]
+
+    def solve_batch(self, sigmas, configs, precision=Precision.DOUBLE):
+        """Raw batched solve: ``(T, status, err)`` arrays for the pairs ``(sigmas[i], configs[i])``."""
+        slots = [self._slot(s) for s in sigmas]
+        return self.plan().solve(slots, configs, int(precision))
+
+    # -- transmissions ------------------------------------------------------------------------
+    def transmission_with_precision(self, sigma, precision=Precision.DOUBLE, config=0):
+        t, st, _ = self.solve_batch([sigma], [config], precision)
+        return _result(t[0], st[0], sigma.energy)
+
+    def transmission_with(self, sigma, config=0):
+        return self.transmission_with_precision(sigma, Precision.DOUBLE, config)
+
+    def transmission(self, energy, config=0):
+        return self.transmission_with(self.self_energies(energy), config)
+
+    def transmissions_with(self, sigmas, configs=None, precision=Precision.DOUBLE):
+        """T for each ``(sigma, config)`` pair in one batch; failed points are ``GreenError``."""
+        if configs is None:
+            configs = [0] * len(sigmas)
+        t, st, _ = self.solve_batch(sigmas, configs, precision)
+        out = []
+        for i, s in enumerate(sigmas):
+            try:
+                out.append(_result(t[i], st[i], s.energy))
+            except GreenError as e:
+                out.append(e)
+        return out
+
+    def transmissions(self, energies, config=0, precision=Precision.DOUBLE):
+        sigmas = []
+        for e in energies:
+            sigmas.append(self.self_energies(e))
+        return self.transmissions_with(sigmas, [config] * len(sigmas), precision)
+
+    def transmissions_checked(self, energies, options: PrecisionOptions, config=0):
+        sigmas = {float(e): self.self_energies(e) for e in energies}
+
+        def run(points, precision):
+            return self.transmissions_with([sigmas[float(e)] for e in points], [config] * len(points), precision)
+
+        return checked(list(energies), options, run)
+
+
+def _result(t, status, energy):
+    if status == _native.OK:
+        return float(t)
+    if status in (_native.SINGULAR, _native.NONFINITE):
+        raise GreenError("Singular", f"lead self-energy or root singular near E = {energy}")
+    if status == _native.REFINE_STALLED:
+        raise GreenError("NoConvergence", f"refinement stalled at E = {energy}")
+    raise GreenError("Singular", f"solve status {status} at E = {energy}")

@@ -1,0 +1,102 @@
+/* caroli_gb300 — C ABI of the GB300 (sm_103a) nested-dissection transmission of caroli.
+ *
+ * This is the boundary a caroli caller binds: plain pointers and sizes, an int status on every
+ * call, no exceptions across the ABI. The caller owns its host buffers; the library owns the
+ * device memory. One CUDA stream per context; a context is not safe to share between threads
+ * without external locking.
+ *
+ * Reference interfaces each entry point replaces (caroli, crates/caroli-green/src/nested.rs):
+ *   caroli_ctx_create / caroli_ctx_destroy   the "cuda" feature's device handle, CudaDevice::new
+ *                                            (crates/caroli-gpu/src/cuda.rs:162-183)
+ *   caroli_plan_upload                       NestedTwoTerminal::from_model        nested.rs:530-610
+ *   caroli_values_upload                     the H values of each disorder configuration
+ *                                            (caroli-cli/src/run.rs:118-121 builds one system each)
+ *   caroli_sigma_upload                      LeadSelfEnergies from self_energies  nested.rs:439-459, :652-676
+ *   caroli_solve_batch                       transmission_with / transmission_with_precision /
+ *                                            transmissions                        nested.rs:618-713
+ *   caroli_transmission_with_grad            no counterpart: the reference has no derivative code;
+ *                                            the adjoint of transmission_with (dT/dV, dT/dJ)
+ *   caroli_last_error                        GreenError / GpuError text           caroli-green/src/lib.rs:34-47
+ */
+#ifndef CAROLI_GB300_H
+#define CAROLI_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct caroli_ctx caroli_ctx;
+
+/* Status codes: return values of every call, and per-solve statuses of caroli_solve_batch. */
+enum {
+  CAROLI_OK = 0,
+  CAROLI_PIVOT_DELAYED = 1,   /* internal: a front refused its pivots (resolved by re-planning) */
+  CAROLI_SINGULAR = 2,        /* GreenError::Singular: the root solve is singular or not finite */
+  CAROLI_NONFINITE = 3,       /* T is not finite */
+  CAROLI_REFINE_STALLED = 4,  /* mixed precision: refinement did not reach its tolerance */
+  CAROLI_TIMEOUT = 5,
+  CAROLI_EINVAL = 16,         /* bad argument (message in caroli_last_error) */
+  CAROLI_ENOMEM = 17,         /* device allocation failed */
+  CAROLI_ECUDA = 18,          /* CUDA error (message in caroli_last_error) */
+  CAROLI_EUNAVAILABLE = 19    /* no usable GPU (GpuError::Unavailable) */
+};
+
+/* Precision of the fronts below the root (Precision, caroli-green/src/precision.rs:22-32). */
+enum {
+  CAROLI_DOUBLE = 0, /* complex f64 throughout */
+  CAROLI_SINGLE = 1, /* complex f32 fronts, f64 root and trace, unrefined (Precision::Single) */
+  CAROLI_MIXED = 2   /* complex f32 fronts as a preconditioner of FP64 iterative refinement of the
+                        whole solve (no counterpart; Precision gains a Mixed variant) */
+};
+
+int caroli_ctx_create(int device_ordinal, caroli_ctx** out);
+void caroli_ctx_destroy(caroli_ctx* ctx);
+const char* caroli_last_error(const caroli_ctx* ctx);
+
+/* Two-terminal system (NestedTwoTerminal::from_model). All arrays are copied.
+ *   n, row_ptr[n+1], cols[nnz]           CSR pattern of H (u32 columns, sorted per row)
+ *   nsites, dim, cells[3*nsites]         site cells (first axis slowest), lattice dimension
+ *   site_offsets[nsites], site_orbitals[nsites]
+ *   range[3]                             hopping range per axis (>= 1)
+ *   n_interior, interior[]               sites of the elimination tree (all but the two lead slices)
+ *   nblocks, labels[n]                   independent block of each orbital, -1 for none
+ *   left_ptr[nblocks+1], left[]          per block, device orbitals of the first slice (lead-cell order)
+ *   right_ptr[nblocks+1], right[]        per block, device orbitals of the last slice
+ * On success *plan_id identifies the system in later calls. */
+int caroli_plan_upload(caroli_ctx* ctx, int64_t n, const int64_t* row_ptr, const uint32_t* cols, int64_t nsites,
+                       int dim, const int64_t* cells, const int64_t* site_offsets, const int64_t* site_orbitals,
+                       const int64_t* range, int64_t n_interior, const int64_t* interior, int nblocks,
+                       const int32_t* labels, const int64_t* left_ptr, const int64_t* left,
+                       const int64_t* right_ptr, const int64_t* right, int* plan_id);
+
+/* Shape of a plan: blocks, tree fronts of block `block`, largest front, root size. */
+int caroli_plan_info(caroli_ctx* ctx, int plan_id, int block, int64_t* fronts, int64_t* max_n, int64_t* max_ne,
+                     int64_t* root_n, int64_t* arena_elems);
+
+/* H values of `nconfigs` disorder configurations on the plan's pattern: values[c*nnz + q] as
+ * interleaved complex128 (re, im). Replaces previously uploaded values. */
+int caroli_values_upload(caroli_ctx* ctx, int plan_id, int nconfigs, const double* values);
+
+/* Lead self-energies of energy slot `slot` (any slot number; re-uploading replaces it):
+ * sigma_l[b], sigma_r[b] are column-major complex128 (nl_b x nl_b, nr_b x nr_b) of block b. */
+int caroli_sigma_upload(caroli_ctx* ctx, int plan_id, int slot, double energy, const double* const* sigma_l,
+                        const double* const* sigma_r);
+
+/* T for `count` instances (energy slot, configuration), summed over the blocks.
+ *   precision       CAROLI_DOUBLE, CAROLI_SINGLE or CAROLI_MIXED
+ *   t[count]        transmissions; status[count] per-instance status (CAROLI_OK ...)
+ *   err[count]      (may be NULL) error estimate: CAROLI_MIXED, the last refinement correction of
+ *                   T; otherwise 0
+ * Returns CAROLI_OK when the batch ran (individual solves may still carry a non-OK status). */
+int caroli_solve_batch(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots, const int32_t* configs,
+                       int precision, double* t, int32_t* status, double* err);
+
+/* Device time of the last caroli_solve_batch (ms), and kernels it launched. */
+int caroli_last_timing(const caroli_ctx* ctx, double* device_ms, int64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CAROLI_GB300_H */

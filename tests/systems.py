@@ -1,0 +1,83 @@
+"""Test systems: the reference's benchmark problems (benchmarks/transport.toml with the disorder of
+caroli-bench/src/main.rs:118-126) and the workloads of the GB300 path."""
+from __future__ import annotations
+
+import json
+import os
+
+import numpy as np
+
+from caroli_gb300 import NestedTwoTerminal, Region, bhz, cubic, graphene, square
+from caroli_gb300.disorder import Moments, ScalarPotential, bench_disorder, disordered
+from caroli_gb300.model import bhz_spin
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+CLEAN = {"square": square, "bhz": bhz, "graphene": graphene}
+PROBLEMS = {"square-clean": ("square", None, None), "square-anderson": ("square", 1, 2.0),
+            "bhz-anderson": ("bhz", 2, 0.5), "graphene-anderson": ("graphene", 4, 1.0)}
+
+
+def bench_golden():
+    with open(os.path.join(GOLDEN, "bench_transmissions.json")) as f:
+        return json.load(f)["results"]
+
+
+def bench_problem(name, width, length=None):
+    """The device and lead models and region of a benchmark problem (L = W by default)."""
+    model_name, seed, w = PROBLEMS[name]
+    clean = CLEAN[model_name]()
+    length = length or width
+    region = Region.cuboid(clean.lattice, [length, width, 0])
+    if seed is None:
+        return clean, clean, region
+    subs = len(clean.lattice.sublattices)
+    orb = clean.lattice.sublattices[0].orbitals
+    pot = bench_disorder(seed, width, length, width, subs, w)
+    return clean.with_onsite_term(ScalarPotential(pot, width, subs, orb)), clean, region
+
+
+def bench_system(name, width):
+    dev, lead, region = bench_problem(name, width)
+    return NestedTwoTerminal.from_model(dev, lead, region, 0)
+
+
+def clean_bhz_ribbon(length=16, width=10):
+    """Config: clean BHZ ribbon with leads of the same model (ti_conductance.rs:20-24)."""
+    m = bhz()
+    return NestedTwoTerminal.from_model(m, m, Region.cuboid(m.lattice, [length, width, 0]), 0)
+
+
+def magnetic_bhz(length, width, configs, concentration=0.2, exchange=0.4, moments=None, spin="opposite-g",
+                 anderson=None):
+    """BHZ ribbon with CLI-style [[disorder]] entries (caroli-cli/src/build.rs:251-310), one system
+    per configuration: magnetic impurities at a concentration over all sites, and optionally an
+    Anderson entry first."""
+    m = bhz()
+    region = Region.cuboid(m.lattice, [length, width, 0])
+    entries = []
+    if anderson is not None:
+        entries.append({"kind": "anderson", "strength": anderson})
+    entries.append({"kind": "magnetic", "concentration": concentration, "exchange": exchange,
+                    "moments": moments or Moments.polarized(1.0), "spin": bhz_spin(spin)})
+    devices = [disordered(m, region, entries, c) for c in range(configs)]
+    return NestedTwoTerminal.from_models(devices, m, region, 0)
+
+
+def cubic_wire(length, width, depth, w=16.5, configs=1, seed=1):
+    """Cubic Anderson wire, leads of the clean cubic model along x."""
+    m = cubic()
+    region = Region.cuboid(m.lattice, [length, width, depth])
+    devices = []
+    for c in range(configs):
+        entries = [{"kind": "anderson", "strength": w, "seed": seed}]
+        devices.append(disordered(m, region, entries, c))
+    return NestedTwoTerminal.from_models(devices, m, region, 0)
+
+
+def oracle_T(sys_, sigma, config=0, precision=0):
+    from oracle import Oracle
+
+    if not hasattr(sys_, "_oracle"):
+        sys_._oracle = Oracle(sys_.system)
+    return sys_._oracle.transmission(sigma.energy, sys_.system.values[config], sigma.blocks, precision)

@@ -1,0 +1,69 @@
+"""GPU path against the oracle on the same inputs (all through the C ABI)."""
+import numpy as np
+import pytest
+
+from systems import bench_golden, bench_system, clean_bhz_ribbon, cubic_wire, magnetic_bhz, oracle_T
+from caroli_gb300 import GreenError, Precision
+
+pytestmark = pytest.mark.gpu
+
+
+def test_clean_bhz_33_energies_double():
+    """Plain FP64: clean BHZ 16 x 10, 33 energies in [-0.16, 0.16]; T(0) = 2 to 1e-8."""
+    sys_ = clean_bhz_ribbon()
+    energies = np.linspace(-0.16, 0.16, 33)
+    sigmas = [sys_.self_energies(e) for e in energies]
+    ts = sys_.transmissions_with(sigmas)
+    for s, t in zip(sigmas, ts):
+        ref = oracle_T(sys_, s)
+        assert abs(t - ref) <= 1e-10 * (1 + abs(ref)), (s.energy, t, ref)
+    assert abs(ts[16] - 2.0) < 1e-8
+
+
+@pytest.mark.parametrize("problem", ["square-anderson", "bhz-anderson", "graphene-anderson", "square-clean"])
+def test_bench_w32_double_matches_oracle_and_published(problem):
+    gold = bench_golden()[f"caroli/{problem}/32"]
+    sys_ = bench_system(problem, 32)
+    sigmas = [sys_.self_energies(e) for e in gold["energies"]]
+    ts = sys_.transmissions_with(sigmas)
+    runs = np.array(gold["runs"])
+    for k, (s, t) in enumerate(zip(sigmas, ts)):
+        ref = oracle_T(sys_, s)
+        assert abs(t - ref) <= 1e-10 * (1 + abs(ref)), (problem, s.energy, t, ref)
+        assert abs(t - np.median(runs[:, k])) <= 1e-8 * (1 + abs(t))
+
+
+def test_clean_square_delayed_pivots():
+    """Clean square lattice at E = 0: interior blocks are exactly singular and get delayed
+    (tests/nested.rs covers E = 0); the GPU re-plans those solves."""
+    sys_ = bench_system("square-clean", 32)
+    s = sys_.self_energies(0.0)
+    t = sys_.transmission_with(s)
+    assert abs(t - oracle_T(sys_, s)) < 1e-9
+    assert abs(t - round(t)) < 1e-8
+
+
+def test_magnetic_configurations_batch():
+    sys_ = magnetic_bhz(24, 12, configs=3)
+    sigmas = [sys_.self_energies(e) for e in (-0.12, 0.0, 0.07)]
+    pairs = [(s, c) for s in sigmas for c in range(3)]
+    ts = sys_.transmissions_with([p[0] for p in pairs], [p[1] for p in pairs])
+    for (s, c), t in zip(pairs, ts):
+        ref = oracle_T(sys_, s, config=c)
+        assert abs(t - ref) <= 1e-10 * (1 + abs(ref))
+
+
+def test_cubic_wire():
+    sys_ = cubic_wire(12, 6, 6, configs=2)
+    for e in (-0.5, 0.3):
+        s = sys_.self_energies(e)
+        for c in range(2):
+            t = sys_.transmission_with(s, config=c)
+            assert abs(t - oracle_T(sys_, s, config=c)) <= 1e-10 * (1 + t)
+
+
+def test_single_precision_follows_double():
+    sys_ = bench_system("bhz-anderson", 32)
+    s = sys_.self_energies(0.3)
+    t32 = sys_.transmission_with_precision(s, Precision.SINGLE)
+    assert abs(t32 - oracle_T(sys_, s)) < 1e-2
