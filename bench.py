@@ -1,0 +1,348 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 nested-dissection transmission (one JSON line on rank 0).
+
+Workload (the configuration the headline metric is quoted on): BHZ ribbon 200 x 64 sites
+(51 200 complex unknowns, two spin blocks of 25 600), magnetic disorder at concentration 0.2 with
+exchange J = 0.4, opposite-g spin matrices (s_z tau_z), moments polarised along z, impurities at
+seeded random sites (CLI convention: configuration c seeded with 1 + c); 33 energies uniform in
+[-0.16, 0.16] x 8 configurations = 264 transmissions per step. Synthetic inputs of that shape
+(no dataset is involved); the lead self-energies are computed once per energy on the host and
+stay resident, as the reference reuses them for every configuration.
+
+A step is one batched pass of the path over the 264 (energy, configuration) solves:
+- ``value``: solves/s of the mixed path (complex-f32 multifrontal factors + FP64 iterative
+  refinement to |dT| <= 1e-8), inputs resident in HBM, device time between CUDA events on the
+  library's stream (the stream every kernel of the library runs on);
+- ``e2e``: the same through the public API with host buffers: every step uploads the H values of
+  the 8 configurations and the self-energies of the 33 energies from host memory and reads the
+  transmissions back;
+- beside them the plain FP64 GPU path on the same batch (the denominator of the target ratio),
+  and max |dT| of the mixed path against it.
+The arena of a step (~33 GB) is far larger than L2, so no L2 flush is needed between steps.
+
+``--impl reference`` times the reference's CPU path on the host cores: the C++ restatement of
+caroli's NestedTwoTerminal (oracle/, FP64, OpenMP over solves), since the reference itself (Rust)
+cannot be built here.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "T(E) solves/s, mixed+refined vs FP64 GPU at |ΔT|≤1e-8; grad/fwd time ratio"
+# Kernel classes whose algorithmic work is counted in flops (the rest in bytes).
+FLOP_CLASSES = {"small_front", "large_front", "front_gemm", "root_inverse", "trace", "refine_residual"}
+WORKLOAD = "bhz-magnetic-200x64: BHZ 200x64, magnetic c=0.2 J=0.4 opposite-g polarised, 33 E in [-0.16,0.16] x 8 configs"
+
+
+def build_workload(length=200, width=64, configs=8, energies=33):
+    from caroli_gb300 import NestedTwoTerminal, Region, bhz
+    from caroli_gb300.disorder import Moments, disordered
+    from caroli_gb300.model import bhz_spin
+
+    m = bhz()
+    region = Region.cuboid(m.lattice, [length, width, 0])
+    entry = {"kind": "magnetic", "concentration": 0.2, "exchange": 0.4, "moments": Moments.polarized(1.0),
+             "spin": bhz_spin("opposite-g")}
+    devices = [disordered(m, region, [entry], c) for c in range(configs)]
+    sys_ = NestedTwoTerminal.from_models(devices, m, region, 0)
+    es = np.linspace(-0.16, 0.16, energies)
+    sigmas = [sys_.self_energies(e) for e in es]
+    pairs = [(s, c) for s in sigmas for c in range(configs)]
+    return sys_, sigmas, pairs
+
+
+class Clocks:
+    """nvidia-smi samples of SM clocks and throttle reasons during a timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out = ""
+
+    def summary(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in getattr(self, "out", "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            p = json.load(f)
+        return {"hbm_gbs": p["hbm_gbs"], "bf16_tflops": p["bf16_tflops"], "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
+
+
+def cpu_baseline(sys_, pairs, sample, threads):
+    """The oracle (C++ restatement of the reference's CPU path) on `sample` instances."""
+    from oracle import Oracle
+
+    orc = Oracle(sys_.system)
+    sub = pairs[:sample]
+    nb = sys_.block_count()
+    blocks, energies, vals, sls, srs = [], [], [], [], []
+    for s, c in sub:
+        for b in range(nb):
+            blocks.append(b)
+            energies.append(s.energy)
+            vals.append(sys_.system.values[c])
+            sls.append(s.blocks[b][0])
+            srs.append(s.blocks[b][1])
+    t0 = time.perf_counter()
+    t, st = orc.solve_batch(blocks, energies, vals, sls, srs, precision=0, threads=threads)
+    dt = time.perf_counter() - t0
+    tsum = t.reshape(len(sub), nb).sum(axis=1)
+    return len(sub) / dt, dt, tsum
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        return world, rank, local, dist, torch
+    return world, rank, local, None, None
+
+
+def barrier(dist, torch):
+    if dist is not None:
+        dist.barrier()
+
+
+def reduce_max(x, dist, torch):
+    if dist is None:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_ours(args):
+    from caroli_gb300 import Precision
+    from caroli_gb300.nested import context
+
+    world, rank, local, dist, torch = dist_setup(args)
+    sys_, sigmas, pairs = build_workload(args.length, args.width, args.configs, args.energies)
+    sys_.device = local
+    plan = sys_.plan()
+    ctx = context(local)
+    S = [p[0] for p in pairs]
+    C = [p[1] for p in pairs]
+    nsolve = len(pairs)
+    for _ in range(args.warmup):
+        sys_.solve_batch(S, C, Precision.MIXED)
+    # Timed region: K steps of the mixed path, inputs resident.
+    barrier(dist, torch)
+    with Clocks(local) as clk:
+        ctx.region_begin()
+        w0 = time.perf_counter()
+        for _ in range(args.steps):
+            t_mixed, st_mixed, err_mixed = sys_.solve_batch(S, C, Precision.MIXED)
+        ms, launches = ctx.region_end()
+        wall = time.perf_counter() - w0
+    barrier(dist, torch)
+    ms_max = reduce_max(ms, dist, torch)
+    fallbacks, max_iters = plan.last_stats()
+    iters, perturbed, jstat = plan.last_job_info()
+    # Plain FP64 GPU path on the same batch (one step after one warm-up).
+    sys_.solve_batch(S, C, Precision.DOUBLE)
+    ctx.region_begin()
+    t_dbl, st_dbl, _ = sys_.solve_batch(S, C, Precision.DOUBLE)
+    ms_dbl, _ = ctx.region_end()
+    dT = np.abs(t_mixed - t_dbl)
+    # End to end through the public API from host buffers.
+    values = np.ascontiguousarray(np.stack(sys_.system.values))
+    h2d = values.nbytes + sum(sum(a.nbytes + b.nbytes for a, b in s.blocks) for s in sigmas)
+    h2d += 2 * 4 * nsolve
+    d2h = nsolve * (8 + 4 + 8)
+    ctx.region_begin()
+    e0 = time.perf_counter()
+    for _ in range(args.steps):
+        plan.upload_values(list(values))
+        for slot, s in enumerate(sigmas):
+            plan.upload_sigma(sys_._slot_of[id(s)][0], s.energy, s.blocks)
+        sys_.solve_batch(S, C, Precision.MIXED)
+    e2e_ms, _ = ctx.region_end()
+    e2e_wall = time.perf_counter() - e0
+    # Per-kernel probe (untimed pass per class): the dominant kernel and its roofline.
+    names = ctx.kernel_classes()
+    probe = {}
+    for k, name in enumerate(names):
+        for q in range(len(names)):
+            ctx.kernel_stats(q, reset=True)
+        ctx.probe(k)
+        sys_.solve_batch(S, C, Precision.MIXED)
+        ctx.probe(-1)
+        stt = ctx.kernel_stats(k)
+        probe[name] = {"ms": stt["ms"], "flops": stt["flops"], "bytes": stt["bytes"], "launches": stt["launches"]}
+    dom = max(probe.items(), key=lambda kv: kv[1]["ms"])
+    pk = peaks()
+    d = dom[1]
+    if dom[0] in FLOP_CLASSES:
+        achieved = d["flops"] / (d["ms"] * 1e-3) / 1e12
+        roof = {"kernel": dom[0], "bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+                "frac": achieved / pk["bf16_tflops"], "traffic": None,
+                "note": f"peak = {pk['source']} bf16 dense; the kernel runs on FP32 CUDA cores"}
+    else:
+        achieved = d["bytes"] / (d["ms"] * 1e-3) / 1e9
+        roof = {"kernel": dom[0], "bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / pk["hbm_gbs"], "traffic": None, "note": f"peak = {pk['source']} HBM copy"}
+    roof["ms_per_step"] = d["ms"]
+    roof["launches_per_step"] = d["launches"]
+    roof["share_of_step"] = d["ms"] / (ms_max / args.steps)
+    kernels = {k: {"ms": round(v["ms"], 3), "launches": v["launches"]} for k, v in probe.items() if v["launches"]}
+    cpu = None
+    if rank == 0 and world == 1 and args.cpu_sample > 0:
+        threads = os.cpu_count() or 1
+        rate, dt, tcpu = cpu_baseline(sys_, pairs, args.cpu_sample, threads)
+        cpu = {"value": rate, "unit": "solves/s", "cores": threads, "kind": "port",
+               "sample": f"{args.cpu_sample} of the step's {nsolve} solves (both blocks each), {dt:.1f} s wall",
+               "max_abs_dT_vs_gpu_fp64": float(np.abs(tcpu - t_dbl[:args.cpu_sample]).max())}
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+    value = world * nsolve * args.steps / (ms_max * 1e-3)
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "solves/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_max / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "c64 factors + f64 refinement",
+        "data": "synthetic (seeded disorder of the reference's CLI conventions; no dataset)",
+        "config": {"workload": WORKLOAD, "solves_per_step": nsolve, "blocks": sys_.block_count(),
+                   "unknowns": sys_.system.n, "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (arena ~33 GB per step)"},
+        "fp64_gpu": {"value": nsolve / (ms_dbl * 1e-3), "unit": "solves/s", "ms_per_step": ms_dbl},
+        "mixed_over_fp64": ms_dbl / (ms_max / args.steps),
+        "max_abs_dT_vs_fp64": float(dT.max()),
+        "median_abs_dT_vs_fp64": float(np.median(dT)),
+        "refinement": {"max_iterations": max_iters, "fp64_recomputed_solves": fallbacks,
+                       "median_iterations": float(np.median(iters)) if len(iters) else None,
+                       "perturbed_pivots_total": int(perturbed.sum()) if len(perturbed) else 0},
+        "grad_fwd_ratio": None,
+        "e2e": {"value": nsolve * args.steps / (e2e_ms * 1e-3), "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "wall_s": e2e_wall},
+        "gpu_launches": int(launches),
+        "roofline": roof,
+        "kernels_ms_per_step": kernels,
+        "clocks": clk.summary(),
+        "wall_s_timed": wall,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import Oracle
+
+    sys_, sigmas, pairs = build_workload(args.length, args.width, args.configs, args.energies)
+    threads = os.cpu_count() or 1
+    sample = args.ref_sample
+    for _ in range(args.warmup):
+        cpu_baseline(sys_, pairs, max(1, sample // 4), threads)
+    times = []
+    for k in range(args.steps):
+        rate, dt, _ = cpu_baseline(sys_, pairs, sample, threads)
+        times.append(dt)
+    total = sum(times)
+    value = sample * args.steps / total
+    line = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128", "impl": "reference",
+        "data": "synthetic (same workload as the GPU arm)",
+        "config": {"workload": WORKLOAD, "solves_per_step": sample, "parallelism": "host cores"},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
+                         "sample": f"{sample} of the workload's {len(pairs)} solves per step, FP64, OpenMP over solves"},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--length", type=int, default=200)
+    ap.add_argument("--width", type=int, default=64)
+    ap.add_argument("--configs", type=int, default=8)
+    ap.add_argument("--energies", type=int, default=33)
+    ap.add_argument("--cpu-sample", type=int, default=32)
+    ap.add_argument("--ref-sample", type=int, default=32)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

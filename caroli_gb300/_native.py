@@ -31,6 +31,15 @@ SIGNATURES = {
     "caroli_sigma_upload": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, ctypes.c_double, P, P]),
     "caroli_solve_batch": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, ctypes.c_int, P, P, P]),
     "caroli_last_timing": (ctypes.c_int, [P, P, P]),
+    "caroli_last_stats": (ctypes.c_int, [P, P, P]),
+    "caroli_last_phases": (ctypes.c_int, [P, P, P, P]),
+    "caroli_region_begin": (ctypes.c_int, [P]),
+    "caroli_region_end": (ctypes.c_int, [P, P, P]),
+    "caroli_kernel_classes": (ctypes.c_int, []),
+    "caroli_last_job_info": (ctypes.c_int, [P, I64, P, P, P, P]),
+    "caroli_kernel_class_name": (ctypes.c_char_p, [ctypes.c_int]),
+    "caroli_probe_kernel": (ctypes.c_int, [P, ctypes.c_int]),
+    "caroli_kernel_stats": (ctypes.c_int, [P, ctypes.c_int, P, P, P, P, ctypes.c_int]),
 }
 
 _lib = None
@@ -76,6 +85,26 @@ class Context:
     def check(self, rc):
         if rc != OK:
             raise NativeError(rc, self.lib.caroli_last_error(self.h).decode())
+
+    def region_begin(self):
+        self.check(self.lib.caroli_region_begin(self.h))
+
+    def region_end(self):
+        ms, n = ctypes.c_double(), ctypes.c_int64()
+        self.check(self.lib.caroli_region_end(self.h, ctypes.byref(ms), ctypes.byref(n)))
+        return ms.value, n.value
+
+    def kernel_classes(self):
+        return [self.lib.caroli_kernel_class_name(k).decode() for k in range(self.lib.caroli_kernel_classes())]
+
+    def probe(self, kclass):
+        self.check(self.lib.caroli_probe_kernel(self.h, kclass))
+
+    def kernel_stats(self, kclass, reset=False):
+        n, f, b, ms = ctypes.c_int64(), ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        self.check(self.lib.caroli_kernel_stats(self.h, kclass, ctypes.byref(n), ctypes.byref(f), ctypes.byref(b),
+                                                ctypes.byref(ms), int(reset)))
+        return {"launches": n.value, "flops": f.value, "bytes": b.value, "ms": ms.value}
 
     def close(self):
         if self.h:
@@ -143,6 +172,24 @@ class Plan:
         self.ctx.check(self.ctx.lib.caroli_solve_batch(self.ctx.h, self.id, n, ptr(slots), ptr(configs), precision,
                                                        ptr(t), ptr(st), ptr(err)))
         return t, st, err
+
+    def last_stats(self):
+        fb, it = ctypes.c_int64(), ctypes.c_int64()
+        self.ctx.check(self.ctx.lib.caroli_last_stats(self.ctx.h, ctypes.byref(fb), ctypes.byref(it)))
+        return fb.value, it.value
+
+    def last_phases(self):
+        a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        self.ctx.check(self.ctx.lib.caroli_last_phases(self.ctx.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return a.value, b.value, c.value
+
+    def last_job_info(self):
+        cnt = ctypes.c_int64()
+        self.ctx.check(self.ctx.lib.caroli_last_job_info(self.ctx.h, 0, None, None, None, ctypes.byref(cnt)))
+        it = np.zeros(cnt.value, np.int32); pt = np.zeros(cnt.value, np.int32); st = np.zeros(cnt.value, np.int32)
+        self.ctx.check(self.ctx.lib.caroli_last_job_info(self.ctx.h, cnt.value, ptr(it), ptr(pt), ptr(st),
+                                                         ctypes.byref(cnt)))
+        return it, pt, st
 
     def last_timing(self):
         ms, launches = ctypes.c_double(), ctypes.c_int64()

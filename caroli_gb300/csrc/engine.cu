@@ -10,15 +10,19 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cmath>
 #include <cstring>
 #include <memory>
 #include <numeric>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/caroli_gb300.h"
 #include "kernels.cuh"
 #include "plan.hpp"
+#include "refine.cuh"
+#include "dense.cuh"
 
 using namespace caroli;
 
@@ -55,8 +59,12 @@ struct DevPlan {
   int32_t* maps = nullptr;
   uint8_t* own = nullptr;
   Entry* entries = nullptr;
+  int32_t* vidx = nullptr;
   void upload(cudaStream_t s) {
     fronts = dalloc<FrontDesc>(host.fronts.size());
+    vidx = dalloc<int32_t>(std::max<size_t>(1, host.vidx.size()));
+    if (!host.vidx.empty())
+      CK(cudaMemcpyAsync(vidx, host.vidx.data(), host.vidx.size() * sizeof(int32_t), cudaMemcpyHostToDevice, s));
     maps = dalloc<int32_t>(std::max<size_t>(1, host.maps.size()));
     own = dalloc<uint8_t>(std::max<size_t>(1, host.own.size()));
     entries = dalloc<Entry>(std::max<size_t>(1, host.entries.size()));
@@ -70,16 +78,36 @@ struct DevPlan {
     CK(cudaStreamSynchronize(s));
   }
   void release() {
-    cudaFree(fronts); cudaFree(maps); cudaFree(own); cudaFree(entries);
-    fronts = nullptr; maps = nullptr; own = nullptr; entries = nullptr;
+    cudaFree(fronts); cudaFree(maps); cudaFree(own); cudaFree(entries); cudaFree(vidx);
+    fronts = nullptr; maps = nullptr; own = nullptr; entries = nullptr; vidx = nullptr;
   }
 };
 
 struct SigmaSlot {
   double energy = 0.0;
   bool set = false;
-  std::vector<double2*> sl, sr, gl, gr;  // per block, device
+  std::vector<double2*> sl, sr, gl, gr, wr;  // per block, device
+  std::vector<int> channels;                // columns of W_R per block
 };
+
+// Block data the refinement needs (block-local CSR of H, slice positions).
+struct DevBlock {
+  int32_t nblk = 0;
+  int64_t nnz = 0;
+  int32_t *csr_ptr = nullptr, *csr_col = nullptr, *slice_l = nullptr, *slice_r = nullptr, *left_local = nullptr,
+          *right_local = nullptr;
+  int64_t* csr_q = nullptr;
+  void release() {
+    for (int32_t* p : {csr_ptr, csr_col, slice_l, slice_r, left_local, right_local}) cudaFree(p);
+    cudaFree(csr_q);
+  }
+};
+
+template <typename T> T* upload_vec(const std::vector<T>& v, cudaStream_t s) {
+  T* d = dalloc<T>(std::max<size_t>(1, v.size()));
+  if (!v.empty()) CK(cudaMemcpyAsync(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+  return d;
+}
 
 struct System {
   // Owned copies of the description.
@@ -89,14 +117,16 @@ struct System {
   SystemDesc desc{};
   std::vector<BlockTree> trees;
   std::vector<std::unique_ptr<DevPlan>> plans;  // static plan per block
+  std::vector<DevBlock> blocks;
   double2* vals = nullptr;
   int nconfigs = 0;
   std::vector<SigmaSlot> slots;
   ~System() {
     for (auto& p : plans) p->release();
+    for (auto& b : blocks) b.release();
     cudaFree(vals);
     for (auto& s : slots)
-      for (auto* v : {&s.sl, &s.sr, &s.gl, &s.gr})
+      for (auto* v : {&s.sl, &s.sr, &s.gl, &s.gr, &s.wr})
         for (auto* p : *v) cudaFree(p);
   }
 };
@@ -118,6 +148,19 @@ struct Buf {
   ~Buf() { cudaFree(p); }
 };
 
+// Kernel classes for per-kernel accounting: launches, algorithmic flops and bytes (computed on
+// the host from the task lists), and device time when the class is probed.
+enum KClass { K_SMALL = 0, K_ASSEMBLE, K_PIVOT, K_GEMM, K_STOREX, K_ROOT_ASM, K_ROOT_INV, K_TRACE,
+              K_REF_FWD, K_REF_ROOT, K_REF_BWD, K_REF_RES, K_REF_CHECK, K_REF_GMRES, K_COUNT };
+const char* const kclass_names[K_COUNT] = {"small_front", "assemble", "large_front", "front_gemm", "store_x",
+                                           "root_assemble", "root_inverse", "trace", "refine_forward",
+                                           "refine_root", "refine_backward", "refine_residual", "refine_check",
+                                           "refine_gmres"};
+struct KStat {
+  int64_t launches = 0;
+  double flops = 0.0, bytes = 0.0, ms = 0.0;
+};
+
 struct JobSpec {
   int block, slot, config;
   const DevPlan* plan;
@@ -128,12 +171,27 @@ struct JobSpec {
 struct caroli_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, evf = nullptr, evr = nullptr, reg0 = nullptr, reg1 = nullptr;
+  int64_t region_launches = 0;
+  KStat kstat[K_COUNT];
+  int probe = -1;  // kernel class timed launch by launch (-1: none)
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> probe_events;
+  size_t probe_used = 0;
+  double factor_ms = 0.0, root_ms = 0.0, tail_ms = 0.0;
   std::string err;
   std::vector<std::unique_ptr<System>> systems;
-  Buf arena, xs, jobs, tasks, fail, status, tout, part;
+  Buf arena, root_arena, xs, jobs, tasks, fail, status, tout, part, pert;
+  Buf rdesc, rx, rr, rd, rtb, rhb, rt, rerr, rdone;
+  Buf inv, ipiv, iy, iscale, ibad;
+  Buf gV, gZ, gH, gg, gcs, gsn, gy, gbeta, gcol, gflags;
+  double inner_tol = 1e-10;
+  int max_iters = 6;
+  double refine_tol = 1e-12;
   double last_ms = 0.0;
   int64_t last_launches = 0;
+  int64_t fallbacks = 0;
+  int64_t refine_iters = 0;
+  std::vector<int32_t> job_iters, job_perturbed, job_status;
   size_t mem_budget = 0;
 };
 
@@ -171,50 +229,297 @@ template <typename F> void in_pieces(size_t count, F fn) {
   for (size_t first = 0; first < count; first += 65535) fn(first, std::min<size_t>(65535, count - first));
 }
 
-// Runs `specs` (all of precision T); fills per-job T, status and (optionally) fail flags.
-template <typename T>
-void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, std::vector<double>& t_out,
-              std::vector<int32_t>& st_out, std::vector<std::vector<uint8_t>>* fails) {
-  using V = typename Cx<T>::V;
+struct LevelRange {
+  size_t first, count;
+  int max_n;
+};
+
+// FP64 iterative refinement of the jobs [begin, begin + cj) after their f32 factorization.
+template <typename LaunchT>
+void refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, size_t begin, size_t cj,
+            const std::vector<LevelRange>& lr, int max_root, const Task* dtasks, const std::vector<JobDesc>& jd,
+            const float2* arena, const std::vector<size_t>& arena_off, const float2* rarena,
+            const std::vector<size_t>& root_off, LaunchT& launch, std::vector<double>& th, std::vector<double>& eh,
+            std::vector<int32_t>& sh, std::vector<int32_t>& ih) {
   cudaStream_t s = ctx->stream;
-  const size_t vb = sizeof(V);
+  std::vector<RefineDesc> rdh(cj);
+  size_t xo = 0, to = 0, ho = 0;
+  int cmax = 0, max_blk = 0;
+  std::vector<size_t> xoffs(cj), toffs(cj), hoffs(cj), coffs(cj);
+  size_t co = 0;
+  double sweep_bytes = 0.0, resid_flops = 0.0;
+  for (size_t j = 0; j < cj; ++j) {
+    const JobSpec& sp = specs[begin + j];
+    const FrontPlan& P = sp.plan->host;
+    const DevBlock& B = sys->blocks[sp.block];
+    const int c = sys->slots[sp.slot].channels[sp.block];
+    cmax = std::max(cmax, c);
+    max_blk = std::max(max_blk, B.nblk);
+    xoffs[j] = xo; xo += (size_t)B.nblk * c;
+    coffs[j] = co; co += (size_t)c;
+    toffs[j] = to; to += (size_t)P.sum_ne * c;
+    hoffs[j] = ho; ho += (size_t)P.sum_nb * c;
+    for (size_t k = 0; k + 1 < P.fronts.size(); ++k) {
+      const double ne = P.fronts[k].ne, n = P.fronts[k].n;
+      sweep_bytes += (ne * ne + 2 * ne * (n - ne)) * sizeof(float2);  // factors read per sweep pair
+    }
+    resid_flops += 8.0 * c * ((double)B.nnz + (double)P.nl * P.nl + (double)P.nr * P.nr);
+  }
+  double2* rx = static_cast<double2*>(ctx->rx.get(std::max<size_t>(xo, 1) * sizeof(double2)));
+  double2* rr = static_cast<double2*>(ctx->rr.get(std::max<size_t>(xo, 1) * sizeof(double2)));
+  float2* rdv = static_cast<float2*>(ctx->rd.get(std::max<size_t>(xo, 1) * sizeof(float2)));
+  float2* rtb = static_cast<float2*>(ctx->rtb.get(std::max<size_t>(to, 1) * sizeof(float2)));
+  float2* rhb = static_cast<float2*>(ctx->rhb.get(std::max<size_t>(ho, 1) * sizeof(float2)));
+  double* rt_out = static_cast<double*>(ctx->rt.get(cj * sizeof(double)));
+  double* rerr = static_cast<double*>(ctx->rerr.get(cj * sizeof(double)));
+  int32_t* rdone = static_cast<int32_t*>(ctx->rdone.get(cj * sizeof(int32_t)));
+  CK(cudaMemsetAsync(rt_out, 0, cj * sizeof(double), s));
+  CK(cudaMemsetAsync(rerr, 0, cj * sizeof(double), s));
+  const size_t M = GM_M;
+  double2* gV = static_cast<double2*>(ctx->gV.get(std::max<size_t>(xo, 1) * (M + 1) * sizeof(double2)));
+  float2* gZ = static_cast<float2*>(ctx->gZ.get(std::max<size_t>(xo, 1) * M * sizeof(float2)));
+  double2* gH = static_cast<double2*>(ctx->gH.get(std::max<size_t>(co, 1) * (M + 1) * M * sizeof(double2)));
+  double2* gg = static_cast<double2*>(ctx->gg.get(std::max<size_t>(co, 1) * (M + 1) * sizeof(double2)));
+  double* gcs = static_cast<double*>(ctx->gcs.get(std::max<size_t>(co, 1) * M * sizeof(double)));
+  double2* gsn = static_cast<double2*>(ctx->gsn.get(std::max<size_t>(co, 1) * M * sizeof(double2)));
+  double2* gy = static_cast<double2*>(ctx->gy.get(std::max<size_t>(co, 1) * M * sizeof(double2)));
+  double* gbeta = static_cast<double*>(ctx->gbeta.get(std::max<size_t>(co, 1) * sizeof(double)));
+  int32_t* gcol = static_cast<int32_t*>(ctx->gcol.get(std::max<size_t>(co, 1) * sizeof(int32_t)));
+  int32_t* gflags = static_cast<int32_t*>(ctx->gflags.get(cj * sizeof(int32_t)));
+  for (size_t j = 0; j < cj; ++j) {
+    const JobSpec& sp = specs[begin + j];
+    const DevPlan& P = *sp.plan;
+    const DevBlock& B = sys->blocks[sp.block];
+    const SigmaSlot& sg = sys->slots[sp.slot];
+    RefineDesc& R = rdh[j];
+    std::memset(&R, 0, sizeof(R));
+    R.fronts = P.fronts; R.maps = P.maps; R.own = P.own; R.vidx = P.vidx;
+    R.arena = arena + arena_off[j];
+    R.root = rarena + root_off[j];
+    R.csr_ptr = B.csr_ptr; R.csr_col = B.csr_col; R.csr_q = B.csr_q;
+    R.vals = jd[j].vals;
+    R.slice_l = B.slice_l; R.slice_r = B.slice_r; R.left_local = B.left_local; R.right_local = B.right_local;
+    R.sigma_l = sg.sl[sp.block]; R.sigma_r = sg.sr[sp.block]; R.gamma_l = sg.gl[sp.block];
+    R.w_r = sg.wr[sp.block];
+    R.energy = sg.energy;
+    R.nblk = B.nblk; R.nl = P.host.nl; R.nr = P.host.nr; R.c = sg.channels[sp.block]; R.root_front = P.host.root;
+    R.sum_ne = P.host.sum_ne; R.sum_nb = P.host.sum_nb;
+    R.x = rx + xoffs[j]; R.r = rr + xoffs[j]; R.d = rdv + xoffs[j];
+    R.tb = rtb + toffs[j]; R.hb = rhb + hoffs[j];
+    R.V = gV + xoffs[j] * (M + 1);
+    R.Z = gZ + xoffs[j] * M;
+    R.H = gH + coffs[j] * (M + 1) * M;
+    R.g = gg + coffs[j] * (M + 1);
+    R.cs = gcs + coffs[j] * M;
+    R.sn = gsn + coffs[j] * M;
+    R.y = gy + coffs[j] * M;
+    R.beta = gbeta + coffs[j];
+    R.col_done = gcol + coffs[j];
+    R.done = R.c == 0 ? 1 : 0;  // no channel: T = 0
+  }
+  RefineDesc* drd = static_cast<RefineDesc*>(ctx->rdesc.get(cj * sizeof(RefineDesc)));
+  CK(cudaMemcpyAsync(drd, rdh.data(), cj * sizeof(RefineDesc), cudaMemcpyHostToDevice, s));
+  const unsigned cchunks = (unsigned)std::max(1, (cmax + RCB - 1) / RCB);
+  in_pieces(cj, [&](size_t f0, size_t c) {
+    launch(K_REF_RES, 0.0, 0.0, [&] { refine_init_kernel<<<dim3(16, (unsigned)c), 256, 0, s>>>(drd + f0, (int)c); });
+  });
+  std::vector<int32_t> dh(cj, 0);
+  const int nlev = (int)lr.size();
+  const unsigned rows = (unsigned)((max_blk + 255) / 256);
+  const unsigned cols = (unsigned)std::max(1, cmax);
+  // Preconditioner application M^-1 V_k -> Z_k (src = dst = k).
+  auto sweep = [&](int src, int dst) {
+    for (int L = 0; L < nlev; ++L) {
+      if (!lr[L].count) continue;
+      const size_t sm = 2 * (size_t)lr[L].max_n * RCB * sizeof(float2);
+      launch(K_REF_FWD, 0.0, sweep_bytes * 0.5 / nlev, [&] {
+        refine_forward_kernel<<<dim3((unsigned)lr[L].count, cchunks), 256, sm, s>>>(drd, dtasks + lr[L].first, src);
+      });
+    }
+    in_pieces(cj, [&](size_t f0, size_t c) {
+      launch(K_REF_ROOT, 0.0, 0.0, [&] {
+        refine_root_kernel<<<dim3((unsigned)c, cchunks), 256, (size_t)max_root * RCB * sizeof(float2), s>>>(drd + f0, src,
+                                                                                                        dst);
+      });
+    });
+    for (int L = nlev - 1; L >= 0; --L) {
+      if (!lr[L].count) continue;
+      const size_t sm = (size_t)lr[L].max_n * RCB * sizeof(float2);
+      launch(K_REF_BWD, 0.0, sweep_bytes * 0.5 / nlev, [&] {
+        refine_backward_kernel<<<dim3((unsigned)lr[L].count, cchunks), 256, sm, s>>>(drd, dtasks + lr[L].first, src,
+                                                                                    dst);
+      });
+    }
+  };
+  for (int it = 0; it < ctx->max_iters; ++it) {
+    in_pieces(cj, [&](size_t f0, size_t c) {
+      launch(K_REF_GMRES, 0.0, 0.0, [&] { gm_start_kernel<<<dim3((unsigned)c, cols), 256, 0, s>>>(drd + f0); });
+    });
+    for (int k = 0; k < GM_M; ++k) {
+      sweep(k, k);
+      in_pieces(cj, [&](size_t f0, size_t c) {
+        launch(K_REF_RES, resid_flops * c / cj, 0.0,
+               [&] { gm_matvec_kernel<<<dim3((unsigned)c, rows), 256, 0, s>>>(drd + f0, k); });
+      });
+      for (int pass = 0; pass < 2; ++pass) {
+        in_pieces(cj, [&](size_t f0, size_t c) {
+          launch(K_REF_GMRES, 0.0, 0.0,
+                 [&] { gm_dot_kernel<<<dim3((unsigned)c, cols, (unsigned)(k + 1)), 256, 0, s>>>(drd + f0, k, pass); });
+          launch(K_REF_GMRES, 0.0, 0.0, [&] { gm_axpy_kernel<<<dim3((unsigned)c, rows), 256, 0, s>>>(drd + f0, k); });
+        });
+      }
+      in_pieces(cj, [&](size_t f0, size_t c) {
+        launch(K_REF_GMRES, 0.0, 0.0,
+               [&] { gm_norm_kernel<<<dim3((unsigned)c, cols), 256, 0, s>>>(drd + f0, k, ctx->inner_tol); });
+      });
+      launch(K_REF_GMRES, 0.0, 0.0, [&] {
+        gm_inner_check_kernel<<<(unsigned)((cj + 127) / 128), 128, 0, s>>>(drd, (int)cj, k, gflags);
+      });
+      CK(cudaMemcpyAsync(dh.data(), gflags, cj * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      bool all = true;
+      for (size_t j = 0; j < cj; ++j) all &= dh[j] != 0;
+      if (all) break;
+    }
+    launch(K_REF_GMRES, 0.0, 0.0, [&] {
+      gm_solve_kernel<<<(unsigned)cj, std::max(32, ((cmax + 31) / 32) * 32), 0, s>>>(drd, (int)cj);
+    });
+    in_pieces(cj, [&](size_t f0, size_t c) {
+      launch(K_REF_GMRES, 0.0, 0.0, [&] { gm_update_kernel<<<dim3((unsigned)c, rows), 256, 0, s>>>(drd + f0); });
+    });
+    launch(K_REF_GMRES, 0.0, 0.0, [&] {
+      gm_residual_kernel<<<(unsigned)((cj + 127) / 128), 128, 0, s>>>(drd, (int)cj);
+    });
+    in_pieces(cj, [&](size_t f0, size_t c) {
+      launch(K_REF_RES, resid_flops * c / cj, 0.0,
+             [&] { refine_residual_kernel<<<dim3((unsigned)c, rows), 256, 0, s>>>(drd + f0); });
+    });
+    launch(K_REF_CHECK, 0.0, 0.0, [&] {
+      refine_check_kernel<<<(unsigned)cj, 256, 0, s>>>(drd, ctx->refine_tol, ctx->max_iters, rt_out, rerr, rdone);
+    });
+    CK(cudaMemcpyAsync(dh.data(), rdone, cj * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    bool all = true;
+    for (size_t j = 0; j < cj; ++j) all &= dh[j] != 0 || rdh[j].c == 0;
+    if (all) break;
+  }
+  CK(cudaEventRecord(ctx->ev1, s));
+  CK(cudaMemcpyAsync(th.data(), rt_out, cj * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(eh.data(), rerr, cj * sizeof(double), cudaMemcpyDeviceToHost, s));
+  std::vector<RefineDesc> fin(cj);
+  CK(cudaMemcpyAsync(fin.data(), drd, cj * sizeof(RefineDesc), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  for (size_t j = 0; j < cj; ++j) {
+    ih[j] = fin[j].iters;
+    if (rdh[j].c == 0) { th[j] = 0.0; eh[j] = 0.0; continue; }
+    if (!fin[j].done || fin[j].stalled) sh[j] = ST_REFINE_STALLED;
+  }
+}
+
+enum Mode { MODE_DOUBLE = 0, MODE_SINGLE = 1, MODE_MIXED = 2 };
+
+struct JobOut {
+  double t = 0.0, err = 0.0;
+  int32_t status = ST_OK;
+  int32_t iters = 0;
+  int32_t perturbed = 0;
+  std::vector<uint8_t> fail;
+};
+
+// Launch bookkeeping: counts, algorithmic work per kernel class, and launch-by-launch device time
+// of the probed class.
+struct Launcher {
+  caroli_ctx* ctx;
+  cudaStream_t s;
+  int64_t launches = 0;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> timed;
+  template <typename F> void operator()(KClass k, double flops, double bytes, F fn) {
+    const bool probe = ctx->probe == (int)k;
+    std::pair<cudaEvent_t, cudaEvent_t> ev{};
+    if (probe) {
+      if (ctx->probe_used == ctx->probe_events.size()) {
+        cudaEvent_t a, b;
+        CK(cudaEventCreate(&a));
+        CK(cudaEventCreate(&b));
+        ctx->probe_events.push_back({a, b});
+      }
+      ev = ctx->probe_events[ctx->probe_used++];
+      CK(cudaEventRecord(ev.first, s));
+    }
+    fn();
+    CK(cudaGetLastError());
+    if (probe) {
+      CK(cudaEventRecord(ev.second, s));
+      timed.push_back({(int)k, ev});
+    }
+    KStat& st = ctx->kstat[k];
+    st.launches += 1;
+    st.flops += flops;
+    st.bytes += bytes;
+    ++launches;
+  }
+  // After a stream synchronisation: device time of the probed launches.
+  void collect() {
+    for (auto& t : timed) {
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, t.second.first, t.second.second));
+      ctx->kstat[t.first].ms += ms;
+    }
+    timed.clear();
+    ctx->probe_used = 0;
+  }
+};
+
+// Runs `specs` in `mode`: complex f64 fronts (DOUBLE), complex f32 fronts under an f64 root
+// (SINGLE), or complex f32 factors refined in FP64 (MIXED). T: front precision, TR: root precision.
+template <typename T, typename TR>
+void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, Mode mode, std::vector<JobOut>& out) {
+  using V = typename Cx<T>::V;
+  using VR = typename Cx<TR>::V;
+  cudaStream_t s = ctx->stream;
+  const size_t vb = sizeof(V), vr = sizeof(VR);
   const size_t nj = specs.size();
-  t_out.assign(nj, 0.0);
-  st_out.assign(nj, ST_OK);
-  if (fails) fails->assign(nj, {});
-  // Chunks of jobs that fit the memory budget.
+  const bool mixed = mode == MODE_MIXED;
+  out.assign(nj, JobOut{});
+  Launcher launch{ctx, s};
   size_t begin = 0;
   while (begin < nj) {
+    // Chunk of jobs within the memory budget.
     size_t end = begin, bytes = 0;
     while (end < nj) {
-      size_t b = (size_t)specs[end].plan->host.arena_elems * vb;
+      const FrontPlan& P = specs[end].plan->host;
+      size_t b = (size_t)P.arena_elems * vb + (size_t)P.fronts[P.root].n * P.fronts[P.root].n * vr;
       if (end > begin && bytes + b > ctx->mem_budget) break;
       bytes += b;
       ++end;
     }
     const size_t cj = end - begin;
-    // Arena offsets, job descriptors, fail-flag offsets.
     std::vector<JobDesc> jd(cj);
-    std::vector<size_t> arena_off(cj), fail_off(cj);
-    size_t aoff = 0, foff = 0;
+    std::vector<size_t> arena_off(cj), root_off(cj), fail_off(cj);
+    size_t aoff = 0, roff = 0, foff = 0;
     int max_levels = 0;
     size_t parts_per_job = 1;
     for (size_t j = 0; j < cj; ++j) {
-      const JobSpec& sp = specs[begin + j];
+      const FrontPlan& P = specs[begin + j].plan->host;
       arena_off[j] = aoff;
-      aoff += (size_t)sp.plan->host.arena_elems;
+      aoff += (size_t)P.arena_elems;
+      root_off[j] = roff;
+      roff += (size_t)P.fronts[P.root].n * P.fronts[P.root].n;
       fail_off[j] = foff;
-      foff += sp.plan->host.fronts.size();
-      max_levels = std::max(max_levels, sp.plan->host.levels);
-      parts_per_job = std::max(parts_per_job, (size_t)(sp.plan->host.nr + 7) / 8);
+      foff += P.fronts.size();
+      max_levels = std::max(max_levels, P.levels);
+      parts_per_job = std::max(parts_per_job, (size_t)(P.nr + 7) / 8);
     }
     V* arena = static_cast<V*>(ctx->arena.get(std::max<size_t>(aoff, 1) * vb));
+    VR* rarena = static_cast<VR*>(ctx->root_arena.get(std::max<size_t>(roff, 1) * vr));
     uint8_t* fail = static_cast<uint8_t*>(ctx->fail.get(std::max<size_t>(foff, 1)));
     int32_t* status = static_cast<int32_t*>(ctx->status.get(cj * sizeof(int32_t)));
+    int* pert = static_cast<int*>(ctx->pert.get(cj * sizeof(int)));
     double* tdev = static_cast<double*>(ctx->tout.get(cj * sizeof(double)));
     double* part = static_cast<double*>(ctx->part.get(cj * parts_per_job * sizeof(double)));
     CK(cudaMemsetAsync(fail, 0, foff, s));
     CK(cudaMemsetAsync(status, 0, cj * sizeof(int32_t), s));
+    CK(cudaMemsetAsync(pert, 0, cj * sizeof(int), s));
     for (size_t j = 0; j < cj; ++j) {
       const JobSpec& sp = specs[begin + j];
       const DevPlan& P = *sp.plan;
@@ -222,6 +527,7 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, s
       JobDesc& d = jd[j];
       d.fronts = P.fronts; d.maps = P.maps; d.own = P.own; d.entries = P.entries;
       d.arena = arena + arena_off[j];
+      d.root_arena = rarena + root_off[j];
       d.vals = sys->vals + (size_t)sp.config * sys->desc.row_ptr[sys->desc.n];
       d.sigma_l = sg.sl[sp.block]; d.sigma_r = sg.sr[sp.block];
       d.gamma_l = sg.gl[sp.block]; d.gamma_r = sg.gr[sp.block];
@@ -232,157 +538,372 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, s
     }
     JobDesc* djobs = static_cast<JobDesc*>(ctx->jobs.get(cj * sizeof(JobDesc)));
     CK(cudaMemcpyAsync(djobs, jd.data(), cj * sizeof(JobDesc), cudaMemcpyHostToDevice, s));
-    // Task lists: per level, small and large tree fronts; then the roots.
-    struct Level { size_t small0, small_n, large0, large_n; int max_small_n, max_large_n, max_large_ne; size_t xs_elems; };
+
+    // Task lists: per level the small fronts then the large ones (contiguous), then the roots.
+    struct Level {
+      size_t small0, small_n, large0, large_n;
+      int max_small_n, max_large_n, max_large_ne, max_n;
+      size_t xs_elems, inv0;
+      double small_flops, small_bytes, inv_flops, gemm0_flops, gemm1_flops, asm_bytes;
+    };
     std::vector<Task> tasks;
     std::vector<Level> levels(max_levels);
+    std::vector<InvTask> inv;  // large fronts' pivot blocks per level, then the roots
     const int small_max = Prec<T>::small_max;
+    size_t inv_piv = 0, inv_y = 0;  // scratch sizes: pivots (entries) and Y blocks (bytes)
+    std::vector<size_t> inv_piv_off, inv_y_off;
     for (int L = 0; L < max_levels; ++L) {
       Level& lv = levels[L];
-      lv = Level{tasks.size(), 0, 0, 0, 0, 0, 0, 0};
+      lv = Level{tasks.size(), 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
       for (size_t j = 0; j < cj; ++j) {
         const auto& fr = specs[begin + j].plan->host.fronts;
         for (size_t k = 0; k + 1 < fr.size(); ++k)
           if (fr[k].level == L && fr[k].n <= small_max) {
             tasks.push_back({(int32_t)j, (int32_t)k, 0});
+            const double ne = fr[k].ne, nb = fr[k].n - fr[k].ne;
             lv.max_small_n = std::max(lv.max_small_n, fr[k].n);
+            lv.small_flops += 8.0 / 3 * ne * ne * ne + 8 * ne * ne * nb + 8 * nb * nb * ne;
+            lv.small_bytes += ((double)fr[k].n * fr[k].n * (mixed ? 1.0 : nb * nb / std::max(1.0, (double)fr[k].n * fr[k].n))) * vb;
           }
       }
       lv.small_n = tasks.size() - lv.small0;
       lv.large0 = tasks.size();
+      lv.inv0 = inv.size();
       size_t xo = 0;
       for (size_t j = 0; j < cj; ++j) {
         const auto& fr = specs[begin + j].plan->host.fronts;
         for (size_t k = 0; k + 1 < fr.size(); ++k)
           if (fr[k].level == L && fr[k].n > small_max) {
             tasks.push_back({(int32_t)j, (int32_t)k, (int64_t)xo});
+            const double ne = fr[k].ne, nb = fr[k].n - fr[k].ne;
             xo += (size_t)fr[k].ne * (fr[k].n - fr[k].ne);
             lv.max_large_n = std::max(lv.max_large_n, fr[k].n);
             lv.max_large_ne = std::max(lv.max_large_ne, fr[k].ne);
+            lv.inv_flops += 8.0 / 3 * ne * ne * ne;
+            lv.gemm0_flops += 8 * ne * ne * nb;
+            lv.gemm1_flops += 8 * nb * nb * ne;
+            lv.asm_bytes += (double)fr[k].n * fr[k].n * vb;
+            if (fr[k].ne > 0) {
+              InvTask it{};
+              it.a = arena + arena_off[j] + fr[k].arena_off;
+              it.ld = fr[k].n;
+              it.n = fr[k].n;
+              it.npiv = fr[k].ne;
+              it.job = (int32_t)j;
+              it.front = (int32_t)k;
+              inv_piv_off.push_back(inv_piv);
+              inv_y_off.push_back(inv_y);
+              inv_piv += fr[k].ne;
+              inv_y += (size_t)GJ_KB * fr[k].n * vb;
+              inv.push_back(it);
+            }
           }
       }
       lv.large_n = tasks.size() - lv.large0;
       lv.xs_elems = xo;
+      lv.max_n = std::max(lv.max_small_n, lv.max_large_n);
     }
-    const size_t root0 = tasks.size();
+    const size_t root0 = tasks.size(), rinv0 = inv.size();
     int max_root = 0;
+    double root_flops = 0.0, trace_flops = 0.0;
     for (size_t j = 0; j < cj; ++j) {
       const auto& P = specs[begin + j].plan->host;
       tasks.push_back({(int32_t)j, P.root, 0});
-      max_root = std::max(max_root, P.fronts[P.root].n);
+      const int m = P.fronts[P.root].n;
+      max_root = std::max(max_root, m);
+      root_flops += 8.0 / 3 * m * (double)m * m + 8.0 * m * (double)m * P.nr;
+      trace_flops += 16.0 * P.nl * (double)P.nl * P.nr;
+      InvTask it{};
+      it.a = rarena + root_off[j];
+      it.ld = m;
+      it.n = m;
+      it.npiv = m;
+      it.job = (int32_t)j;
+      it.front = -1;
+      inv_piv_off.push_back(inv_piv);
+      inv_y_off.push_back(inv_y);
+      inv_piv += m;
+      inv_y += (size_t)GJ_KB * m * vr;
+      inv.push_back(it);
     }
+    // Inverse scratch: pivots, the Y blocks (sized for the wider type), scale and flags.
+    int32_t* dpiv = static_cast<int32_t*>(ctx->ipiv.get(std::max<size_t>(inv_piv, 1) * sizeof(int32_t)));
+    unsigned char* dy = static_cast<unsigned char*>(ctx->iy.get(std::max<size_t>(inv_y, 16)));
+    double* dscale = static_cast<double*>(ctx->iscale.get(std::max<size_t>(inv.size(), 1) * sizeof(double)));
+    int32_t* dbad = static_cast<int32_t*>(ctx->ibad.get(std::max<size_t>(inv.size(), 1) * sizeof(int32_t)));
+    for (size_t q = 0; q < inv.size(); ++q) {
+      inv[q].piv = dpiv + inv_piv_off[q];
+      inv[q].y = dy + inv_y_off[q];
+      inv[q].scale2 = dscale + q;
+      inv[q].bad = dbad + q;
+    }
+    InvTask* dinv = static_cast<InvTask*>(ctx->inv.get(std::max<size_t>(inv.size(), 1) * sizeof(InvTask)));
+    if (!inv.empty())
+      CK(cudaMemcpyAsync(dinv, inv.data(), inv.size() * sizeof(InvTask), cudaMemcpyHostToDevice, s));
     Task* dtasks = static_cast<Task*>(ctx->tasks.get(tasks.size() * sizeof(Task)));
     CK(cudaMemcpyAsync(dtasks, tasks.data(), tasks.size() * sizeof(Task), cudaMemcpyHostToDevice, s));
     size_t xs_max = 1;
     for (auto& lv : levels) xs_max = std::max(xs_max, lv.xs_elems);
     V* xs = static_cast<V*>(ctx->xs.get(xs_max * vb));
 
+    // Batched blocked inverse of `count` matrices starting at dinv + first, largest n.
+    // Batched blocked sweep of `count` fronts starting at dinv + first: largest size nmax, largest
+    // pivot count pmax.
+    auto inverse = [&](auto tag, size_t first, size_t count, int nmax, int pmax, double tol, int perturb, KClass cls,
+                       double flops) {
+      using TT = decltype(tag);
+      using VV = typename Cx<TT>::V;
+      if (!count || nmax <= 0 || pmax <= 0) return;
+      const size_t work = 2 * (size_t)nmax * sizeof(VV);
+      const size_t staged = (size_t)nmax * GJ_KB * sizeof(VV) + work;
+      const size_t sm = staged <= (size_t)SMEM_LIMIT ? staged : work;
+      const int panels = (pmax + GJ_KB - 1) / GJ_KB;
+      const double per = flops / (2.0 * panels + 2.0);
+      launch(cls, per, 0.0, [&] { inv_scale_kernel<TT><<<(unsigned)count, 256, 0, s>>>(dinv + first); });
+      for (int k0 = 0; k0 < pmax; k0 += GJ_KB) {
+        launch(cls, per, 0.0, [&] {
+          inv_panel_kernel<TT><<<(unsigned)count, 256, sm, s>>>(dinv + first, k0, tol, perturb, (int)sm);
+        });
+        const unsigned rt = (unsigned)((nmax + 63) / 64);
+        in_pieces(count, [&](size_t f0, size_t c) {
+          launch(cls, per * c / count, 0.0, [&] {
+            inv_update_kernel<TT><<<dim3(rt, rt, (unsigned)c), 256, 0, s>>>(dinv + first + f0, k0);
+          });
+        });
+      }
+      launch(cls, per, 0.0, [&] { inv_finish_kernel<TT><<<(unsigned)count, 256, 0, s>>>(dinv + first, djobs, status); });
+    };
+
     CK(cudaEventRecord(ctx->ev0, s));
-    int64_t launches = 0;
+    const int perturb = mixed ? 1 : 0;
+    // Factorization, level by level.
     for (int L = 0; L < max_levels; ++L) {
       const Level& lv = levels[L];
       if (lv.small_n) {
-        size_t sm = small_smem(lv.max_small_n, vb);
-        small_front_kernel<T, false><<<(unsigned)lv.small_n, 256, sm, s>>>(djobs, dtasks + lv.small0, Prec<T>::tol);
-        ++launches;
+        const size_t sm = small_smem(lv.max_small_n, vb);
+        launch(K_SMALL, lv.small_flops, lv.small_bytes, [&] {
+          if (mixed)
+            small_front_kernel<T, true><<<(unsigned)lv.small_n, 256, sm, s>>>(djobs, dtasks + lv.small0, Prec<T>::tol,
+                                                                              perturb, pert);
+          else
+            small_front_kernel<T, false><<<(unsigned)lv.small_n, 256, sm, s>>>(djobs, dtasks + lv.small0,
+                                                                               Prec<T>::tol, perturb, pert);
+        });
       }
       if (lv.large_n) {
         const Task* lt = dtasks + lv.large0;
         const int mt = (lv.max_large_n + 63) / 64;
-        const size_t sm = pivot_smem(lv.max_large_ne, vb);
         in_pieces(lv.large_n, [&](size_t f0, size_t c) {
-          assemble_kernel<T><<<dim3((lv.max_large_n + 31) / 32, (unsigned)c), 256, 0, s>>>(djobs, lt + f0, 0);
-          ++launches;
-        });
-        pivot_block_kernel<T><<<(unsigned)lv.large_n, 1024, sm, s>>>(djobs, lt, Prec<T>::tol, (int)sm, 0, status);
-        ++launches;
-        for (int mode = 0; mode < 2; ++mode)
-          in_pieces(lv.large_n, [&](size_t f0, size_t c) {
-            front_gemm_kernel<T><<<dim3(mt, mt, (unsigned)c), 256, 0, s>>>(djobs, lt + f0, xs, mode);
-            ++launches;
+          launch(K_ASSEMBLE, 0.0, lv.asm_bytes * c / lv.large_n, [&] {
+            assemble_kernel<T, T><<<dim3((lv.max_large_n + 31) / 32, (unsigned)c), 256, 0, s>>>(djobs, lt + f0, 0);
           });
-        in_pieces(lv.large_n, [&](size_t f0, size_t c) {
-          store_x_kernel<T><<<dim3(8, (unsigned)c), 256, 0, s>>>(djobs, lt + f0, xs);
-          ++launches;
         });
+        const size_t ninv = (L + 1 < max_levels ? levels[L + 1].inv0 : rinv0) - lv.inv0;
+        inverse(T{}, lv.inv0, ninv, lv.max_large_n, lv.max_large_ne, Prec<T>::tol, perturb, K_PIVOT,
+                lv.inv_flops + lv.gemm0_flops + lv.gemm1_flops);
+        (void)mt;
+        (void)xs;
       }
-      CK(cudaGetLastError());
     }
-    // Roots: always complex f64 for DOUBLE; the fronts' precision otherwise.
-    {
-      const Task* rt = dtasks + root0;
-      in_pieces(cj, [&](size_t f0, size_t c) {
-        assemble_kernel<T><<<dim3((max_root + 31) / 32, (unsigned)c), 256, 0, s>>>(djobs, rt + f0, 1);
-        ++launches;
+    CK(cudaEventRecord(ctx->evf, s));
+    // Root front in TR, then its inverse. The reference's root LU has no stability test (a zero
+    // pivot means a singular root); in mixed precision tiny root pivots are perturbed like the
+    // fronts' (the refinement corrects).
+    const Task* rt = dtasks + root0;
+    in_pieces(cj, [&](size_t f0, size_t c) {
+      launch(K_ROOT_ASM, 0.0, 0.0, [&] {
+        assemble_kernel<T, TR><<<dim3((max_root + 31) / 32, (unsigned)c), 256, 0, s>>>(djobs, rt + f0, 1);
       });
-      const size_t sm = pivot_smem(max_root, vb);
-      pivot_block_kernel<T><<<(unsigned)cj, 1024, sm, s>>>(djobs, rt, 0.0, (int)sm, 1, status);
-      ++launches;
+    });
+    inverse(TR{}, rinv0, cj, max_root, max_root, mixed ? Prec<T>::tol * 1e-2 : 0.0, perturb, K_ROOT_INV, root_flops);
+    CK(cudaEventRecord(ctx->evr, s));
+    std::vector<double> th(cj), eh(cj, 0.0);
+    std::vector<int32_t> sh(cj, ST_OK), ih(cj, 0);
+    if (!mixed) {
       in_pieces(cj, [&](size_t f0, size_t c) {
-        trace_kernel<T><<<dim3((unsigned)parts_per_job, (unsigned)c), 256, 0, s>>>(djobs + f0, part + f0 * parts_per_job,
-                                                                                 (int)parts_per_job);
-        ++launches;
+        launch(K_TRACE, trace_flops * c / cj, 0.0, [&] {
+          trace_kernel<TR><<<dim3((unsigned)parts_per_job, (unsigned)c), 256, 0, s>>>(djobs + f0, part + f0 * parts_per_job,
+                                                                                    (int)parts_per_job);
+        });
       });
-      trace_finish_kernel<<<(unsigned)((cj + 127) / 128), 128, 0, s>>>(part, (int)parts_per_job, (int)cj, tdev, status);
-      ++launches;
-      CK(cudaGetLastError());
+      launch(K_TRACE, 0.0, 0.0, [&] {
+        trace_finish_kernel<<<(unsigned)((cj + 127) / 128), 128, 0, s>>>(part, (int)parts_per_job, (int)cj, tdev, status);
+      });
+      CK(cudaEventRecord(ctx->ev1, s));
+      CK(cudaMemcpyAsync(th.data(), tdev, cj * sizeof(double), cudaMemcpyDeviceToHost, s));
+    } else {
+      if constexpr (std::is_same<T, float>::value && std::is_same<TR, float>::value) {
+        std::vector<LevelRange> lr;
+        for (const Level& lv : levels) lr.push_back({lv.small0, lv.small_n + lv.large_n, lv.max_n});
+        refine(ctx, sys, specs, begin, cj, lr, max_root, dtasks, jd, arena, arena_off, rarena, root_off, launch, th,
+               eh, sh, ih);
+      }
     }
-    CK(cudaEventRecord(ctx->ev1, s));
-    std::vector<double> th(cj);
-    std::vector<int32_t> sh(cj);
+    std::vector<int32_t> sdev(cj);
     std::vector<uint8_t> fh(foff);
-    CK(cudaMemcpyAsync(th.data(), tdev, cj * sizeof(double), cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(sh.data(), status, cj * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(sdev.data(), status, cj * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(fh.data(), fail, foff, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    float ms = 0.f;
+    launch.collect();
+    float ms = 0.f, mf = 0.f, mr = 0.f;
     CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    CK(cudaEventElapsedTime(&mf, ctx->ev0, ctx->evf));
+    CK(cudaEventElapsedTime(&mr, ctx->evf, ctx->evr));
     ctx->last_ms += ms;
-    ctx->last_launches += launches;
+    ctx->factor_ms += mf;
+    ctx->root_ms += mr;
+    ctx->tail_ms += ms - mf - mr;
+    std::vector<int> ph(cj, 0);
+    CK(cudaMemcpy(ph.data(), pert, cj * sizeof(int), cudaMemcpyDeviceToHost));
+    for (size_t j = 0; j < cj; ++j) ctx->refine_iters = std::max<int64_t>(ctx->refine_iters, ih[j]);
     for (size_t j = 0; j < cj; ++j) {
-      t_out[begin + j] = th[j];
-      int32_t st = sh[j];
+      JobOut& o = out[begin + j];
+      o.t = th[j];
+      o.err = eh[j];
+      o.iters = ih[j];
+      int32_t st = sdev[j] != ST_OK ? sdev[j] : sh[j];
+      if (st == ST_OK && !std::isfinite(o.t)) st = ST_NONFINITE;
       const size_t nf = specs[begin + j].plan->host.fronts.size();
       bool delayed = false;
       for (size_t k = 0; k < nf; ++k) delayed |= fh[fail_off[j] + k] != 0;
-      if (delayed) st = ST_PIVOT_DELAYED;
-      st_out[begin + j] = st;
-      if (fails && delayed) (*fails)[begin + j].assign(fh.begin() + fail_off[j], fh.begin() + fail_off[j] + nf);
+      if (delayed && !mixed) {
+        st = ST_PIVOT_DELAYED;
+        o.fail.assign(fh.begin() + fail_off[j], fh.begin() + fail_off[j] + nf);
+      } else if (delayed) {
+        st = ST_REFINE_STALLED;
+      }
+      o.status = st;
+      o.perturbed = ph[j];
     }
     begin = end;
   }
+  ctx->last_launches += launch.launches;
+  ctx->region_launches += launch.launches;
 }
 
-template <typename T>
-void solve_jobs(caroli_ctx* ctx, System* sys, std::vector<JobSpec>& specs, std::vector<double>& t,
-                std::vector<int32_t>& st) {
-  std::vector<std::vector<uint8_t>> fails;
-  run_jobs<T>(ctx, sys, specs, t, st, &fails);
-  // Jobs with refused pivots: re-plan with those fronts delayed and run them again, one by one.
-  for (size_t j = 0; j < specs.size(); ++j) {
-    if (st[j] != ST_PIVOT_DELAYED) continue;
-    const BlockTree& tree = sys->trees[specs[j].block];
-    std::vector<uint8_t> delayed(tree.nodes.size(), 0);
-    for (size_t k = 0; k < tree.nodes.size(); ++k) delayed[k] = fails[j][k];
-    for (size_t round = 0; round <= tree.nodes.size(); ++round) {
-      DevPlan dp;
-      dp.host = make_plan(sys->desc, tree, delayed);
-      dp.upload(ctx->stream);
-      std::vector<JobSpec> one{{specs[j].block, specs[j].slot, specs[j].config, &dp}};
-      std::vector<double> t1;
-      std::vector<int32_t> s1;
-      std::vector<std::vector<uint8_t>> f1;
-      run_jobs<T>(ctx, sys, one, t1, s1, &f1);
-      dp.release();
-      t[j] = t1[0];
-      st[j] = s1[0];
-      if (s1[0] != ST_PIVOT_DELAYED) break;
-      bool grew = false;
+// Runs jobs; those with refused pivots are re-planned with the refusing fronts delayed to their
+// parents and re-run together, round after round, until none refuses (nested.rs:356-373).
+template <typename T, typename TR>
+void solve_with_delays(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, Mode mode,
+                       std::vector<JobOut>& out) {
+  run_jobs<T, TR>(ctx, sys, specs, mode, out);
+  std::vector<size_t> pending;
+  std::vector<std::vector<uint8_t>> delayed(specs.size());
+  for (size_t j = 0; j < specs.size(); ++j)
+    if (out[j].status == ST_PIVOT_DELAYED) {
+      pending.push_back(j);
+      delayed[j].assign(sys->trees[specs[j].block].nodes.size(), 0);
+    }
+  for (int round = 0; !pending.empty() && round < 64; ++round) {
+    std::vector<std::unique_ptr<DevPlan>> plans;
+    std::vector<JobSpec> again;
+    for (size_t j : pending) {
+      const BlockTree& tree = sys->trees[specs[j].block];
       for (size_t k = 0; k < tree.nodes.size(); ++k)
-        if (f1[0][k] && !delayed[k]) { delayed[k] = 1; grew = true; }
-      if (!grew) { st[j] = ST_SINGULAR; break; }
+        if (k < out[j].fail.size() && out[j].fail[k]) delayed[j][k] = 1;
+      auto dp = std::make_unique<DevPlan>();
+      dp->host = make_plan(sys->desc, tree, delayed[j]);
+      dp->upload(ctx->stream);
+      again.push_back({specs[j].block, specs[j].slot, specs[j].config, dp.get()});
+      plans.push_back(std::move(dp));
+    }
+    std::vector<JobOut> res;
+    run_jobs<T, TR>(ctx, sys, again, mode, res);
+    for (auto& p : plans) p->release();
+    std::vector<size_t> next;
+    for (size_t q = 0; q < pending.size(); ++q) {
+      const size_t j = pending[q];
+      bool grew = false;
+      if (res[q].status == ST_PIVOT_DELAYED)
+        for (size_t k = 0; k < res[q].fail.size() && k < delayed[j].size(); ++k)
+          if (res[q].fail[k] && !delayed[j][k]) grew = true;
+      out[j] = res[q];
+      if (res[q].status == ST_PIVOT_DELAYED) {
+        if (grew) next.push_back(j);
+        else out[j].status = ST_SINGULAR;
+      }
+    }
+    pending.swap(next);
+  }
+}
+
+void solve_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, Mode mode, std::vector<JobOut>& out) {
+  if (mode == MODE_DOUBLE) {
+    solve_with_delays<double, double>(ctx, sys, specs, mode, out);
+  } else if (mode == MODE_SINGLE) {
+    solve_with_delays<float, double>(ctx, sys, specs, mode, out);
+  } else {
+    run_jobs<float, float>(ctx, sys, specs, mode, out);
+    // Points the reduced precision could not resolve are computed in double precision
+    // (precision.rs:102-115 does the same for failed points).
+    std::vector<JobSpec> again;
+    std::vector<size_t> idx;
+    for (size_t j = 0; j < specs.size(); ++j)
+      if (out[j].status != ST_OK) {
+        again.push_back(specs[j]);
+        idx.push_back(j);
+      }
+    if (!again.empty()) {
+      const double ms = ctx->last_ms;
+      std::vector<JobOut> res;
+      solve_with_delays<double, double>(ctx, sys, again, MODE_DOUBLE, res);
+      ctx->fallbacks += (int64_t)again.size();
+      (void)ms;
+      for (size_t q = 0; q < idx.size(); ++q) {
+        const int32_t it = out[idx[q]].iters, pt = out[idx[q]].perturbed, st = out[idx[q]].status;
+        out[idx[q]] = res[q];
+        out[idx[q]].err = 0.0;
+        out[idx[q]].iters = it;
+        out[idx[q]].perturbed = pt;
+        if (out[idx[q]].status == ST_OK) out[idx[q]].status = 100 + st;  // recomputed in double
+      }
     }
   }
+}
+
+// W with W W^† = Γ for a Hermitian positive semi-definite Γ (m x m, column-major interleaved):
+// pivoted Cholesky, stopped when the largest remaining diagonal is below 1e-15 of the largest
+// diagonal, just above the rounding noise of Γ = i(Σ - Σ^†). (gamma_root, nested.rs:1036-1047,
+// cuts eigenvalues at 1e-12; a Cholesky residual is not aligned with small eigenvalues, so its
+// cut must be tighter for T = Tr[Γ_L G W W^† G^†] to keep the reference's full-Γ trace to 1e-12.)
+// Returns the number of columns (channels); w is m x columns.
+int gamma_factor(const std::vector<double>& g, size_t m, std::vector<double>& w) {
+  std::vector<double> dres(m);
+  double top = 0.0;
+  for (size_t i = 0; i < m; ++i) {
+    dres[i] = g[2 * (i + i * m)];
+    top = std::max(top, dres[i]);
+  }
+  std::vector<uint8_t> used(m, 0);
+  std::vector<double> cols;  // interleaved, m per column
+  const double tol = 1e-15 * top;
+  for (size_t k = 0; k < m; ++k) {
+    size_t p = m;
+    double best = tol;
+    for (size_t i = 0; i < m; ++i)
+      if (!used[i] && dres[i] > best) { best = dres[i]; p = i; }
+    if (p == m) break;
+    used[p] = 1;
+    const double piv = std::sqrt(dres[p]);
+    std::vector<double> col(2 * m);
+    for (size_t i = 0; i < m; ++i) {
+      double re = g[2 * (i + p * m)], im = g[2 * (i + p * m) + 1];
+      for (size_t t = 0; t < k; ++t) {
+        const double* c = &cols[2 * m * t];
+        // L[i,t] conj(L[p,t])
+        re -= c[2 * i] * c[2 * p] + c[2 * i + 1] * c[2 * p + 1];
+        im -= c[2 * i + 1] * c[2 * p] - c[2 * i] * c[2 * p + 1];
+      }
+      col[2 * i] = used[i] && i != p ? 0.0 : re / piv;
+      col[2 * i + 1] = used[i] && i != p ? 0.0 : im / piv;
+    }
+    col[2 * p + 1] = 0.0;
+    for (size_t i = 0; i < m; ++i)
+      if (!used[i]) dres[i] -= col[2 * i] * col[2 * i] + col[2 * i + 1] * col[2 * i + 1];
+    cols.insert(cols.end(), col.begin(), col.end());
+  }
+  w = cols;
+  return (int)(cols.size() / (2 * m));
 }
 
 double2* upload_c64(const double* host, size_t count, cudaStream_t s) {
@@ -408,11 +929,19 @@ int caroli_ctx_create(int device_ordinal, caroli_ctx** out) {
     CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
     CK(cudaEventCreate(&ctx->ev0));
     CK(cudaEventCreate(&ctx->ev1));
+    CK(cudaEventCreate(&ctx->evf));
+    CK(cudaEventCreate(&ctx->evr));
+    CK(cudaEventCreate(&ctx->reg0));
+    CK(cudaEventCreate(&ctx->reg1));
     size_t free_b = 0, total_b = 0;
     CK(cudaMemGetInfo(&free_b, &total_b));
     ctx->mem_budget = free_b / 2;
     for (auto* k : {(const void*)small_front_kernel<double, false>, (const void*)small_front_kernel<float, false>,
-                    (const void*)pivot_block_kernel<double>, (const void*)pivot_block_kernel<float>})
+                    (const void*)small_front_kernel<double, true>, (const void*)small_front_kernel<float, true>,
+                    (const void*)pivot_block_kernel<double>, (const void*)pivot_block_kernel<float>,
+                    (const void*)inv_panel_kernel<double>, (const void*)inv_panel_kernel<float>,
+                    (const void*)refine_forward_kernel, (const void*)refine_backward_kernel,
+                    (const void*)refine_root_kernel})
       CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_LIMIT));
   } catch (const CudaError& e) {
     return CAROLI_ECUDA;
@@ -428,6 +957,14 @@ void caroli_ctx_destroy(caroli_ctx* ctx) {
   ctx->systems.clear();
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->evf) cudaEventDestroy(ctx->evf);
+  if (ctx->evr) cudaEventDestroy(ctx->evr);
+  if (ctx->reg0) cudaEventDestroy(ctx->reg0);
+  if (ctx->reg1) cudaEventDestroy(ctx->reg1);
+  for (auto& e : ctx->probe_events) {
+    cudaEventDestroy(e.first);
+    cudaEventDestroy(e.second);
+  }
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -485,6 +1022,22 @@ int caroli_plan_upload(caroli_ctx* ctx, int64_t n, const int64_t* row_ptr, const
       dp->host = make_plan(d, sys->trees[b], {});
       dp->upload(ctx->stream);
       sys->plans.push_back(std::move(dp));
+      const BlockTree& t = sys->trees[b];
+      DevBlock B;
+      B.nblk = (int32_t)t.orbitals.size();
+      B.nnz = (int64_t)t.csr_col.size();
+      std::vector<int32_t> sl(B.nblk, -1), sr(B.nblk, -1);
+      for (size_t a = 0; a < t.left_local.size(); ++a) sl[t.left_local[a]] = (int32_t)a;
+      for (size_t a = 0; a < t.right_local.size(); ++a) sr[t.right_local[a]] = (int32_t)a;
+      B.csr_ptr = upload_vec(t.csr_ptr, ctx->stream);
+      B.csr_col = upload_vec(t.csr_col, ctx->stream);
+      B.csr_q = upload_vec(t.csr_q, ctx->stream);
+      B.slice_l = upload_vec(sl, ctx->stream);
+      B.slice_r = upload_vec(sr, ctx->stream);
+      B.left_local = upload_vec(t.left_local, ctx->stream);
+      B.right_local = upload_vec(t.right_local, ctx->stream);
+      CK(cudaStreamSynchronize(ctx->stream));
+      sys->blocks.push_back(B);
     }
     ctx->systems.push_back(std::move(sys));
     *plan_id = (int)ctx->systems.size() - 1;
@@ -539,10 +1092,11 @@ int caroli_sigma_upload(caroli_ctx* ctx, int plan_id, int slot, double energy, c
     CK(cudaSetDevice(ctx->device));
     if ((int)sys->slots.size() <= slot) sys->slots.resize(slot + 1);
     SigmaSlot& sg = sys->slots[slot];
-    for (auto* v : {&sg.sl, &sg.sr, &sg.gl, &sg.gr}) {
+    for (auto* v : {&sg.sl, &sg.sr, &sg.gl, &sg.gr, &sg.wr}) {
       for (auto* p : *v) cudaFree(p);
       v->clear();
     }
+    sg.channels.clear();
     for (size_t b = 0; b < sys->plans.size(); ++b) {
       const FrontPlan& p = sys->plans[b]->host;
       const size_t nl = p.nl, nr = p.nr;
@@ -559,6 +1113,10 @@ int caroli_sigma_upload(caroli_ctx* ctx, int plan_id, int slot, double energy, c
       };
       gamma(sigma_l[b], nl, gl);
       gamma(sigma_r[b], nr, gr);
+      std::vector<double> wr;
+      const int ch = gamma_factor(gr, nr, wr);
+      sg.channels.push_back(ch);
+      sg.wr.push_back(upload_c64(wr.data(), nr * (size_t)ch, ctx->stream));
       sg.sl.push_back(upload_c64(sigma_l[b], nl * nl, ctx->stream));
       sg.sr.push_back(upload_c64(sigma_r[b], nr * nr, ctx->stream));
       sg.gl.push_back(upload_c64(gl.data(), nl * nl, ctx->stream));
@@ -590,25 +1148,36 @@ int caroli_solve_batch(caroli_ctx* ctx, int plan_id, int count, const int32_t* s
     CK(cudaSetDevice(ctx->device));
     ctx->last_ms = 0.0;
     ctx->last_launches = 0;
+    ctx->factor_ms = ctx->root_ms = ctx->tail_ms = 0.0;
     const int nb = (int)sys->plans.size();
     std::vector<JobSpec> specs;
     specs.reserve((size_t)count * nb);
     for (int i = 0; i < count; ++i)
       for (int b = 0; b < nb; ++b) specs.push_back({b, slots[i], configs[i], sys->plans[b].get()});
-    std::vector<double> tj;
-    std::vector<int32_t> sj;
-    if (precision == CAROLI_DOUBLE) solve_jobs<double>(ctx, sys, specs, tj, sj);
-    else solve_jobs<float>(ctx, sys, specs, tj, sj);
+    std::vector<JobOut> jo;
+    ctx->fallbacks = 0;
+    ctx->refine_iters = 0;
+    solve_jobs(ctx, sys, specs, (Mode)precision, jo);
+    ctx->job_iters.clear();
+    ctx->job_perturbed.clear();
+    ctx->job_status.clear();
+    for (const JobOut& o : jo) {
+      ctx->job_iters.push_back(o.iters);
+      ctx->job_perturbed.push_back(o.perturbed);
+      ctx->job_status.push_back(o.status);
+    }
     for (int i = 0; i < count; ++i) {
-      double sum = 0.0;
+      double sum = 0.0, e = 0.0;
       int32_t st = ST_OK;
       for (int b = 0; b < nb; ++b) {
-        sum += tj[(size_t)i * nb + b];
-        if (st == ST_OK) st = sj[(size_t)i * nb + b];
+        const JobOut& o = jo[(size_t)i * nb + b];
+        sum += o.t;
+        e += o.err;
+        if (st == ST_OK) st = o.status >= 100 ? ST_OK : o.status;
       }
       t[i] = sum;
       status[i] = st;
-      if (err) err[i] = 0.0;
+      if (err) err[i] = e;
     }
     return CAROLI_OK;
   } catch (const CudaError& e) {
@@ -617,6 +1186,75 @@ int caroli_solve_batch(caroli_ctx* ctx, int plan_id, int count, const int32_t* s
   } catch (const std::exception& e) {
     return fail_with(ctx, CAROLI_EINVAL, e.what());
   }
+}
+
+int caroli_last_phases(const caroli_ctx* ctx, double* factor_ms, double* root_ms, double* tail_ms) {
+  if (!ctx) return CAROLI_EINVAL;
+  if (factor_ms) *factor_ms = ctx->factor_ms;
+  if (root_ms) *root_ms = ctx->root_ms;
+  if (tail_ms) *tail_ms = ctx->tail_ms;
+  return CAROLI_OK;
+}
+
+int caroli_last_job_info(const caroli_ctx* ctx, int64_t capacity, int32_t* iters, int32_t* perturbed,
+                         int32_t* status, int64_t* count) {
+  if (!ctx) return CAROLI_EINVAL;
+  const int64_t n = (int64_t)ctx->job_iters.size();
+  if (count) *count = n;
+  for (int64_t j = 0; j < std::min(n, capacity); ++j) {
+    if (iters) iters[j] = ctx->job_iters[j];
+    if (perturbed) perturbed[j] = ctx->job_perturbed[j];
+    if (status) status[j] = ctx->job_status[j];
+  }
+  return CAROLI_OK;
+}
+
+int caroli_last_stats(const caroli_ctx* ctx, int64_t* fallbacks, int64_t* max_refine_iters) {
+  if (!ctx) return CAROLI_EINVAL;
+  if (fallbacks) *fallbacks = ctx->fallbacks;
+  if (max_refine_iters) *max_refine_iters = ctx->refine_iters;
+  return CAROLI_OK;
+}
+
+int caroli_kernel_classes(void) { return K_COUNT; }
+
+const char* caroli_kernel_class_name(int k) { return (k >= 0 && k < K_COUNT) ? kclass_names[k] : ""; }
+
+int caroli_probe_kernel(caroli_ctx* ctx, int kclass) {
+  if (!ctx || kclass < -1 || kclass >= K_COUNT) return CAROLI_EINVAL;
+  ctx->probe = kclass;
+  return CAROLI_OK;
+}
+
+int caroli_kernel_stats(caroli_ctx* ctx, int kclass, int64_t* launches, double* flops, double* bytes, double* ms,
+                        int reset) {
+  if (!ctx || kclass < 0 || kclass >= K_COUNT) return CAROLI_EINVAL;
+  KStat& st = ctx->kstat[kclass];
+  if (launches) *launches = st.launches;
+  if (flops) *flops = st.flops;
+  if (bytes) *bytes = st.bytes;
+  if (ms) *ms = st.ms;
+  if (reset) st = KStat{};
+  return CAROLI_OK;
+}
+
+int caroli_region_begin(caroli_ctx* ctx) {
+  if (!ctx) return CAROLI_EINVAL;
+  cudaSetDevice(ctx->device);
+  ctx->region_launches = 0;
+  return cudaEventRecord(ctx->reg0, ctx->stream) == cudaSuccess ? CAROLI_OK : CAROLI_ECUDA;
+}
+
+int caroli_region_end(caroli_ctx* ctx, double* device_ms, int64_t* launches) {
+  if (!ctx) return CAROLI_EINVAL;
+  cudaSetDevice(ctx->device);
+  if (cudaEventRecord(ctx->reg1, ctx->stream) != cudaSuccess || cudaEventSynchronize(ctx->reg1) != cudaSuccess)
+    return CAROLI_ECUDA;
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, ctx->reg0, ctx->reg1) != cudaSuccess) return CAROLI_ECUDA;
+  if (device_ms) *device_ms = ms;
+  if (launches) *launches = ctx->region_launches;
+  return CAROLI_OK;
 }
 
 int caroli_last_timing(const caroli_ctx* ctx, double* device_ms, int64_t* launches) {

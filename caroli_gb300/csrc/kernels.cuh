@@ -2,10 +2,10 @@
 //
 // Every front lives in a per-solve arena as an n x n column-major complex matrix, interleaved
 // (re, im). After elimination of its ne leading variables a front holds
-//     [ F11^-1 | X = F11^-1 F12 ]
-//     [ F21    | S = F22 - F21 X ]
+//     [ F11^-1          | X = F11^-1 F12 ]
+//     [ W = -F21 F11^-1 | S = F22 - F21 X ]
 // The parent gathers S (the trailing nb x nb block) through an index map; a refinement solve
-// reads F11^-1, X and F21 (forward: t = F11^-1 r_e, r_b -= F21 t; backward: x_e = t - X x_b).
+// reads F11^-1, X and W (forward: t = F11^-1 r_e, r_b += W r_e; backward: x_e = t - X x_b).
 //
 // The elimination is the reference's partial-pivoting Schur step (nested.rs:1167-1223,
 // caroli-dense/src/field.rs:79-105) written as an in-place Gauss-Jordan sweep: the pivots (and so
@@ -34,7 +34,8 @@ struct JobDesc {
   const int32_t* maps;
   const uint8_t* own;
   const Entry* entries;
-  void* arena;
+  void* arena;             // tree fronts, in the precision of the fronts
+  void* root_arena;        // the root front (m x m), in the precision of the root
   const double2* vals;     // H values of the configuration (on the system's pattern)
   const double2* sigma_l;  // nl x nl, column-major
   const double2* sigma_r;  // nr x nr
@@ -145,18 +146,21 @@ __device__ __forceinline__ int block_argmax(double v, int i, double* redv, int* 
 // ---- assembly -----------------------------------------------------------------------------------
 // Element (i, j) of a front before its H entries: the children's handed blocks through their
 // index maps, plus z on the diagonal of the own separator, minus Σ on the root.
-template <typename T>
+template <typename TC, typename T = TC>
 __device__ __forceinline__ typename Cx<T>::V gather(const JobDesc& J, const FrontDesc& f, int i, int j,
                                                      bool is_root) {
   using V = typename Cx<T>::V;
-  const V* arena = static_cast<const V*>(J.arena);
+  using VC = typename Cx<TC>::V;
+  const VC* arena = static_cast<const VC*>(J.arena);
   V v = cx<V>(0.0, 0.0);
   for (int c = 0; c < f.nchild; ++c) {
     const int32_t* map = J.maps + f.map_off[c];
     int a = map[i], b = map[j];
     if (a >= 0 && b >= 0) {
       const FrontDesc& cf = J.fronts[f.child[c]];
-      v = cadd(v, arena[cf.arena_off + f.child_off[c] + a + (int64_t)b * cf.n]);
+      VC w = arena[cf.arena_off + f.child_off[c] + a + (int64_t)b * cf.n];
+      v.x += (T)w.x;
+      v.y += (T)w.y;
     }
   }
   if (i == j && J.own[f.own_off + i]) v.x += (T)J.energy;
@@ -185,12 +189,17 @@ __device__ __forceinline__ void apply_entries(const JobDesc& J, const FrontDesc&
 
 // ---- Gauss-Jordan sweep -------------------------------------------------------------------------
 // In-place sweep of the leading ne pivots of an n x n matrix F (column-major, leading dimension
-// ld), pivot rows restricted to [k, ne). Rows >= ne only keep the columns >= ne they need (the
-// Schur complement). On exit F[0:ne, 0:ne] = F11^-1 (columns unpermuted), F[0:ne, ne:n] = X,
-// F[ne:n, ne:n] = S. Returns false when a pivot is not above tol * max|F11| (uniform in the block).
+// ld), pivot rows restricted to [k, ne). On exit (columns of the first block unpermuted)
+//   F[0:ne, 0:ne] = F11^-1, F[0:ne, ne:n] = X = F11^-1 F12,
+//   F[ne:n, 0:ne] = W = -F21 F11^-1, F[ne:n, ne:n] = S = F22 - F21 X.
+// Returns false when a pivot is not above tol * max|F11| (uniform in the block).
+// With `perturb`, a pivot below the threshold is replaced by tol * max|F11| in its own direction
+// (static pivoting, counted in *perturbed) instead of refusing the block: the factors then only
+// precondition an iterative refinement that removes the perturbation.
 template <typename T>
 __device__ bool gj_sweep(typename Cx<T>::V* F, int64_t ld, int n, int ne, double tol, typename Cx<T>::V* prow,
-                         typename Cx<T>::V* colk, int* piv, double* redv, int* redi) {
+                         typename Cx<T>::V* colk, int* piv, double* redv, int* redi, bool perturb = false,
+                         int* perturbed = nullptr) {
   using V = typename Cx<T>::V;
   const int tid = threadIdx.x, nt = blockDim.x;
   double local = 0.0;
@@ -209,7 +218,19 @@ __device__ bool gj_sweep(typename Cx<T>::V* F, int64_t ld, int n, int ne, double
     }
     double big;
     int p = block_argmax(best, bi, redv, redi, &big);
-    if (!(big > thresh) || p >= ne) return false;
+    if (!(big > thresh) || p >= ne) {
+      if (!perturb) return false;
+      // NaN or an empty column: nothing sensible to perturb.
+      if (!(big >= 0.0) || !(scale2 > 0.0) || p >= ne) return false;
+      if (tid == 0) {
+        V& d = F[p + k * ld];
+        const double mag = sqrt(big), target = tol * sqrt(scale2);
+        if (mag > 0.0) { d.x = (T)(d.x / mag * target); d.y = (T)(d.y / mag * target); }
+        else { d.x = (T)target; d.y = (T)0; }
+        if (perturbed) atomicAdd(perturbed, 1);
+      }
+      __syncthreads();
+    }
     if (tid == 0) piv[k] = p;
     if (p != k)
       for (int j = tid; j < n; j += nt) {
@@ -224,7 +245,6 @@ __device__ bool gj_sweep(typename Cx<T>::V* F, int64_t ld, int n, int ne, double
     __syncthreads();
     for (int64_t idx = tid; idx < (int64_t)n * n; idx += nt) {
       const int i = (int)(idx % n), j = (int)(idx / n);
-      if (i >= ne && j <= k) continue;
       V* d = &F[i + j * ld];
       if (i == k) *d = prow[j];
       else if (j == k) *d = cmul(cx<V>(-colk[i].x, -colk[i].y), inv);
@@ -236,7 +256,7 @@ __device__ bool gj_sweep(typename Cx<T>::V* F, int64_t ld, int n, int ne, double
   for (int k = ne - 1; k >= 0; --k) {
     int p = piv[k];
     if (p != k)
-      for (int i = tid; i < ne; i += nt) {
+      for (int i = tid; i < n; i += nt) {
         V a = F[i + k * ld];
         F[i + k * ld] = F[i + p * ld];
         F[i + p * ld] = a;
@@ -249,7 +269,8 @@ __device__ bool gj_sweep(typename Cx<T>::V* F, int64_t ld, int n, int ne, double
 // ---- small fronts: assembly and elimination in shared memory, one CTA per front ---------------
 template <typename T, bool KEEP>
 __global__ void __launch_bounds__(256) small_front_kernel(const JobDesc* __restrict__ jobs,
-                                                          const Task* __restrict__ tasks, double tol) {
+                                                          const Task* __restrict__ tasks, double tol, int perturb,
+                                                          int* __restrict__ perturbed) {
   using V = typename Cx<T>::V;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const Task t = tasks[blockIdx.x];
@@ -275,19 +296,13 @@ __global__ void __launch_bounds__(256) small_front_kernel(const JobDesc* __restr
     for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) out[idx] = F[idx % n + (idx / n) * ld];
     return;
   }
-  if (KEEP)
-    for (int idx = threadIdx.x; idx < (n - ne) * ne; idx += blockDim.x) {
-      int i = ne + idx % (n - ne), j = idx / (n - ne);
-      out[i + (int64_t)j * n] = F[i + j * ld];
-    }
-  bool ok = gj_sweep<T>(F, ld, n, ne, tol, prow, colk, piv, redv, redi);
+  bool ok = gj_sweep<T>(F, ld, n, ne, tol, prow, colk, piv, redv, redi, perturb != 0, perturbed ? perturbed + t.job : nullptr);
   if (!ok) {
     if (threadIdx.x == 0) J.fail[t.front] = 1;
     return;
   }
   for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
     int i = idx % n, j = idx / n;
-    if (i >= ne && j < ne) continue;
     if (!KEEP && (i < ne || j < ne)) continue;
     out[i + (int64_t)j * n] = F[i + j * ld];
   }
@@ -295,7 +310,8 @@ __global__ void __launch_bounds__(256) small_front_kernel(const JobDesc* __restr
 
 // ---- large fronts -------------------------------------------------------------------------------
 // Assembly into the arena, a tile of 32 columns per CTA.
-template <typename T>
+// TC: precision of the children, T: of this front (the root may be wider than its children).
+template <typename TC, typename T>
 __global__ void __launch_bounds__(256) assemble_kernel(const JobDesc* __restrict__ jobs, const Task* __restrict__ tasks,
                                                        int is_root) {
   using V = typename Cx<T>::V;
@@ -306,10 +322,10 @@ __global__ void __launch_bounds__(256) assemble_kernel(const JobDesc* __restrict
   const int c0 = blockIdx.x * 32;
   if (c0 >= n) return;
   const int c1 = min(n, c0 + 32);
-  V* F = static_cast<V*>(J.arena) + f.arena_off;
+  V* F = is_root ? static_cast<V*>(J.root_arena) : static_cast<V*>(J.arena) + f.arena_off;
   for (int64_t idx = threadIdx.x; idx < (int64_t)n * (c1 - c0); idx += blockDim.x) {
     int i = (int)(idx % n), j = c0 + (int)(idx / n);
-    F[i + (int64_t)j * n] = gather<T>(J, f, i, j, is_root != 0);
+    F[i + (int64_t)j * n] = gather<TC, T>(J, f, i, j, is_root != 0);
   }
   __syncthreads();
   apply_entries<T>(J, f, F, n, c0, c1);
@@ -321,7 +337,8 @@ template <typename T>
 __global__ void __launch_bounds__(1024) pivot_block_kernel(const JobDesc* __restrict__ jobs,
                                                            const Task* __restrict__ tasks, double tol,
                                                            int smem_bytes, int is_root,
-                                                           int32_t* __restrict__ root_status) {
+                                                           int32_t* __restrict__ root_status, int perturb,
+                                                           int* __restrict__ perturbed) {
   using V = typename Cx<T>::V;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const Task t = tasks[blockIdx.x];
@@ -330,7 +347,7 @@ __global__ void __launch_bounds__(1024) pivot_block_kernel(const JobDesc* __rest
   const int n = f.n;
   const int ne = is_root ? n : f.ne;
   if (ne == 0) return;
-  V* G = static_cast<V*>(J.arena) + f.arena_off;
+  V* G = is_root ? static_cast<V*>(J.root_arena) : static_cast<V*>(J.arena) + f.arena_off;
   // Stage the block in shared memory only when it fits in what this launch allocated.
   const int64_t extra = 2 * (int64_t)ne * sizeof(V) + ((ne + 1) & ~1) * 4 + 32 * 8 + 32 * 4 + 16;
   const bool staged = (int64_t)ne * (ne | 1) * (int64_t)sizeof(V) + extra <= smem_bytes;
@@ -352,7 +369,7 @@ __global__ void __launch_bounds__(1024) pivot_block_kernel(const JobDesc* __rest
   int* piv = reinterpret_cast<int*>(colk + ne);
   double* redv = reinterpret_cast<double*>(piv + ((ne + 1) & ~1));
   int* redi = reinterpret_cast<int*>(redv + 32);
-  bool ok = gj_sweep<T>(F, ld, ne, ne, tol, prow, colk, piv, redv, redi);
+  bool ok = gj_sweep<T>(F, ld, ne, ne, tol, prow, colk, piv, redv, redi, perturb != 0, perturbed ? perturbed + t.job : nullptr);
   if (!ok) {
     if (threadIdx.x == 0) {
       if (is_root) root_status[t.job] = ST_SINGULAR;
@@ -466,7 +483,7 @@ __global__ void __launch_bounds__(256) trace_kernel(const JobDesc* __restrict__ 
   const JobDesc& J = jobs[blockIdx.y];
   const FrontDesc f = J.fronts[J.root];
   const int m = f.n, nl = J.nl, nr = J.nr;
-  const V* Gfull = static_cast<const V*>(J.arena) + f.arena_off;
+  const V* Gfull = static_cast<const V*>(J.root_arena);
   // G(i, j) = Ginv(nd + i, nd + rpos + j).
   auto G = [&](int i, int j) -> double2 {
     V v = Gfull[(J.nd + i) + (int64_t)(J.nd + J.rpos + j) * m];

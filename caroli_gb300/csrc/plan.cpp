@@ -116,6 +116,24 @@ std::vector<BlockTree> build_trees(const SystemDesc& d) {
     boundaries(d, t.nodes);
     t.left.assign(d.left + d.left_ptr[b], d.left + d.left_ptr[b + 1]);
     t.right.assign(d.right + d.right_ptr[b], d.right + d.right_ptr[b + 1]);
+    t.local.assign(d.n, -1);
+    for (int64_t o = 0; o < d.n; ++o)
+      if (d.labels[o] == b) {
+        t.local[o] = (int32_t)t.orbitals.size();
+        t.orbitals.push_back(o);
+      }
+    t.csr_ptr.push_back(0);
+    for (int64_t o : t.orbitals) {
+      for (int64_t q = d.row_ptr[o]; q < d.row_ptr[o + 1]; ++q) {
+        int32_t c = t.local[d.cols[q]];
+        if (c < 0) continue;  // an explicit zero coupling another block
+        t.csr_col.push_back(c);
+        t.csr_q.push_back(q);
+      }
+      t.csr_ptr.push_back((int32_t)t.csr_col.size());
+    }
+    for (int64_t o : t.left) t.left_local.push_back(t.local[o]);
+    for (int64_t o : t.right) t.right_local.push_back(t.local[o]);
     out.push_back(std::move(t));
   }
   return out;
@@ -200,6 +218,12 @@ FrontPlan make_plan(const SystemDesc& d, const BlockTree& t, const std::vector<u
     f.ent_cnt = (int64_t)p.entries.size() - f.ent_off;
     f.arena_off = arena;
     arena += (int64_t)f.n * f.n;
+    f.var_off = (int64_t)p.vidx.size();
+    for (int64_t v : vars) p.vidx.push_back(t.local[v]);
+    f.toff = p.sum_ne;
+    f.hoff = p.sum_nb;
+    p.sum_ne += f.ne;
+    p.sum_nb += f.n - f.ne;
     p.max_ne = std::max<int64_t>(p.max_ne, f.ne);
     p.max_n = std::max<int64_t>(p.max_n, f.n);
     handed[k] = delay ? vars : node.boundary;
@@ -248,6 +272,10 @@ FrontPlan make_plan(const SystemDesc& d, const BlockTree& t, const std::vector<u
   r.ent_cnt = (int64_t)p.entries.size() - r.ent_off;
   r.arena_off = arena;
   arena += (int64_t)r.n * r.n;
+  r.var_off = (int64_t)p.vidx.size();
+  for (int64_t v : vars) p.vidx.push_back(t.local[v]);
+  r.toff = p.sum_ne;
+  r.hoff = p.sum_nb;
   p.arena_elems = arena;
   p.max_n = std::max<int64_t>(p.max_n, r.n);
   p.vars[nn] = std::move(vars);

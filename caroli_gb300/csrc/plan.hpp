@@ -37,6 +37,9 @@ struct FrontDesc {
   int64_t ent_off;       // entries [ent_off, ent_off + ent_cnt) in `entries`
   int64_t ent_cnt;
   int64_t arena_off;     // element offset of the front inside a solve's arena (n x n, column-major)
+  int64_t var_off;       // block-local indices of the front's variables in `vidx` (n entries)
+  int64_t toff;          // row offset of the front's ne x c block in a solve's forward buffer
+  int64_t hoff;          // row offset of its (n - ne) x c handed block in a solve's update buffer
 };
 
 struct SystemDesc {
@@ -69,6 +72,14 @@ struct BlockTree {
   std::vector<TreeNode> nodes;  // post-order
   std::vector<int32_t> top;     // children of the root
   std::vector<int64_t> left, right;
+  // Block-local numbering (for refinement solves): the block's orbitals in increasing order, the
+  // local index of every orbital of the system (-1 outside the block), and H restricted to the
+  // block as CSR with local columns and the index of each entry in the system's value array.
+  std::vector<int64_t> orbitals;
+  std::vector<int32_t> local;
+  std::vector<int32_t> csr_ptr, csr_col;
+  std::vector<int64_t> csr_q;
+  std::vector<int32_t> left_local, right_local;
 };
 
 struct FrontPlan {
@@ -77,6 +88,8 @@ struct FrontPlan {
   std::vector<uint8_t> own;
   std::vector<Entry> entries;
   std::vector<std::vector<int64_t>> vars;  // variables of each front (elim then rest)
+  std::vector<int32_t> vidx;               // block-local index of each front variable
+  int64_t sum_ne = 0, sum_nb = 0;          // rows of the forward and update buffers
   int32_t levels = 0;                      // the root runs at level `levels - 1`
   int64_t arena_elems = 0;
   int32_t root = 0;

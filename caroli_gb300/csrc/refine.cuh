@@ -1,0 +1,578 @@
+// Mixed precision: FP64 iterative refinement of the whole block solve, preconditioned by the
+// complex-f32 multifrontal factors kept in the arena.
+//
+// For one block with A = z - H - Σ_L - Σ_R, the right-hand side is B = e_R W_R, where W_R W_R^† =
+// Γ_R (a rank-revealing factor of the right lead's broadening, one column per channel). Then
+// X = A^-1 B holds G W_R on every orbital, and T = Tr[Γ_L G_LR Γ_R G_LR^†] = Σ_j x_Lj^† Γ_L x_Lj,
+// the Caroli trace of caroli-green/src/lib.rs:106-113 rewritten with Γ_R = W_R W_R^†.
+//
+// Each iteration: D = M^-1 R (f32 forward and backward sweeps through the tree and the f32 root
+// inverse), X += D, R = B - A X with H, Σ in FP64 (CSR of the block), T and the correction norm
+// in FP64. A front's factors are [F11^-1 | X; W | S] with W = -F21 F11^-1 (see kernels.cuh):
+//   forward  z = own r + Σ_children h_c,  t = F11^-1 z_e,  h = z_b + W z_e  (handed to the parent)
+//   root     x = F_root^-1 z
+//   backward x_e = t - X x_b
+#pragma once
+#include "kernels.cuh"
+
+namespace caroli {
+
+constexpr int RCB = 8;  // right-hand-side columns per CTA in the tree sweeps
+
+struct RefineDesc {
+  const FrontDesc* fronts;
+  const int32_t* maps;
+  const uint8_t* own;
+  const int32_t* vidx;
+  const float2* arena;  // f32 factors
+  const float2* root;   // f32 root inverse (m x m)
+  const int32_t* csr_ptr;
+  const int32_t* csr_col;
+  const int64_t* csr_q;
+  const double2* vals;
+  const int32_t* slice_l;  // per block-local row: position in the left slice, or -1
+  const int32_t* slice_r;
+  const int32_t* left_local;
+  const int32_t* right_local;
+  const double2* sigma_l;
+  const double2* sigma_r;
+  const double2* gamma_l;
+  const double2* w_r;  // nr x c, column-major
+  double energy;
+  int32_t nblk, nl, nr, c, root_front;
+  int64_t sum_ne, sum_nb;
+  double2* x;  // nblk x c
+  double2* r;  // nblk x c
+  float2* d;   // nblk x c
+  float2* tb;  // sum_ne x c
+  float2* hb;  // sum_nb x c
+  double t_prev, t_cur, corr, err;
+  int32_t done, iters, stalled, pad;
+  // GMRES (right-preconditioned by the f32 factors) for the correction of each outer step.
+  double2* V;   // (m + 1) Arnoldi vectors, each nblk x c
+  float2* Z;    // m preconditioned vectors M^-1 V_k, each nblk x c
+  double2* H;   // per column: (m + 1) x m Hessenberg, column-major
+  double2* g;   // per column: m + 1 (rotated right-hand side)
+  double* cs;   // per column: m cosines of the Givens rotations
+  double2* sn;  // per column: m sines
+  double2* y;   // per column: m solution coefficients
+  double* beta; // per column: |r_j|
+  int32_t* col_done;  // per column: the inner solve converged (or the column is empty)
+  int32_t inner, inner_done;  // Arnoldi steps of the current outer step; all columns converged
+  double inner_res;            // largest relative residual the last inner solve reached
+};
+
+constexpr int GM_M = 12;  // Arnoldi steps per outer step
+
+__device__ __forceinline__ float2 f2(double2 v) { return make_float2((float)v.x, (float)v.y); }
+
+// Forward sweep of the fronts of one level: grid (tasks, column chunks).
+// The sweeps solve M d = v for v = the residual (src < 0) or the Arnoldi vector V_src, and write
+// d to R.d (dst < 0) or to Z_dst.
+__device__ __forceinline__ const double2* sweep_src(const RefineDesc& R, int src) {
+  return src < 0 ? R.r : R.V + (int64_t)src * R.nblk * R.c;
+}
+__device__ __forceinline__ float2* sweep_dst(const RefineDesc& R, int dst) {
+  return dst < 0 ? R.d : R.Z + (int64_t)dst * R.nblk * R.c;
+}
+
+__global__ void __launch_bounds__(256) refine_forward_kernel(RefineDesc* __restrict__ rd, const Task* __restrict__ tasks,
+                                                             int src) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const Task tk = tasks[blockIdx.x];
+  const RefineDesc& R = rd[tk.job];
+  if (R.done || (src >= 0 && R.inner_done)) return;
+  const double2* rin = sweep_src(R, src);
+  const int j0 = blockIdx.y * RCB;
+  const int cb = min(RCB, R.c - j0);
+  if (cb <= 0) return;
+  const FrontDesc f = R.fronts[tk.front];
+  const int n = f.n, ne = f.ne, nb = n - ne;
+  float2* z = reinterpret_cast<float2*>(smem_raw);  // n x RCB, row-major
+  float2* ts = z + (size_t)n * RCB;                  // ne x RCB
+  const float2* F = R.arena + f.arena_off;
+  for (int idx = threadIdx.x; idx < n * cb; idx += blockDim.x) {
+    const int p = idx / cb, j = idx % cb;
+    float2 v = make_float2(0.f, 0.f);
+    if (R.own[f.own_off + p]) v = f2(rin[R.vidx[f.var_off + p] + (int64_t)(j0 + j) * R.nblk]);
+    for (int c = 0; c < f.nchild; ++c) {
+      const int a = R.maps[f.map_off[c] + p];
+      if (a >= 0) {
+        const FrontDesc& cf = R.fronts[f.child[c]];
+        float2 h = R.hb[(cf.hoff + a) + (int64_t)(j0 + j) * R.sum_nb];
+        v.x += h.x; v.y += h.y;
+      }
+    }
+    z[p * RCB + j] = v;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < ne; i += blockDim.x) {
+    float2 acc[RCB];
+#pragma unroll
+    for (int j = 0; j < RCB; ++j) acc[j] = make_float2(0.f, 0.f);
+    for (int k = 0; k < ne; ++k) {
+      const float2 a = F[i + (int64_t)k * n];
+#pragma unroll
+      for (int j = 0; j < RCB; ++j) acc[j] = cfma(acc[j], a, z[k * RCB + j]);
+    }
+#pragma unroll
+    for (int j = 0; j < RCB; ++j) {
+      ts[i * RCB + j] = acc[j];
+      if (j < cb) R.tb[(f.toff + i) + (int64_t)(j0 + j) * R.sum_ne] = acc[j];
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    float2 acc[RCB];
+#pragma unroll
+    for (int j = 0; j < RCB; ++j) acc[j] = z[(ne + i) * RCB + j];
+    for (int k = 0; k < ne; ++k) {
+      const float2 a = F[(ne + i) + (int64_t)k * n];
+#pragma unroll
+      for (int j = 0; j < RCB; ++j) acc[j] = cfma(acc[j], a, z[k * RCB + j]);
+    }
+#pragma unroll
+    for (int j = 0; j < RCB; ++j)
+      if (j < cb) R.hb[(f.hoff + i) + (int64_t)(j0 + j) * R.sum_nb] = acc[j];
+  }
+}
+
+// Root: x = F_root^-1 z on the root's variables. grid (jobs, column chunks).
+__global__ void __launch_bounds__(256) refine_root_kernel(RefineDesc* __restrict__ rd, int src, int dst) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const RefineDesc& R = rd[blockIdx.x];
+  if (R.done || (src >= 0 && R.inner_done)) return;
+  const double2* rin = sweep_src(R, src);
+  float2* dout = sweep_dst(R, dst);
+  const int j0 = blockIdx.y * RCB;
+  const int cb = min(RCB, R.c - j0);
+  if (cb <= 0) return;
+  const FrontDesc f = R.fronts[R.root_front];
+  const int m = f.n;
+  float2* z = reinterpret_cast<float2*>(smem_raw);
+  for (int idx = threadIdx.x; idx < m * cb; idx += blockDim.x) {
+    const int p = idx / cb, j = idx % cb;
+    float2 v = make_float2(0.f, 0.f);
+    if (R.own[f.own_off + p]) v = f2(rin[R.vidx[f.var_off + p] + (int64_t)(j0 + j) * R.nblk]);
+    for (int c = 0; c < f.nchild; ++c) {
+      const int a = R.maps[f.map_off[c] + p];
+      if (a >= 0) {
+        const FrontDesc& cf = R.fronts[f.child[c]];
+        float2 h = R.hb[(cf.hoff + a) + (int64_t)(j0 + j) * R.sum_nb];
+        v.x += h.x; v.y += h.y;
+      }
+    }
+    z[p * RCB + j] = v;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < m; i += blockDim.x) {
+    float2 acc[RCB];
+#pragma unroll
+    for (int j = 0; j < RCB; ++j) acc[j] = make_float2(0.f, 0.f);
+    for (int k = 0; k < m; ++k) {
+      const float2 a = R.root[i + (int64_t)k * m];
+#pragma unroll
+      for (int j = 0; j < RCB; ++j) acc[j] = cfma(acc[j], a, z[k * RCB + j]);
+    }
+    const int row = R.vidx[f.var_off + i];
+#pragma unroll
+    for (int j = 0; j < RCB; ++j)
+      if (j < cb) dout[row + (int64_t)(j0 + j) * R.nblk] = acc[j];
+  }
+}
+
+// Backward sweep of one level (top-down): x_e = t - X x_b.
+__global__ void __launch_bounds__(256) refine_backward_kernel(RefineDesc* __restrict__ rd, const Task* __restrict__ tasks,
+                                                              int src, int dst) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const Task tk = tasks[blockIdx.x];
+  const RefineDesc& R = rd[tk.job];
+  if (R.done || (src >= 0 && R.inner_done)) return;
+  float2* dout = sweep_dst(R, dst);
+  const int j0 = blockIdx.y * RCB;
+  const int cb = min(RCB, R.c - j0);
+  if (cb <= 0) return;
+  const FrontDesc f = R.fronts[tk.front];
+  const int n = f.n, ne = f.ne, nb = n - ne;
+  if (ne == 0) return;
+  float2* xb = reinterpret_cast<float2*>(smem_raw);  // nb x RCB
+  const float2* F = R.arena + f.arena_off;
+  for (int idx = threadIdx.x; idx < nb * cb; idx += blockDim.x) {
+    const int p = idx / cb, j = idx % cb;
+    xb[p * RCB + j] = dout[R.vidx[f.var_off + ne + p] + (int64_t)(j0 + j) * R.nblk];
+  }
+  for (int idx = threadIdx.x; idx < nb * RCB; idx += blockDim.x)
+    if (idx % RCB >= cb) xb[idx] = make_float2(0.f, 0.f);
+  __syncthreads();
+  for (int i = threadIdx.x; i < ne; i += blockDim.x) {
+    float2 acc[RCB];
+#pragma unroll
+    for (int j = 0; j < RCB; ++j)
+      acc[j] = j < cb ? R.tb[(f.toff + i) + (int64_t)(j0 + j) * R.sum_ne] : make_float2(0.f, 0.f);
+    for (int k = 0; k < nb; ++k) {
+      const float2 a = F[i + (int64_t)(ne + k) * n];
+#pragma unroll
+      for (int j = 0; j < RCB; ++j) acc[j] = cfms(acc[j], a, xb[k * RCB + j]);
+    }
+    const int row = R.vidx[f.var_off + i];
+#pragma unroll
+    for (int j = 0; j < RCB; ++j)
+      if (j < cb) dout[row + (int64_t)(j0 + j) * R.nblk] = acc[j];
+  }
+}
+
+// x += d, then the FP64 residual r = B - A x of every row: grid (jobs, row chunks of 256).
+__global__ void __launch_bounds__(256) refine_update_kernel(RefineDesc* __restrict__ rd) {
+  RefineDesc& R = rd[blockIdx.x];
+  if (R.done) return;
+  const int i = blockIdx.y * 256 + threadIdx.x;
+  if (i >= R.nblk) return;
+  for (int j = 0; j < R.c; ++j) {
+    const int64_t q = i + (int64_t)j * R.nblk;
+    const float2 dv = R.d[q];
+    R.x[q].x += (double)dv.x;
+    R.x[q].y += (double)dv.y;
+  }
+}
+
+__global__ void __launch_bounds__(256) refine_residual_kernel(RefineDesc* __restrict__ rd) {
+  const RefineDesc& R = rd[blockIdx.x];
+  if (R.done) return;
+  const int i = blockIdx.y * 256 + threadIdx.x;
+  if (i >= R.nblk) return;
+  const int li = R.slice_l[i], ri = R.slice_r[i];
+  for (int j = 0; j < R.c; ++j) {
+    const double2* xj = R.x + (int64_t)j * R.nblk;
+    double2 acc = ri >= 0 ? R.w_r[ri + (int64_t)j * R.nr] : make_double2(0.0, 0.0);
+    acc.x -= R.energy * xj[i].x;
+    acc.y -= R.energy * xj[i].y;
+    for (int q = R.csr_ptr[i]; q < R.csr_ptr[i + 1]; ++q) acc = cfma(acc, R.vals[R.csr_q[q]], xj[R.csr_col[q]]);
+    if (li >= 0)
+      for (int a = 0; a < R.nl; ++a) acc = cfma(acc, R.sigma_l[li + (int64_t)a * R.nl], xj[R.left_local[a]]);
+    if (ri >= 0)
+      for (int a = 0; a < R.nr; ++a) acc = cfma(acc, R.sigma_r[ri + (int64_t)a * R.nr], xj[R.right_local[a]]);
+    R.r[i + (int64_t)j * R.nblk] = acc;
+  }
+}
+
+// T = Σ_j x_Lj^† Γ_L x_Lj and the relative size of the last correction on the left slice (the only
+// rows T depends on); convergence decision. After a GMRES correction reaching inner relative
+// residual rho, the remaining relative error of x_L is about corr * rho: converged when that is
+// below `tol`; stalled when not finite, growing, or out of outer steps. Error estimate
+// |T| * 2 * corr * rho.
+__global__ void __launch_bounds__(256) refine_check_kernel(RefineDesc* __restrict__ rd, double tol, int max_iters,
+                                                           double* __restrict__ t_out, double* __restrict__ err_out,
+                                                           int32_t* __restrict__ done_out) {
+  __shared__ double red[3][32];
+  RefineDesc& R = rd[blockIdx.x];
+  if (R.done) {
+    if (threadIdx.x == 0) done_out[blockIdx.x] = R.stalled ? 2 : 1;
+    return;
+  }
+  double tl = 0.0, dn = 0.0, xn = 0.0;
+  for (int idx = threadIdx.x; idx < R.nl * R.c; idx += blockDim.x) {
+    const int a = idx % R.nl, j = idx / R.nl;
+    const double2* xj = R.x + (int64_t)j * R.nblk;
+    const int row = R.left_local[a];
+    double2 g = make_double2(0.0, 0.0);
+    for (int b = 0; b < R.nl; ++b) g = cfma(g, R.gamma_l[a + (int64_t)b * R.nl], xj[R.left_local[b]]);
+    const double2 xa = xj[row];
+    tl += xa.x * g.x + xa.y * g.y;
+    const float2 dv = R.d[row + (int64_t)j * R.nblk];
+    dn += (double)dv.x * dv.x + (double)dv.y * dv.y;
+    xn += xa.x * xa.x + xa.y * xa.y;
+  }
+  double vals[3] = {tl, dn, xn};
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  for (int k = 0; k < 3; ++k) {
+    double v = vals[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (l == 0) red[k][w] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sum[3] = {0.0, 0.0, 0.0};
+    for (int k = 0; k < 3; ++k)
+      for (int q = 0; q < (int)(blockDim.x >> 5); ++q) sum[k] += red[k][q];
+    const double corr = sum[2] > 0.0 ? sqrt(sum[1] / sum[2]) : (sum[1] > 0.0 ? INFINITY : 0.0);
+    const double prev = R.corr;
+    R.iters += 1;
+    R.t_prev = R.t_cur;
+    R.t_cur = sum[0];
+    const bool finite = isfinite(sum[0]) && isfinite(corr);
+    // After a GMRES step the remaining error is about corr times the inner residual reached.
+    const double rho = R.inner_res;
+    const bool conv = finite && (corr == 0.0 || corr * rho <= tol);
+    const bool stall = !finite || (!conv && R.iters >= max_iters) || (R.iters > 2 && corr > prev);
+    R.corr = corr;
+    R.err = fabs(sum[0]) * 2.0 * corr * rho;
+    if (conv || stall) {
+      R.done = 1;
+      R.stalled = stall && !conv;
+    }
+    t_out[blockIdx.x] = sum[0];
+    err_out[blockIdx.x] = R.err;
+    done_out[blockIdx.x] = R.done ? (R.stalled ? 2 : 1) : 0;
+  }
+}
+
+__global__ void refine_init_kernel(RefineDesc* __restrict__ rd, int njobs) {
+  const int job = blockIdx.y;
+  if (job >= njobs) return;
+  RefineDesc& R = rd[job];
+  const int64_t total = (int64_t)R.nblk * R.c;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(q % R.nblk), j = (int)(q / R.nblk);
+    const int ri = R.slice_r[i];
+    R.x[q] = make_double2(0.0, 0.0);
+    R.r[q] = ri >= 0 ? R.w_r[ri + (int64_t)j * R.nr] : make_double2(0.0, 0.0);
+  }
+}
+
+}  // namespace caroli
+
+namespace caroli {
+
+// ---- GMRES for the correction of an outer step ---------------------------------------------------
+// Right preconditioning: A M^-1 u = r, d = M^-1 (V y) = Z y. Arnoldi vectors in FP64, classical
+// Gram-Schmidt applied twice, complex Givens rotations (c real), per right-hand-side column.
+
+__device__ __forceinline__ double block_sum(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = (blockDim.x + 31) >> 5;
+  __syncthreads();
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    v = l < nw ? red[l] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (l == 0) red[0] = v;
+  }
+  __syncthreads();
+  const double r = red[0];
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ double2 cconj_mul(double2 a, double2 b) {  // conj(a) b
+  return make_double2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
+}
+
+// beta_j = |r_j|, V_0 = r / beta, g = (beta, 0, ...). grid (jobs, columns).
+__global__ void __launch_bounds__(256) gm_start_kernel(RefineDesc* __restrict__ rd) {
+  __shared__ double red[32];
+  RefineDesc& R = rd[blockIdx.x];
+  const int j = blockIdx.y;
+  if (R.done || j >= R.c) return;
+  const double2* r = R.r + (int64_t)j * R.nblk;
+  double ss = 0.0;
+  for (int i = threadIdx.x; i < R.nblk; i += blockDim.x) ss += r[i].x * r[i].x + r[i].y * r[i].y;
+  const double beta = sqrt(block_sum(ss, red));
+  const double inv = beta > 0.0 ? 1.0 / beta : 0.0;
+  double2* v0 = R.V + (int64_t)j * R.nblk;
+  for (int i = threadIdx.x; i < R.nblk; i += blockDim.x) v0[i] = make_double2(r[i].x * inv, r[i].y * inv);
+  if (threadIdx.x == 0) {
+    R.beta[j] = beta;
+    R.col_done[j] = beta > 0.0 ? 0 : -1;
+    double2* g = R.g + (int64_t)j * (GM_M + 1);
+    for (int i = 0; i <= GM_M; ++i) g[i] = make_double2(i == 0 ? beta : 0.0, 0.0);
+    if (j == 0) {
+      R.inner = 0;
+      R.inner_done = 0;
+    }
+  }
+}
+
+// w = A z_k into V_{k+1}, A = z - H - Σ_L - Σ_R in FP64. grid (jobs, row chunks of 256).
+__global__ void __launch_bounds__(256) gm_matvec_kernel(RefineDesc* __restrict__ rd, int k) {
+  const RefineDesc& R = rd[blockIdx.x];
+  if (R.done || R.inner_done) return;
+  const int i = blockIdx.y * 256 + threadIdx.x;
+  if (i >= R.nblk) return;
+  const int li = R.slice_l[i], ri = R.slice_r[i];
+  const float2* Zk = R.Z + (int64_t)k * R.nblk * R.c;
+  double2* W = R.V + (int64_t)(k + 1) * R.nblk * R.c;
+  for (int j = 0; j < R.c; ++j) {
+    const float2* zj = Zk + (int64_t)j * R.nblk;
+    auto zd = [&](int q) { return make_double2((double)zj[q].x, (double)zj[q].y); };
+    double2 acc = zd(i);
+    acc.x *= R.energy;
+    acc.y *= R.energy;
+    for (int q = R.csr_ptr[i]; q < R.csr_ptr[i + 1]; ++q) acc = cfms(acc, R.vals[R.csr_q[q]], zd(R.csr_col[q]));
+    if (li >= 0)
+      for (int a = 0; a < R.nl; ++a) acc = cfms(acc, R.sigma_l[li + (int64_t)a * R.nl], zd(R.left_local[a]));
+    if (ri >= 0)
+      for (int a = 0; a < R.nr; ++a) acc = cfms(acc, R.sigma_r[ri + (int64_t)a * R.nr], zd(R.right_local[a]));
+    W[i + (int64_t)j * R.nblk] = acc;
+  }
+}
+
+// Gram-Schmidt coefficients c_i = V_i^† w (i <= k) into y (pass 0 stores them in H, pass 1 adds).
+// grid (jobs, columns, k + 1).
+__global__ void __launch_bounds__(256) gm_dot_kernel(RefineDesc* __restrict__ rd, int k, int pass) {
+  __shared__ double red[32];
+  RefineDesc& R = rd[blockIdx.x];
+  const int j = blockIdx.y, i = blockIdx.z;
+  if (R.done || R.inner_done || j >= R.c || R.col_done[j] != 0) return;
+  const double2* v = R.V + (int64_t)i * R.nblk * R.c + (int64_t)j * R.nblk;
+  const double2* w = R.V + (int64_t)(k + 1) * R.nblk * R.c + (int64_t)j * R.nblk;
+  double re = 0.0, im = 0.0;
+  for (int q = threadIdx.x; q < R.nblk; q += blockDim.x) {
+    const double2 p = cconj_mul(v[q], w[q]);
+    re += p.x;
+    im += p.y;
+  }
+  re = block_sum(re, red);
+  im = block_sum(im, red);
+  if (threadIdx.x == 0) {
+    R.y[(int64_t)j * GM_M + i] = make_double2(re, im);
+    double2* h = R.H + (int64_t)j * (GM_M + 1) * GM_M + i + (int64_t)k * (GM_M + 1);
+    if (pass == 0) *h = make_double2(re, im);
+    else { h->x += re; h->y += im; }
+  }
+}
+
+// w -= Σ_i c_i V_i. grid (jobs, row chunks).
+__global__ void __launch_bounds__(256) gm_axpy_kernel(RefineDesc* __restrict__ rd, int k) {
+  const RefineDesc& R = rd[blockIdx.x];
+  if (R.done || R.inner_done) return;
+  const int q = blockIdx.y * 256 + threadIdx.x;
+  if (q >= R.nblk) return;
+  for (int j = 0; j < R.c; ++j) {
+    if (R.col_done[j] != 0) continue;
+    double2* w = R.V + (int64_t)(k + 1) * R.nblk * R.c + (int64_t)j * R.nblk;
+    double2 acc = w[q];
+    for (int i = 0; i <= k; ++i)
+      acc = cfms(acc, R.y[(int64_t)j * GM_M + i], R.V[(int64_t)i * R.nblk * R.c + (int64_t)j * R.nblk + q]);
+    w[q] = acc;
+  }
+}
+
+// h_{k+1,k} = |w|, V_{k+1} = w / |w|, then the Givens rotations of column k and the residual
+// estimate |g_{k+1}|; a column converges when it is below tol * beta. grid (jobs, columns).
+__global__ void __launch_bounds__(256) gm_norm_kernel(RefineDesc* __restrict__ rd, int k, double tol) {
+  __shared__ double red[32];
+  RefineDesc& R = rd[blockIdx.x];
+  const int j = blockIdx.y;
+  if (R.done || R.inner_done || j >= R.c || R.col_done[j] != 0) return;
+  double2* w = R.V + (int64_t)(k + 1) * R.nblk * R.c + (int64_t)j * R.nblk;
+  double ss = 0.0;
+  for (int q = threadIdx.x; q < R.nblk; q += blockDim.x) ss += w[q].x * w[q].x + w[q].y * w[q].y;
+  const double nrm = sqrt(block_sum(ss, red));
+  const double inv = nrm > 0.0 ? 1.0 / nrm : 0.0;
+  for (int q = threadIdx.x; q < R.nblk; q += blockDim.x) w[q] = make_double2(w[q].x * inv, w[q].y * inv);
+  if (threadIdx.x != 0) return;
+  double2* H = R.H + (int64_t)j * (GM_M + 1) * GM_M + (int64_t)k * (GM_M + 1);
+  double2* g = R.g + (int64_t)j * (GM_M + 1);
+  double* cs = R.cs + (int64_t)j * GM_M;
+  double2* sn = R.sn + (int64_t)j * GM_M;
+  H[k + 1] = make_double2(nrm, 0.0);
+  for (int i = 0; i < k; ++i) {
+    // [h_i; h_{i+1}] <- [c s; -conj(s) c] [h_i; h_{i+1}]
+    const double2 a = H[i], b = H[i + 1];
+    const double2 sb = cmul(sn[i], b);
+    const double2 sa = cconj_mul(sn[i], a);
+    H[i] = make_double2(cs[i] * a.x + sb.x, cs[i] * a.y + sb.y);
+    H[i + 1] = make_double2(cs[i] * b.x - sa.x, cs[i] * b.y - sa.y);
+  }
+  const double2 a = H[k], b = H[k + 1];
+  const double na = sqrt(a.x * a.x + a.y * a.y), nb = sqrt(b.x * b.x + b.y * b.y);
+  const double r = sqrt(na * na + nb * nb);
+  double c;
+  double2 sv;
+  if (r == 0.0) { c = 1.0; sv = make_double2(0.0, 0.0); }
+  else if (na == 0.0) { c = 0.0; sv = make_double2(b.x / nb, -b.y / nb); }  // s = conj(b)/|b|
+  else {
+    c = na / r;
+    // s = (a / |a|) conj(b) / r
+    const double2 ua = make_double2(a.x / na, a.y / na);
+    sv = cmul(ua, make_double2(b.x / r, -b.y / r));
+  }
+  cs[k] = c;
+  sn[k] = sv;
+  H[k] = make_double2(c * a.x + (cmul(sv, b)).x, c * a.y + (cmul(sv, b)).y);
+  H[k + 1] = make_double2(0.0, 0.0);
+  const double2 gk = g[k];
+  g[k] = make_double2(c * gk.x, c * gk.y);
+  const double2 t = cconj_mul(sv, gk);
+  g[k + 1] = make_double2(-t.x, -t.y);
+  const double res = sqrt(g[k + 1].x * g[k + 1].x + g[k + 1].y * g[k + 1].y);
+  if (!(res > tol * R.beta[j]) || nrm == 0.0) R.col_done[j] = k + 1;
+}
+
+// After step k: a job's inner solve ends when every column converged or after GM_M steps.
+__global__ void gm_inner_check_kernel(RefineDesc* __restrict__ rd, int njobs, int k, int32_t* __restrict__ flags) {
+  const int job = blockIdx.x * blockDim.x + threadIdx.x;
+  if (job >= njobs) return;
+  RefineDesc& R = rd[job];
+  if (R.done) { flags[job] = 1; return; }
+  if (R.inner_done) { flags[job] = 1; return; }
+  R.inner = k + 1;
+  bool all = true;
+  for (int j = 0; j < R.c; ++j) all &= R.col_done[j] != 0;
+  if (all || k + 1 >= GM_M) R.inner_done = 1;
+  flags[job] = R.inner_done;
+}
+
+// y = H^-1 g on each column's steps, d = Z y, x += d, R.d = d; the largest relative inner
+// residual of the job goes to R.err (reused by the outer check). grid (jobs, row chunks).
+__global__ void gm_solve_kernel(RefineDesc* __restrict__ rd, int njobs) {
+  const int job = blockIdx.x;
+  if (job >= njobs) return;
+  RefineDesc& R = rd[job];
+  if (R.done) return;
+  const int j = threadIdx.x;
+  if (j >= R.c) return;
+  const int kc = R.col_done[j] > 0 ? R.col_done[j] : (R.col_done[j] < 0 ? 0 : R.inner);
+  const double2* H = R.H + (int64_t)j * (GM_M + 1) * GM_M;
+  const double2* g = R.g + (int64_t)j * (GM_M + 1);
+  double2* y = R.y + (int64_t)j * GM_M;
+  for (int i = kc - 1; i >= 0; --i) {
+    double2 acc = g[i];
+    for (int t = i + 1; t < kc; ++t) acc = cfms(acc, H[i + (int64_t)t * (GM_M + 1)], y[t]);
+    const double2 d = H[i + (int64_t)i * (GM_M + 1)];
+    const double dd = d.x * d.x + d.y * d.y;
+    y[i] = dd > 0.0 ? make_double2((acc.x * d.x + acc.y * d.y) / dd, (acc.y * d.x - acc.x * d.y) / dd)
+                    : make_double2(0.0, 0.0);
+  }
+  for (int t = kc; t < GM_M; ++t) y[t] = make_double2(0.0, 0.0);
+}
+
+__global__ void __launch_bounds__(256) gm_update_kernel(RefineDesc* __restrict__ rd) {
+  const RefineDesc& R = rd[blockIdx.x];
+  if (R.done) return;
+  const int q = blockIdx.y * 256 + threadIdx.x;
+  if (q >= R.nblk) return;
+  for (int j = 0; j < R.c; ++j) {
+    double2 acc = make_double2(0.0, 0.0);
+    for (int t = 0; t < GM_M; ++t) {
+      const double2 yt = R.y[(int64_t)j * GM_M + t];
+      if (yt.x == 0.0 && yt.y == 0.0) continue;
+      const float2 z = R.Z[(int64_t)t * R.nblk * R.c + (int64_t)j * R.nblk + q];
+      acc = cfma(acc, yt, make_double2((double)z.x, (double)z.y));
+    }
+    const int64_t o = q + (int64_t)j * R.nblk;
+    R.x[o].x += acc.x;
+    R.x[o].y += acc.y;
+    R.d[o] = make_float2((float)acc.x, (float)acc.y);
+  }
+}
+
+// Largest relative inner residual of each job's last outer step.
+__global__ void gm_residual_kernel(RefineDesc* __restrict__ rd, int njobs) {
+  const int job = blockIdx.x * blockDim.x + threadIdx.x;
+  if (job >= njobs) return;
+  RefineDesc& R = rd[job];
+  if (R.done) return;
+  double worst = 0.0;
+  for (int j = 0; j < R.c; ++j) {
+    if (R.col_done[j] < 0) continue;
+    const int k = R.col_done[j] > 0 ? R.col_done[j] : R.inner;
+    const double2 gk = R.g[(int64_t)j * (GM_M + 1) + k];
+    const double res = sqrt(gk.x * gk.x + gk.y * gk.y) / fmax(R.beta[j], 1e-300);
+    worst = fmax(worst, res);
+  }
+  R.inner_res = worst;
+}
+
+}  // namespace caroli

@@ -93,8 +93,40 @@ int caroli_sigma_upload(caroli_ctx* ctx, int plan_id, int slot, double energy, c
 int caroli_solve_batch(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots, const int32_t* configs,
                        int precision, double* t, int32_t* status, double* err);
 
+/* Timed region on the context's stream: caroli_region_end returns the device time between the
+ * two calls (CUDA events on the stream every kernel of the library runs on) and the number of
+ * kernels the library launched in between. */
+int caroli_region_begin(caroli_ctx* ctx);
+int caroli_region_end(caroli_ctx* ctx, double* device_ms, int64_t* launches);
+
+/* Per-kernel-class accounting (classes 0 .. caroli_kernel_classes()-1, named by
+ * caroli_kernel_class_name): launches, algorithmic flops (complex multiply-add = 8 flops, the
+ * reference's LU/TRSM/GEMM counts) and bytes attributed to the class. caroli_probe_kernel(ctx, k)
+ * makes later solves time every launch of class k with CUDA events (-1: none); `ms` is their total.
+ * `reset` clears the class's counters after reading them. */
+int caroli_kernel_classes(void);
+const char* caroli_kernel_class_name(int kclass);
+int caroli_probe_kernel(caroli_ctx* ctx, int kclass);
+int caroli_kernel_stats(caroli_ctx* ctx, int kclass, int64_t* launches, double* flops, double* bytes, double* ms,
+                        int reset);
+
 /* Device time of the last caroli_solve_batch (ms), and kernels it launched. */
 int caroli_last_timing(const caroli_ctx* ctx, double* device_ms, int64_t* launches);
+
+/* Of the last caroli_solve_batch: solves recomputed in double precision (CAROLI_MIXED points the
+ * refinement could not resolve, as precision::checked recomputes failed points), and the largest
+ * number of refinement iterations a solve took. */
+int caroli_last_stats(const caroli_ctx* ctx, int64_t* fallbacks, int64_t* max_refine_iters);
+
+/* Per block solve of the last caroli_solve_batch (instance-major, blocks fastest; up to
+ * `capacity` entries, *count = all): refinement iterations, pivots perturbed by static pivoting,
+ * and status (100 + s: status s in reduced precision, then recomputed in double precision). */
+int caroli_last_job_info(const caroli_ctx* ctx, int64_t capacity, int32_t* iters, int32_t* perturbed,
+                         int32_t* status, int64_t* count);
+
+/* Device time of the last caroli_solve_batch split into the tree factorization, the root
+ * inverse, and the rest (trace, or refinement and double-precision recomputations), in ms. */
+int caroli_last_phases(const caroli_ctx* ctx, double* factor_ms, double* root_ms, double* tail_ms);
 
 #ifdef __cplusplus
 }

@@ -67,3 +67,29 @@ def test_single_precision_follows_double():
     s = sys_.self_energies(0.3)
     t32 = sys_.transmission_with_precision(s, Precision.SINGLE)
     assert abs(t32 - oracle_T(sys_, s)) < 1e-2
+
+
+def test_mixed_refined_matches_double():
+    """Mixed precision: f32 factors + FP64 refinement reach |ΔT| <= 1e-8 of the oracle."""
+    sys_ = magnetic_bhz(40, 16, configs=2)
+    sigmas = [sys_.self_energies(e) for e in np.linspace(-0.16, 0.16, 5)]
+    pairs = [(s, c) for s in sigmas for c in range(2)]
+    t, st, err = sys_.solve_batch([p[0] for p in pairs], [p[1] for p in pairs], Precision.MIXED)
+    assert (st == 0).all(), st
+    for (s, c), tm in zip(pairs, t):
+        ref = oracle_T(sys_, s, config=c)
+        assert abs(tm - ref) <= 1e-8, (s.energy, c, tm, ref)
+
+
+@pytest.mark.parametrize("problem", ["bhz-anderson", "graphene-anderson", "square-anderson"])
+def test_mixed_bench_w32(problem):
+    gold = bench_golden()[f"caroli/{problem}/32"]
+    sys_ = bench_system(problem, 32)
+    sigmas = [sys_.self_energies(e) for e in gold["energies"]]
+    t, st, err = sys_.solve_batch(sigmas, [0] * len(sigmas), Precision.MIXED)
+    assert (st == 0).all(), st
+    fallbacks, iters = sys_.plan().last_stats()
+    assert fallbacks == 0 and iters <= 4, (fallbacks, iters)
+    for s, tm in zip(sigmas, t):
+        ref = oracle_T(sys_, s)
+        assert abs(tm - ref) <= 1e-8, (problem, s.energy, tm, ref)
