@@ -205,7 +205,8 @@ def run_ours(args):
     dT = np.abs(t_mixed - t_dbl)
     # End to end through the public API from host buffers.
     values = np.ascontiguousarray(np.stack(sys_.system.values))
-    h2d = values.nbytes + sum(sum(a.nbytes + b.nbytes for a, b in s.blocks) for s in sigmas)
+    h2d = values.nbytes + sum(sum(a.nbytes + b.nbytes for a, b in s.blocks) + sum(w.nbytes for w in s.w_right())
+                              for s in sigmas)
     h2d += 2 * 4 * nsolve
     d2h = nsolve * (8 + 4 + 8)
     ctx.region_begin()
@@ -213,7 +214,7 @@ def run_ours(args):
     for _ in range(args.steps):
         plan.upload_values(list(values))
         for slot, s in enumerate(sigmas):
-            plan.upload_sigma(sys_._slot_of[id(s)][0], s.energy, s.blocks)
+            plan.upload_sigma(sys_._slot_of[id(s)][0], s.energy, s.blocks, s.w_right())
         sys_.solve_batch(S, C, Precision.MIXED)
     e2e_ms, _ = ctx.region_end()
     e2e_wall = time.perf_counter() - e0

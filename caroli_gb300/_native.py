@@ -28,7 +28,7 @@ SIGNATURES = {
                                           P, P, ctypes.POINTER(ctypes.c_int)]),
     "caroli_plan_info": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P, P]),
     "caroli_values_upload": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P]),
-    "caroli_sigma_upload": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, ctypes.c_double, P, P]),
+    "caroli_sigma_upload": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, ctypes.c_double, P, P, P, P]),
     "caroli_solve_batch": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, ctypes.c_int, P, P, P]),
     "caroli_last_timing": (ctypes.c_int, [P, P, P]),
     "caroli_last_stats": (ctypes.c_int, [P, P, P]),
@@ -155,12 +155,20 @@ class Plan:
         v = np.ascontiguousarray(np.stack(values), dtype=np.complex128)
         self.ctx.check(self.ctx.lib.caroli_values_upload(self.ctx.h, self.id, v.shape[0], ptr(v)))
 
-    def upload_sigma(self, slot, energy, sigmas):
+    def upload_sigma(self, slot, energy, sigmas, w_right=None):
+        """Σ of every block; ``w_right[b]`` (nr x channels) with W W^† = Γ_R, or None."""
         ls = [np.asfortranarray(sl, dtype=np.complex128) for sl, _ in sigmas]
         rs = [np.asfortranarray(sr, dtype=np.complex128) for _, sr in sigmas]
         pl = np.array([a.ctypes.data for a in ls], dtype=np.uintp)
         pr = np.array([a.ctypes.data for a in rs], dtype=np.uintp)
-        self.ctx.check(self.ctx.lib.caroli_sigma_upload(self.ctx.h, self.id, slot, energy, ptr(pl), ptr(pr)))
+        pw = ch = None
+        if w_right is not None:
+            ws = [np.asfortranarray(w, dtype=np.complex128) for w in w_right]
+            pw = np.array([w.ctypes.data if w.size else 0 for w in ws], dtype=np.uintp)
+            ch = np.array([w.shape[1] for w in ws], dtype=np.int32)
+            self._keep_w = ws
+        self.ctx.check(self.ctx.lib.caroli_sigma_upload(self.ctx.h, self.id, slot, energy, ptr(pl), ptr(pr),
+                                                        ptr(pw), ptr(ch)))
 
     def solve(self, slots, configs, precision=DOUBLE):
         slots = np.ascontiguousarray(slots, np.int32)

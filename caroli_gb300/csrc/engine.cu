@@ -1085,7 +1085,7 @@ int caroli_values_upload(caroli_ctx* ctx, int plan_id, int nconfigs, const doubl
 }
 
 int caroli_sigma_upload(caroli_ctx* ctx, int plan_id, int slot, double energy, const double* const* sigma_l,
-                        const double* const* sigma_r) {
+                        const double* const* sigma_r, const double* const* w_right, const int32_t* channels) {
   System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
   if (!sys || slot < 0 || !sigma_l || !sigma_r) return fail_with(ctx, CAROLI_EINVAL, "caroli_sigma_upload: bad arguments");
   try {
@@ -1114,7 +1114,14 @@ int caroli_sigma_upload(caroli_ctx* ctx, int plan_id, int slot, double energy, c
       gamma(sigma_l[b], nl, gl);
       gamma(sigma_r[b], nr, gr);
       std::vector<double> wr;
-      const int ch = gamma_factor(gr, nr, wr);
+      int ch;
+      if (w_right && channels) {
+        ch = channels[b];
+        if (ch < 0 || (size_t)ch > nr) return fail_with(ctx, CAROLI_EINVAL, "caroli_sigma_upload: bad channel count");
+        wr.assign(w_right[b], w_right[b] + 2 * nr * (size_t)ch);
+      } else {
+        ch = gamma_factor(gr, nr, wr);
+      }
       sg.channels.push_back(ch);
       sg.wr.push_back(upload_c64(wr.data(), nr * (size_t)ch, ctx->stream));
       sg.sl.push_back(upload_c64(sigma_l[b], nl * nl, ctx->stream));

@@ -204,12 +204,15 @@ def broadening(sigma):
     return 1j * (sigma - sigma.conj().T)
 
 
-def gamma_root(sigma):
-    """``W`` with ``W W† = Γ``: eigenvectors of ``Γ`` with eigenvalues above ``1e-12`` of the
-    largest, scaled by their square roots (``nested.rs:1036-1047``)."""
+def gamma_root(sigma, cut=1e-12):
+    """``W`` with ``W W† = Γ``: eigenvectors of ``Γ`` with eigenvalues above ``cut`` times the
+    largest, scaled by their square roots (``nested.rs:1036-1047`` cuts at 1e-12). The mixed
+    transmission takes its right-hand sides from here: T = Σ_j x_j^† Γ_L x_j with x = G W_R
+    differs from the full-Γ trace only by the dropped eigenvalues (rounding noise of Σ, which may
+    be slightly negative), a few 1e-10 at worst on the reference's benchmark problems."""
     g = broadening(sigma)
     g = 0.5 * (g + g.conj().T)
     vals, vecs = np.linalg.eigh(g)
     top = np.abs(vals).max() if len(vals) else 0.0
-    keep = vals > 1e-12 * top
+    keep = vals > cut * top
     return vecs[:, keep] * np.sqrt(vals[keep])[None, :]

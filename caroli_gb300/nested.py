@@ -29,7 +29,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _native
-from .leads import GreenError, LeadSolver
+from .leads import GreenError, LeadSolver, gamma_root
 from .precision import Precision, PrecisionOptions, checked
 from .system import System, build_system
 
@@ -43,6 +43,12 @@ class LeadSelfEnergies:
 
     def key(self):
         return id(self)
+
+    def w_right(self):
+        """Per block, W_R with W_R W_R^† = Γ_R (the mixed path's right-hand sides)."""
+        if not hasattr(self, "_w_right"):
+            self._w_right = [gamma_root(sr) for _, sr in self.blocks]
+        return self._w_right
 
 
 _CONTEXTS = {}
@@ -108,7 +114,7 @@ class NestedTwoTerminal:
         key = id(sigma)
         if key not in self._slot_of or self._slot_of[key][1] is not sigma:
             slot = len(self._slot_of)
-            self.plan().upload_sigma(slot, sigma.energy, sigma.blocks)
+            self.plan().upload_sigma(slot, sigma.energy, sigma.blocks, sigma.w_right())
             self._slot_of[key] = (slot, sigma)
         return self._slot_of[key][0]
 

@@ -80,9 +80,14 @@ int caroli_plan_info(caroli_ctx* ctx, int plan_id, int block, int64_t* fronts, i
 int caroli_values_upload(caroli_ctx* ctx, int plan_id, int nconfigs, const double* values);
 
 /* Lead self-energies of energy slot `slot` (any slot number; re-uploading replaces it):
- * sigma_l[b], sigma_r[b] are column-major complex128 (nl_b x nl_b, nr_b x nr_b) of block b. */
+ * sigma_l[b], sigma_r[b] are column-major complex128 (nl_b x nl_b, nr_b x nr_b) of block b.
+ * w_right[b] (nr_b x channels[b], column-major complex128) with w_right w_right^† = Γ_R =
+ * i(Σ_R - Σ_R^†) is the right-hand side of CAROLI_MIXED (gamma_root, nested.rs:1036-1047: the
+ * eigenvectors of Γ_R with positive eigenvalues, scaled by their square roots). Both may be NULL:
+ * the library then factors Γ_R by pivoted Cholesky, which is less robust when Σ_R is inexact
+ * (Γ_R slightly indefinite). */
 int caroli_sigma_upload(caroli_ctx* ctx, int plan_id, int slot, double energy, const double* const* sigma_l,
-                        const double* const* sigma_r);
+                        const double* const* sigma_r, const double* const* w_right, const int32_t* channels);
 
 /* T for `count` instances (energy slot, configuration), summed over the blocks.
  *   precision       CAROLI_DOUBLE, CAROLI_SINGLE or CAROLI_MIXED
