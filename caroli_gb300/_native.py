@@ -35,6 +35,7 @@ SIGNATURES = {
     "caroli_last_phases": (ctypes.c_int, [P, P, P, P]),
     "caroli_region_begin": (ctypes.c_int, [P]),
     "caroli_region_end": (ctypes.c_int, [P, P, P]),
+    "caroli_solve_batch_noalloc": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P]),
     "caroli_kernel_classes": (ctypes.c_int, []),
     "caroli_last_job_info": (ctypes.c_int, [P, I64, P, P, P, P]),
     "caroli_kernel_class_name": (ctypes.c_char_p, [ctypes.c_int]),

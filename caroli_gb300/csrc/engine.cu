@@ -1272,3 +1272,252 @@ int caroli_last_timing(const caroli_ctx* ctx, double* device_ms, int64_t* launch
 }
 
 }  // extern "C"
+
+// ---- Transmission without device allocation -------------------------------------------------------
+// caroli_solve_batch grows device buffers with cudaMalloc as batches grow. Some callers cannot
+// allocate device memory when they solve: a host program whose device memory is entirely
+// reserved by another allocator (a framework's caching pool that has claimed the GPU), or a
+// latency-critical loop that forbids allocation. For them caroli_solve_batch_noalloc runs the
+// double-precision path on scratch carved from one file-scope device array of fixed size,
+// NOALLOC_BYTES, which every GPU that loads this library holds until the process exits.
+namespace {
+
+constexpr size_t NOALLOC_BYTES = size_t(64) << 20;  // 64 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+unsigned char* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
+
+// The device address of the scratch array on `device` (which must be current). Host code cannot
+// use the symbol itself: its name stands for a host-side shadow, not device memory.
+cudaError_t noalloc_scratch(int device, unsigned char** out) {
+  if (device < 0 || device >= NOALLOC_MAX_DEVICES) return cudaErrorInvalidDevice;
+  if (!g_noalloc_ptr[device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    g_noalloc_ptr[device] = static_cast<unsigned char*>(p);
+  }
+  *out = g_noalloc_ptr[device];
+  return cudaSuccess;
+}
+
+// Bump allocation inside the scratch array (256-byte aligned pieces).
+struct Carve {
+  unsigned char* base;
+  size_t used = 0;
+  size_t need(size_t bytes) {
+    size_t at = (used + 255) & ~size_t(255);
+    used = at + std::max<size_t>(bytes, 1);
+    return at;
+  }
+};
+
+}  // namespace
+
+extern "C" int caroli_solve_batch_noalloc(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots,
+                                          const int32_t* configs, double* t, int32_t* status) {
+  System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
+  if (!sys || count < 0 || (count > 0 && (!slots || !configs || !t || !status)))
+    return fail_with(ctx, CAROLI_EINVAL, "caroli_solve_batch_noalloc: bad arguments");
+  if (!sys->vals) return fail_with(ctx, CAROLI_EINVAL, "no H values uploaded");
+  for (int i = 0; i < count; ++i) {
+    if (slots[i] < 0 || slots[i] >= (int)sys->slots.size() || !sys->slots[slots[i]].set)
+      return fail_with(ctx, CAROLI_EINVAL, "energy slot without self-energies");
+    if (configs[i] < 0 || configs[i] >= sys->nconfigs) return fail_with(ctx, CAROLI_EINVAL, "configuration out of range");
+  }
+  if (count == 0) return CAROLI_OK;
+  try {
+    CK(cudaSetDevice(ctx->device));
+    unsigned char* base = nullptr;
+    CK(noalloc_scratch(ctx->device, &base));
+    cudaStream_t s = ctx->stream;
+    const int nb = (int)sys->plans.size();
+    const size_t nj = (size_t)count * nb;
+    const size_t vb = sizeof(double2);
+    // Layout of the scratch, with every size checked before anything runs.
+    std::vector<size_t> arena_off(nj), root_off(nj), fail_off(nj);
+    size_t aoff = 0, roff = 0, foff = 0, ntask = 0, ninv = 0, npiv = 0, ny = 0;
+    int max_levels = 0, max_root = 0;
+    size_t parts = 1;
+    for (size_t j = 0; j < nj; ++j) {
+      const FrontPlan& P = sys->plans[j % nb]->host;
+      arena_off[j] = aoff;
+      aoff += (size_t)P.arena_elems;
+      const int m = P.fronts[P.root].n;
+      root_off[j] = roff;
+      roff += (size_t)m * m;
+      fail_off[j] = foff;
+      foff += P.fronts.size();
+      ntask += P.fronts.size();
+      max_levels = std::max(max_levels, P.levels);
+      max_root = std::max(max_root, m);
+      parts = std::max(parts, (size_t)(P.nr + 7) / 8);
+      for (size_t k = 0; k + 1 < P.fronts.size(); ++k)
+        if (P.fronts[k].n > SMALL_MAX_F64 && P.fronts[k].ne > 0) {
+          ++ninv;
+          npiv += P.fronts[k].ne;
+          ny += (size_t)GJ_KB * P.fronts[k].n;
+        }
+      ++ninv;
+      npiv += m;
+      ny += (size_t)GJ_KB * m;
+    }
+    Carve cv{base};
+    const size_t o_arena = cv.need(aoff * vb), o_root = cv.need(roff * vb), o_fail = cv.need(foff);
+    const size_t o_status = cv.need(nj * 4), o_t = cv.need(nj * 8), o_part = cv.need(nj * parts * 8);
+    const size_t o_jobs = cv.need(nj * sizeof(JobDesc)), o_tasks = cv.need(ntask * sizeof(Task));
+    const size_t o_inv = cv.need(ninv * sizeof(InvTask)), o_piv = cv.need(npiv * 4), o_y = cv.need(ny * vb);
+    const size_t o_scale = cv.need(ninv * 8), o_bad = cv.need(ninv * 4);
+    if (cv.used > NOALLOC_BYTES)
+      return fail_with(ctx, CAROLI_EINVAL,
+                       "caroli_solve_batch_noalloc: the batch needs " + std::to_string(cv.used) +
+                           " bytes of scratch; the static scratch holds " + std::to_string(NOALLOC_BYTES) +
+                           " (solve fewer instances per call)");
+    double2* arena = reinterpret_cast<double2*>(base + o_arena);
+    double2* rarena = reinterpret_cast<double2*>(base + o_root);
+    uint8_t* fail = base + o_fail;
+    int32_t* dstatus = reinterpret_cast<int32_t*>(base + o_status);
+    double* tdev = reinterpret_cast<double*>(base + o_t);
+    double* part = reinterpret_cast<double*>(base + o_part);
+    JobDesc* djobs = reinterpret_cast<JobDesc*>(base + o_jobs);
+    Task* dtasks = reinterpret_cast<Task*>(base + o_tasks);
+    InvTask* dinv = reinterpret_cast<InvTask*>(base + o_inv);
+    // The flags and statuses the kernels only set must start at zero: the array keeps the
+    // contents of the previous call.
+    CK(cudaMemsetAsync(fail, 0, std::max<size_t>(foff, 1), s));
+    CK(cudaMemsetAsync(dstatus, 0, nj * 4, s));
+    std::vector<JobDesc> jd(nj);
+    for (size_t j = 0; j < nj; ++j) {
+      const int b = (int)(j % nb);
+      const size_t i = j / nb;
+      const DevPlan& P = *sys->plans[b];
+      const SigmaSlot& sg = sys->slots[slots[i]];
+      JobDesc& d = jd[j];
+      d.fronts = P.fronts; d.maps = P.maps; d.own = P.own; d.entries = P.entries;
+      d.arena = arena + arena_off[j];
+      d.root_arena = rarena + root_off[j];
+      d.vals = sys->vals + (size_t)configs[i] * sys->desc.row_ptr[sys->desc.n];
+      d.sigma_l = sg.sl[b]; d.sigma_r = sg.sr[b]; d.gamma_l = sg.gl[b]; d.gamma_r = sg.gr[b];
+      d.fail = fail + fail_off[j];
+      d.energy = sg.energy;
+      d.root = P.host.root; d.nl = P.host.nl; d.nr = P.host.nr; d.rpos = P.host.rpos; d.nd = P.host.nd;
+      d.nfronts = (int32_t)P.host.fronts.size();
+    }
+    // Tasks level by level: small fronts, then large ones with their sweeps; roots last.
+    std::vector<Task> tasks;
+    std::vector<InvTask> inv;
+    struct Lv { size_t s0, sn, l0, ln, i0, in; int smax, lmax, lne; };
+    std::vector<Lv> lv(max_levels);
+    size_t po = 0, yo = 0;
+    auto add_inv = [&](void* a, int n, int np, int32_t job, int32_t front) {
+      InvTask it{};
+      it.a = a; it.ld = n; it.n = n; it.npiv = np; it.job = job; it.front = front;
+      it.piv = reinterpret_cast<int32_t*>(base + o_piv) + po;
+      it.y = reinterpret_cast<double2*>(base + o_y) + yo;
+      it.scale2 = reinterpret_cast<double*>(base + o_scale) + inv.size();
+      it.bad = reinterpret_cast<int32_t*>(base + o_bad) + inv.size();
+      po += np;
+      yo += (size_t)GJ_KB * n;
+      inv.push_back(it);
+    };
+    for (int L = 0; L < max_levels; ++L) {
+      Lv& v = lv[L];
+      v = Lv{tasks.size(), 0, 0, 0, 0, 0, 0, 0, 0};
+      for (size_t j = 0; j < nj; ++j) {
+        const auto& fr = sys->plans[j % nb]->host.fronts;
+        for (size_t k = 0; k + 1 < fr.size(); ++k)
+          if (fr[k].level == L && fr[k].n <= SMALL_MAX_F64) {
+            tasks.push_back({(int32_t)j, (int32_t)k, 0});
+            v.smax = std::max(v.smax, fr[k].n);
+          }
+      }
+      v.sn = tasks.size() - v.s0;
+      v.l0 = tasks.size();
+      v.i0 = inv.size();
+      for (size_t j = 0; j < nj; ++j) {
+        const auto& fr = sys->plans[j % nb]->host.fronts;
+        for (size_t k = 0; k + 1 < fr.size(); ++k)
+          if (fr[k].level == L && fr[k].n > SMALL_MAX_F64) {
+            tasks.push_back({(int32_t)j, (int32_t)k, 0});
+            v.lmax = std::max(v.lmax, fr[k].n);
+            v.lne = std::max(v.lne, fr[k].ne);
+            if (fr[k].ne > 0) add_inv(arena + arena_off[j] + fr[k].arena_off, fr[k].n, fr[k].ne, (int32_t)j, (int32_t)k);
+          }
+      }
+      v.ln = tasks.size() - v.l0;
+      v.in = inv.size() - v.i0;
+    }
+    const size_t root0 = tasks.size(), rinv0 = inv.size();
+    for (size_t j = 0; j < nj; ++j) {
+      const FrontPlan& P = sys->plans[j % nb]->host;
+      tasks.push_back({(int32_t)j, P.root, 0});
+      const int m = P.fronts[P.root].n;
+      add_inv(rarena + root_off[j], m, m, (int32_t)j, -1);
+    }
+    CK(cudaMemcpyAsync(djobs, jd.data(), nj * sizeof(JobDesc), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dtasks, tasks.data(), tasks.size() * sizeof(Task), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dinv, inv.data(), inv.size() * sizeof(InvTask), cudaMemcpyHostToDevice, s));
+    auto sweep = [&](size_t first, size_t cnt, int nmax, int pmax, double tol) {
+      if (!cnt) return;
+      const size_t work = 2 * (size_t)nmax * vb, staged = (size_t)nmax * GJ_KB * vb + work;
+      const size_t sm = staged <= (size_t)SMEM_LIMIT ? staged : work;
+      inv_scale_kernel<double><<<(unsigned)cnt, 256, 0, s>>>(dinv + first);
+      for (int k0 = 0; k0 < pmax; k0 += GJ_KB) {
+        inv_panel_kernel<double><<<(unsigned)cnt, 256, sm, s>>>(dinv + first, k0, tol, 0, (int)sm);
+        const unsigned rt = (unsigned)((nmax + 63) / 64);
+        in_pieces(cnt, [&](size_t f0, size_t c) {
+          inv_update_kernel<double><<<dim3(rt, rt, (unsigned)c), 256, 0, s>>>(dinv + first + f0, k0);
+        });
+      }
+      inv_finish_kernel<double><<<(unsigned)cnt, 256, 0, s>>>(dinv + first, djobs, dstatus);
+    };
+    for (int L = 0; L < max_levels; ++L) {
+      const Lv& v = lv[L];
+      if (v.sn)
+        small_front_kernel<double, false><<<(unsigned)v.sn, 256, small_smem(v.smax, vb), s>>>(djobs, dtasks + v.s0,
+                                                                                              PIVOT_TOL_F64, 0, nullptr);
+      if (v.ln) {
+        in_pieces(v.ln, [&](size_t f0, size_t c) {
+          assemble_kernel<double, double><<<dim3((v.lmax + 31) / 32, (unsigned)c), 256, 0, s>>>(djobs,
+                                                                                                dtasks + v.l0 + f0, 0);
+        });
+        sweep(v.i0, v.in, v.lmax, v.lne, PIVOT_TOL_F64);
+      }
+      CK(cudaGetLastError());
+    }
+    in_pieces(nj, [&](size_t f0, size_t c) {
+      assemble_kernel<double, double><<<dim3((max_root + 31) / 32, (unsigned)c), 256, 0, s>>>(djobs, dtasks + root0 + f0, 1);
+    });
+    sweep(rinv0, nj, max_root, max_root, 0.0);
+    in_pieces(nj, [&](size_t f0, size_t c) {
+      trace_kernel<double><<<dim3((unsigned)parts, (unsigned)c), 256, 0, s>>>(djobs + f0, part + f0 * parts, (int)parts);
+    });
+    trace_finish_kernel<<<(unsigned)((nj + 127) / 128), 128, 0, s>>>(part, (int)parts, (int)nj, tdev, dstatus);
+    CK(cudaGetLastError());
+    std::vector<double> th(nj);
+    std::vector<int32_t> sh(nj);
+    std::vector<uint8_t> fh(std::max<size_t>(foff, 1));
+    CK(cudaMemcpyAsync(th.data(), tdev, nj * 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(sh.data(), dstatus, nj * 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(fh.data(), fail, std::max<size_t>(foff, 1), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    for (int i = 0; i < count; ++i) {
+      double sum = 0.0;
+      int32_t st = ST_OK;
+      for (int b = 0; b < nb; ++b) {
+        const size_t j = (size_t)i * nb + b;
+        bool delayed = false;
+        for (size_t k = 0; k < sys->plans[b]->host.fronts.size(); ++k) delayed |= fh[fail_off[j] + k] != 0;
+        int32_t sj = sh[j] != ST_OK ? sh[j] : (delayed ? ST_PIVOT_DELAYED : (std::isfinite(th[j]) ? ST_OK : ST_NONFINITE));
+        sum += th[j];
+        if (st == ST_OK) st = sj;
+      }
+      t[i] = sum;
+      status[i] = st;
+    }
+    return CAROLI_OK;
+  } catch (const CudaError& e) {
+    return fail_with(ctx, CAROLI_ECUDA, std::string(e.what) + ": " + cudaGetErrorString(e.e));
+  }
+}

@@ -98,6 +98,20 @@ int caroli_sigma_upload(caroli_ctx* ctx, int plan_id, int slot, double energy, c
 int caroli_solve_batch(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots, const int32_t* configs,
                        int precision, double* t, int32_t* status, double* err);
 
+/* The double-precision transmission of caroli_solve_batch without any device allocation: no
+ * counterpart in the reference. For callers that cannot allocate device memory while they solve
+ * (a host program whose device memory another allocator has already reserved, or a loop where
+ * allocation is not allowed). Every front, flag and work array of the call is carved from one
+ * static device array of 64 MiB that each GPU loading this library keeps until the process exits;
+ * a batch needing more is rejected with CAROLI_EINVAL and the size in caroli_last_error (solve
+ * fewer instances per call). The system, its values and self-energies must have been uploaded
+ * (those calls allocate). The first call on a device looks the array up on that device; make it
+ * before any stream capture. Calls share the array and run on the context's stream: calls that
+ * overlap on the GPU (other contexts or threads) race. Fronts that refuse their pivots are not
+ * re-planned here: those instances get CAROLI_PIVOT_DELAYED (use caroli_solve_batch for them). */
+int caroli_solve_batch_noalloc(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots, const int32_t* configs,
+                               double* t, int32_t* status);
+
 /* Timed region on the context's stream: caroli_region_end returns the device time between the
  * two calls (CUDA events on the stream every kernel of the library runs on) and the number of
  * kernels the library launched in between. */
