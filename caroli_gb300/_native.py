@@ -27,6 +27,7 @@ SIGNATURES = {
     "caroli_plan_upload": (ctypes.c_int, [P, I64, P, P, I64, ctypes.c_int, P, P, P, P, I64, P, ctypes.c_int, P, P, P,
                                           P, P, ctypes.POINTER(ctypes.c_int)]),
     "caroli_plan_info": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P, P]),
+    "caroli_plan_fronts": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, I64, P, P, P, P]),
     "caroli_values_upload": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P]),
     "caroli_sigma_upload": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, ctypes.c_double, P, P, P, P]),
     "caroli_solve_batch": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, ctypes.c_int, P, P, P]),
@@ -151,6 +152,16 @@ class Plan:
         vals = [ctypes.c_int64() for _ in range(5)]
         self.ctx.check(self.ctx.lib.caroli_plan_info(self.ctx.h, self.id, block, *[ctypes.byref(v) for v in vals]))
         return dict(zip(["fronts", "max_n", "max_ne", "root_n", "arena_elems"], [v.value for v in vals]))
+
+    def fronts(self, block):
+        """``(n, ne, level)`` arrays of the block's tree fronts (post-order)."""
+        cnt = ctypes.c_int64()
+        self.ctx.check(self.ctx.lib.caroli_plan_fronts(self.ctx.h, self.id, block, 0, None, None, None,
+                                                       ctypes.byref(cnt)))
+        n = np.zeros(cnt.value, np.int32); ne = np.zeros(cnt.value, np.int32); lv = np.zeros(cnt.value, np.int32)
+        self.ctx.check(self.ctx.lib.caroli_plan_fronts(self.ctx.h, self.id, block, cnt.value, ptr(n), ptr(ne), ptr(lv),
+                                                       ctypes.byref(cnt)))
+        return n, ne, lv
 
     def upload_values(self, values):
         v = np.ascontiguousarray(np.stack(values), dtype=np.complex128)

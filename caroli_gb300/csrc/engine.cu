@@ -23,6 +23,7 @@
 #include "plan.hpp"
 #include "refine.cuh"
 #include "dense.cuh"
+#include "tiny.cuh"
 
 using namespace caroli;
 
@@ -230,7 +231,8 @@ template <typename F> void in_pieces(size_t count, F fn) {
 }
 
 struct LevelRange {
-  size_t first, count;
+  size_t tiny0, tiny_n;  // fronts of at most TINY_MAX variables (one warp each)
+  size_t first, count;   // the others
   int max_n;
 };
 
@@ -330,6 +332,11 @@ void refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, siz
   // Preconditioner application M^-1 V_k -> Z_k (src = dst = k).
   auto sweep = [&](int src, int dst) {
     for (int L = 0; L < nlev; ++L) {
+      if (lr[L].tiny_n)
+        launch(K_REF_FWD, 0.0, 0.0, [&] {
+          tiny_forward_kernel<<<(unsigned)((lr[L].tiny_n + TINY_WARPS - 1) / TINY_WARPS), 256, 0, s>>>(
+              drd, dtasks + lr[L].tiny0, (int)lr[L].tiny_n, src);
+        });
       if (!lr[L].count) continue;
       const size_t sm = 2 * (size_t)lr[L].max_n * RCB * sizeof(float2);
       launch(K_REF_FWD, 0.0, sweep_bytes * 0.5 / nlev, [&] {
@@ -343,6 +350,11 @@ void refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, siz
       });
     });
     for (int L = nlev - 1; L >= 0; --L) {
+      if (lr[L].tiny_n)
+        launch(K_REF_BWD, 0.0, 0.0, [&] {
+          tiny_backward_kernel<<<(unsigned)((lr[L].tiny_n + TINY_WARPS - 1) / TINY_WARPS), 256, 0, s>>>(
+              drd, dtasks + lr[L].tiny0, (int)lr[L].tiny_n, src, dst);
+        });
       if (!lr[L].count) continue;
       const size_t sm = (size_t)lr[L].max_n * RCB * sizeof(float2);
       launch(K_REF_BWD, 0.0, sweep_bytes * 0.5 / nlev, [&] {
@@ -541,6 +553,7 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
 
     // Task lists: per level the small fronts then the large ones (contiguous), then the roots.
     struct Level {
+      size_t tiny0, tiny_n;
       size_t small0, small_n, large0, large_n;
       int max_small_n, max_large_n, max_large_ne, max_n;
       size_t xs_elems, inv0;
@@ -554,11 +567,22 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
     std::vector<size_t> inv_piv_off, inv_y_off;
     for (int L = 0; L < max_levels; ++L) {
       Level& lv = levels[L];
-      lv = Level{tasks.size(), 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+      lv = Level{tasks.size(), 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
       for (size_t j = 0; j < cj; ++j) {
         const auto& fr = specs[begin + j].plan->host.fronts;
         for (size_t k = 0; k + 1 < fr.size(); ++k)
-          if (fr[k].level == L && fr[k].n <= small_max) {
+          if (fr[k].level == L && fr[k].n <= TINY_MAX) {
+            tasks.push_back({(int32_t)j, (int32_t)k, 0});
+            const double ne = fr[k].ne, nb = fr[k].n - fr[k].ne;
+            lv.small_flops += 8.0 / 3 * ne * ne * ne + 8 * ne * ne * nb + 8 * nb * nb * ne;
+          }
+      }
+      lv.tiny_n = tasks.size() - lv.tiny0;
+      lv.small0 = tasks.size();
+      for (size_t j = 0; j < cj; ++j) {
+        const auto& fr = specs[begin + j].plan->host.fronts;
+        for (size_t k = 0; k + 1 < fr.size(); ++k)
+          if (fr[k].level == L && fr[k].n > TINY_MAX && fr[k].n <= small_max) {
             tasks.push_back({(int32_t)j, (int32_t)k, 0});
             const double ne = fr[k].ne, nb = fr[k].n - fr[k].ne;
             lv.max_small_n = std::max(lv.max_small_n, fr[k].n);
@@ -601,7 +625,7 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
       }
       lv.large_n = tasks.size() - lv.large0;
       lv.xs_elems = xo;
-      lv.max_n = std::max(lv.max_small_n, lv.max_large_n);
+      lv.max_n = std::max(std::max(lv.max_small_n, lv.max_large_n), lv.tiny_n ? TINY_MAX : 0);
     }
     const size_t root0 = tasks.size(), rinv0 = inv.size();
     int max_root = 0;
@@ -679,6 +703,17 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
     // Factorization, level by level.
     for (int L = 0; L < max_levels; ++L) {
       const Level& lv = levels[L];
+      if (lv.tiny_n) {
+        const unsigned blocks = (unsigned)((lv.tiny_n + TINY_WARPS - 1) / TINY_WARPS);
+        launch(K_SMALL, 0.0, 0.0, [&] {
+          if (mixed)
+            tiny_front_kernel<T, true><<<blocks, 256, tiny_smem<T>(), s>>>(djobs, dtasks + lv.tiny0, (int)lv.tiny_n,
+                                                                           Prec<T>::tol, perturb, pert);
+          else
+            tiny_front_kernel<T, false><<<blocks, 256, tiny_smem<T>(), s>>>(djobs, dtasks + lv.tiny0, (int)lv.tiny_n,
+                                                                            Prec<T>::tol, perturb, pert);
+        });
+      }
       if (lv.small_n) {
         const size_t sm = small_smem(lv.max_small_n, vb);
         launch(K_SMALL, lv.small_flops, lv.small_bytes, [&] {
@@ -734,7 +769,7 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
     } else {
       if constexpr (std::is_same<T, float>::value && std::is_same<TR, float>::value) {
         std::vector<LevelRange> lr;
-        for (const Level& lv : levels) lr.push_back({lv.small0, lv.small_n + lv.large_n, lv.max_n});
+        for (const Level& lv : levels) lr.push_back({lv.tiny0, lv.tiny_n, lv.small0, lv.small_n + lv.large_n, lv.max_n});
         refine(ctx, sys, specs, begin, cj, lr, max_root, dtasks, jd, arena, arena_off, rarena, root_off, launch, th,
                eh, sh, ih);
       }
@@ -940,6 +975,8 @@ int caroli_ctx_create(int device_ordinal, caroli_ctx** out) {
                     (const void*)small_front_kernel<double, true>, (const void*)small_front_kernel<float, true>,
                     (const void*)pivot_block_kernel<double>, (const void*)pivot_block_kernel<float>,
                     (const void*)inv_panel_kernel<double>, (const void*)inv_panel_kernel<float>,
+                    (const void*)tiny_front_kernel<double, false>, (const void*)tiny_front_kernel<double, true>,
+                    (const void*)tiny_front_kernel<float, false>, (const void*)tiny_front_kernel<float, true>,
                     (const void*)refine_forward_kernel, (const void*)refine_backward_kernel,
                     (const void*)refine_root_kernel})
       CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_LIMIT));
@@ -1064,6 +1101,21 @@ int caroli_plan_info(caroli_ctx* ctx, int plan_id, int block, int64_t* fronts, i
   if (max_ne) *max_ne = p.max_ne;
   if (root_n) *root_n = p.fronts[p.root].n;
   if (arena_elems) *arena_elems = p.arena_elems;
+  return CAROLI_OK;
+}
+
+int caroli_plan_fronts(caroli_ctx* ctx, int plan_id, int block, int64_t capacity, int32_t* n, int32_t* ne,
+                       int32_t* level, int64_t* count) {
+  System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
+  if (!sys || block < 0 || block >= (int)sys->plans.size()) return fail_with(ctx, CAROLI_EINVAL, "unknown plan or block");
+  const auto& fr = sys->plans[block]->host.fronts;
+  const int64_t m = (int64_t)fr.size() - 1;  // tree fronts, without the root
+  if (count) *count = m;
+  for (int64_t k = 0; k < std::min(m, capacity); ++k) {
+    if (n) n[k] = fr[k].n;
+    if (ne) ne[k] = fr[k].ne;
+    if (level) level[k] = fr[k].level;
+  }
   return CAROLI_OK;
 }
 

@@ -1,0 +1,223 @@
+// Fronts of at most 32 variables, one warp each (eight per CTA): three quarters of the fronts of a
+// 2D nested-dissection tree are this small (leaves and the separators just above them) and carry
+// about 2 % of the flops, so a block-wide synchronisation per pivot would dominate their cost.
+// Lane i owns row i of the front; the warp synchronises with __syncwarp only.
+//
+// tiny_front_kernel is small_front_kernel (same assembly, same Gauss-Jordan sweep and pivot test,
+// same factor layout [F11^-1 X; W S]); tiny_forward/backward_kernel are the refinement sweeps of
+// refine.cuh for these fronts.
+#pragma once
+#include "kernels.cuh"
+#include "refine.cuh"
+
+namespace caroli {
+
+constexpr int TINY_MAX = 32;
+constexpr int TINY_WARPS = 8;
+
+// Dynamic shared memory of tiny_front_kernel.
+template <typename T> constexpr size_t tiny_smem() {
+  return (size_t)TINY_WARPS * (TINY_MAX * (TINY_MAX + 1) + TINY_MAX) * sizeof(typename Cx<T>::V);
+}
+
+template <typename T, bool KEEP>
+__global__ void __launch_bounds__(256) tiny_front_kernel(const JobDesc* __restrict__ jobs, const Task* __restrict__ tasks,
+                                                         int ntasks, double tol, int perturb, int* __restrict__ perturbed) {
+  using V = typename Cx<T>::V;
+  constexpr int LD = TINY_MAX + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];  // per warp: front (32 x 33) and pivot row
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ti = blockIdx.x * TINY_WARPS + w;
+  if (ti >= ntasks) return;
+  const Task t = tasks[ti];
+  const JobDesc& J = jobs[t.job];
+  const FrontDesc f = J.fronts[t.front];
+  const int n = f.n, ne = f.ne;
+  V* F = reinterpret_cast<V*>(smem_raw) + (size_t)w * (TINY_MAX * LD + TINY_MAX);
+  V* prow = F + TINY_MAX * LD;
+  // Assembly: lane i builds row i.
+  if (lane < n)
+    for (int j = 0; j < n; ++j) F[lane + j * LD] = gather<T>(J, f, lane, j, false);
+  __syncwarp();
+  for (int64_t e = lane; e < f.ent_cnt; e += 32) {
+    const Entry en = J.entries[f.ent_off + e];
+    double2 h = J.vals[en.q];
+    if (en.conj) h.y = -h.y;
+    V& d = F[en.a + en.b * LD];
+    d = csub(d, from64<V>(h));
+  }
+  __syncwarp();
+  V* out = static_cast<V*>(J.arena) + f.arena_off;
+  if (ne > 0) {
+    double scale2 = 0.0;
+    if (lane < ne)
+      for (int j = 0; j < ne; ++j) scale2 = fmax(scale2, cabs2(F[lane + j * LD]));
+    for (int o = 16; o > 0; o >>= 1) scale2 = fmax(scale2, __shfl_xor_sync(0xffffffffu, scale2, o));
+    const double thresh = tol * tol * scale2;
+    int mypiv = 0;  // lane k keeps piv[k]
+    for (int k = 0; k < ne; ++k) {
+      double best = (lane >= k && lane < ne) ? cabs2(F[lane + k * LD]) : -1.0;
+      int bi = (lane >= k && lane < ne) ? lane : 0x7fffffff;
+      for (int o = 16; o > 0; o >>= 1) {
+        const double b2 = __shfl_xor_sync(0xffffffffu, best, o);
+        const int i2 = __shfl_xor_sync(0xffffffffu, bi, o);
+        argmax_pair(best, bi, b2, i2);
+      }
+      int p = bi;
+      if (!(best > thresh) || p >= ne) {
+        if (!perturb || !(best >= 0.0) || !(scale2 > 0.0) || p >= ne) {
+          if (lane == 0) J.fail[t.front] = 1;
+          return;
+        }
+        if (lane == 0) {
+          V& d = F[p + k * LD];
+          const double mag = sqrt(best), target = tol * sqrt(scale2);
+          if (mag > 0.0) { d.x = (T)(d.x / mag * target); d.y = (T)(d.y / mag * target); }
+          else { d.x = (T)target; d.y = (T)0; }
+          if (perturbed) atomicAdd(perturbed + t.job, 1);
+        }
+        __syncwarp();
+      }
+      if (lane == k) mypiv = p;
+      if (p != k && lane < n) {
+        const V a = F[k + lane * LD];
+        F[k + lane * LD] = F[p + lane * LD];
+        F[p + lane * LD] = a;
+      }
+      __syncwarp();
+      const V inv = cinv(F[k + k * LD]);
+      if (lane < n) prow[lane] = (lane == k) ? inv : cmul(F[k + lane * LD], inv);
+      __syncwarp();
+      if (lane < n) {
+        const V ck = F[lane + k * LD];
+        for (int j = 0; j < n; ++j) {
+          V* d = &F[lane + j * LD];
+          if (lane == k) *d = prow[j];
+          else if (j == k) *d = cmul(cx<V>(-ck.x, -ck.y), inv);
+          else *d = cfms(*d, ck, prow[j]);
+        }
+      }
+      __syncwarp();
+    }
+    // Undo the interchanges on the columns, last first (lane i moves its own row's entries).
+    for (int k = ne - 1; k >= 0; --k) {
+      const int p = __shfl_sync(0xffffffffu, mypiv, k);
+      if (p != k && lane < n) {
+        const V a = F[lane + k * LD];
+        F[lane + k * LD] = F[lane + p * LD];
+        F[lane + p * LD] = a;
+      }
+    }
+    __syncwarp();
+  }
+  if (lane < n)
+    for (int j = 0; j < n; ++j) {
+      if (ne > 0 && !KEEP && (lane < ne || j < ne)) continue;
+      out[lane + (int64_t)j * n] = F[lane + j * LD];
+    }
+}
+
+// Forward sweep for tiny fronts: t = F11^-1 z_e, h = z_b + W z_e.
+__global__ void __launch_bounds__(256) tiny_forward_kernel(RefineDesc* __restrict__ rd, const Task* __restrict__ tasks,
+                                                           int ntasks, int src) {
+  __shared__ float2 Zs[TINY_WARPS][TINY_MAX * RCB];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ti = blockIdx.x * TINY_WARPS + w;
+  if (ti >= ntasks) return;
+  const Task tk = tasks[ti];
+  const RefineDesc& R = rd[tk.job];
+  if (R.done || (src >= 0 && R.inner_done)) return;
+  const double2* rin = sweep_src(R, src);
+  const FrontDesc f = R.fronts[tk.front];
+  const int n = f.n, ne = f.ne, nb = n - ne;
+  const float2* F = R.arena + f.arena_off;
+  float2* z = Zs[w];
+  for (int j0 = 0; j0 < R.c; j0 += RCB) {
+    const int cb = min(RCB, R.c - j0);
+    if (lane < n) {
+      const bool own = R.own[f.own_off + lane];
+      const int row = R.vidx[f.var_off + lane];
+      int ca[2] = {-1, -1};
+      for (int c = 0; c < f.nchild; ++c) ca[c] = R.maps[f.map_off[c] + lane];
+      for (int j = 0; j < RCB; ++j) {
+        float2 v = make_float2(0.f, 0.f);
+        if (j < cb) {
+          if (own) v = f2(rin[row + (int64_t)(j0 + j) * R.nblk]);
+          for (int c = 0; c < f.nchild; ++c)
+            if (ca[c] >= 0) {
+              const FrontDesc& cf = R.fronts[f.child[c]];
+              const float2 h = R.hb[(cf.hoff + ca[c]) + (int64_t)(j0 + j) * R.sum_nb];
+              v.x += h.x; v.y += h.y;
+            }
+        }
+        z[lane * RCB + j] = v;
+      }
+    }
+    __syncwarp();
+    if (lane < n) {
+      float2 acc[RCB];
+      const bool top = lane < ne;
+#pragma unroll
+      for (int j = 0; j < RCB; ++j) acc[j] = top ? make_float2(0.f, 0.f) : z[lane * RCB + j];
+      // Row `lane` of [F11^-1; W] times z_e.
+      for (int k = 0; k < ne; ++k) {
+        const float2 a = F[lane + (int64_t)k * n];
+#pragma unroll
+        for (int j = 0; j < RCB; ++j) acc[j] = cfma(acc[j], a, z[k * RCB + j]);
+      }
+#pragma unroll
+      for (int j = 0; j < RCB; ++j) {
+        if (j >= cb) continue;
+        if (top) R.tb[(f.toff + lane) + (int64_t)(j0 + j) * R.sum_ne] = acc[j];
+        else R.hb[(f.hoff + lane - ne) + (int64_t)(j0 + j) * R.sum_nb] = acc[j];
+      }
+    }
+    __syncwarp();
+  }
+  (void)nb;
+}
+
+// Backward sweep for tiny fronts: x_e = t - X x_b.
+__global__ void __launch_bounds__(256) tiny_backward_kernel(RefineDesc* __restrict__ rd, const Task* __restrict__ tasks,
+                                                            int ntasks, int src, int dst) {
+  __shared__ float2 Xs[TINY_WARPS][TINY_MAX * RCB];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ti = blockIdx.x * TINY_WARPS + w;
+  if (ti >= ntasks) return;
+  const Task tk = tasks[ti];
+  const RefineDesc& R = rd[tk.job];
+  if (R.done || (src >= 0 && R.inner_done)) return;
+  float2* dout = sweep_dst(R, dst);
+  const FrontDesc f = R.fronts[tk.front];
+  const int n = f.n, ne = f.ne, nb = n - ne;
+  if (ne == 0) return;
+  const float2* F = R.arena + f.arena_off;
+  float2* xb = Xs[w];
+  for (int j0 = 0; j0 < R.c; j0 += RCB) {
+    const int cb = min(RCB, R.c - j0);
+    if (lane < nb) {
+      const int row = R.vidx[f.var_off + ne + lane];
+      for (int j = 0; j < RCB; ++j)
+        xb[lane * RCB + j] = j < cb ? dout[row + (int64_t)(j0 + j) * R.nblk] : make_float2(0.f, 0.f);
+    }
+    __syncwarp();
+    if (lane < ne) {
+      float2 acc[RCB];
+#pragma unroll
+      for (int j = 0; j < RCB; ++j)
+        acc[j] = j < cb ? R.tb[(f.toff + lane) + (int64_t)(j0 + j) * R.sum_ne] : make_float2(0.f, 0.f);
+      for (int k = 0; k < nb; ++k) {
+        const float2 a = F[lane + (int64_t)(ne + k) * n];
+#pragma unroll
+        for (int j = 0; j < RCB; ++j) acc[j] = cfms(acc[j], a, xb[k * RCB + j]);
+      }
+      const int row = R.vidx[f.var_off + lane];
+#pragma unroll
+      for (int j = 0; j < RCB; ++j)
+        if (j < cb) dout[row + (int64_t)(j0 + j) * R.nblk] = acc[j];
+    }
+    __syncwarp();
+  }
+}
+
+}  // namespace caroli

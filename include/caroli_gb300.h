@@ -75,6 +75,11 @@ int caroli_plan_upload(caroli_ctx* ctx, int64_t n, const int64_t* row_ptr, const
 int caroli_plan_info(caroli_ctx* ctx, int plan_id, int block, int64_t* fronts, int64_t* max_n, int64_t* max_ne,
                      int64_t* root_n, int64_t* arena_elems);
 
+/* The tree fronts of a block in post-order (up to `capacity`; *count = all): variables n, variables
+ * eliminated ne, execution level (children run at lower levels). No device work. */
+int caroli_plan_fronts(caroli_ctx* ctx, int plan_id, int block, int64_t capacity, int32_t* n, int32_t* ne,
+                       int32_t* level, int64_t* count);
+
 /* H values of `nconfigs` disorder configurations on the plan's pattern: values[c*nnz + q] as
  * interleaved complex128 (re, im). Replaces previously uploaded values. */
 int caroli_values_upload(caroli_ctx* ctx, int plan_id, int nconfigs, const double* values);

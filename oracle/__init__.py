@@ -37,6 +37,7 @@ def lib():
         L.oracle_solve_batch.argtypes = [P, ctypes.c_int64, P, P, P, P, P, ctypes.c_int, ctypes.c_int, P, P]
         L.oracle_free.argtypes = [P]
         L.oracle_tree_info.argtypes = [P, ctypes.c_int, P, P, P]
+        L.oracle_tree_fronts.argtypes = [P, ctypes.c_int, ctypes.c_int64, P, P]
         _lib = L
     return _lib
 
@@ -88,6 +89,13 @@ class Oracle:
         a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
         lib().oracle_tree_info(self.h, block, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
         return a.value, b.value, c.value
+
+    def tree_fronts(self, block):
+        nodes = self.tree_info(block)[0]
+        n = np.zeros(nodes, np.int32)
+        ne = np.zeros(nodes, np.int32)
+        lib().oracle_tree_fronts(self.h, block, nodes, _p(n), _p(ne))
+        return n, ne
 
     def solve_block(self, block, energy, vals, sigma_l, sigma_r, precision=0, want_g=False):
         """``(status, T, G_LR or None, delayed count)`` for one block."""

@@ -638,6 +638,17 @@ int oracle_solve_batch(void* handle, int64_t count, const int32_t* blocks, const
   return 0;
 }
 
+// Sizes of the planned fronts of a block in post-order: n = separator + boundary, ne = separator.
+int oracle_tree_fronts(void* handle, int block, int64_t capacity, int32_t* n, int32_t* ne) {
+  const System& sys = *static_cast<System*>(handle);
+  const Tree& t = sys.blocks[block].tree;
+  for (size_t k = 0; k < t.nodes.size() && (int64_t)k < capacity; ++k) {
+    n[k] = (int32_t)(t.plans[k].vars.size());
+    ne[k] = (int32_t)t.plans[k].ne;
+  }
+  return (int)t.nodes.size();
+}
+
 int oracle_tree_info(void* handle, int block, int64_t* nodes, int64_t* max_ne, int64_t* max_nb) {
   const System& sys = *static_cast<System*>(handle);
   const Tree& t = sys.blocks[block].tree;
