@@ -184,6 +184,11 @@ def run_ours(args):
     nsolve = len(pairs)
     for _ in range(args.warmup):
         sys_.solve_batch(S, C, Precision.MIXED)
+    if args.profile_run:
+        # One step of the mixed path and nothing else (for a profiler's launch list).
+        sys_.solve_batch(S, C, Precision.MIXED)
+        print(json.dumps({"profile_run": True, "solves": nsolve, "launches": plan.last_timing()[1]}))
+        return
     # Timed region: K steps of the mixed path, inputs resident.
     barrier(dist, torch)
     with Clocks(local) as clk:
@@ -338,6 +343,7 @@ def main():
     ap.add_argument("--energies", type=int, default=33)
     ap.add_argument("--cpu-sample", type=int, default=32)
     ap.add_argument("--ref-sample", type=int, default=32)
+    ap.add_argument("--profile-run", action="store_true", help="warm-up steps and one step, no timing (profilers)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -80,7 +80,8 @@ class Context:
         h = ctypes.c_void_p()
         rc = lib.caroli_ctx_create(device, ctypes.byref(h))
         if rc != OK:
-            raise NativeError(rc, "no usable CUDA device" if rc == EUNAVAILABLE else "caroli_ctx_create failed")
+            why = "no usable CUDA device" if rc == EUNAVAILABLE else lib.caroli_last_error(None).decode()
+            raise NativeError(rc, f"caroli_ctx_create: {why}")
         self.h = h
         self.lib = lib
 

@@ -42,12 +42,12 @@ __global__ void __launch_bounds__(256) inv_scale_kernel(const InvTask* __restric
   __shared__ double red[32];
   const InvTask t = tasks[blockIdx.x];
   const V* A = static_cast<const V*>(t.a);
-  double m = 0.0;
+  T mt = 0;
   for (int64_t idx = threadIdx.x; idx < (int64_t)t.npiv * t.npiv; idx += blockDim.x) {
     const int i = (int)(idx % t.npiv), j = (int)(idx / t.npiv);
-    m = fmax(m, cabs2(A[i + (int64_t)j * t.ld]));
+    mt = fmax(mt, cnorm(A[i + (int64_t)j * t.ld]));
   }
-  m = block_max(m, red);
+  const double m = block_max((double)mt, red);
   if (threadIdx.x == 0) {
     *t.scale2 = m;
     *t.bad = 0;
@@ -93,14 +93,14 @@ __global__ void __launch_bounds__(256) inv_panel_kernel(const InvTask* __restric
   const double thresh = tol * tol * scale2;
   for (int kk = 0; kk < kb; ++kk) {
     const int k = k0 + kk;
-    double best = -1.0;
+    T best = -1;
     int bi = 0x7fffffff;
     for (int i = k + threadIdx.x; i < np; i += blockDim.x) {
-      const double m = cabs2(P[i + kk * pld]);
+      const T m = cnorm(P[i + kk * pld]);
       if (m > best) { best = m; bi = i; }
     }
     double big;
-    const int p = block_argmax(best, bi, redv, redi, &big);
+    const int p = block_argmax((double)best, bi, redv, redi, &big);
     if (!(big > thresh) || p >= np) {
       if (!perturb || !(big >= 0.0) || !(scale2 > 0.0) || p >= np) {
         if (threadIdx.x == 0) *t.bad = 1;

@@ -53,9 +53,13 @@ template <typename T> T* dalloc(size_t count) {
   return static_cast<T*>(p);
 }
 
+// Source of plan identities (never reused, unlike addresses of freed plans).
+uint64_t g_plan_generation = 0;
+
 // Device copy of a front plan.
 struct DevPlan {
   FrontPlan host;
+  uint64_t id = ++g_plan_generation;
   FrontDesc* fronts = nullptr;
   int32_t* maps = nullptr;
   uint8_t* own = nullptr;
@@ -167,6 +171,32 @@ struct JobSpec {
   const DevPlan* plan;
 };
 
+// One tree level of a batch: its fronts split by size class, and their algorithmic work.
+struct TaskLevel {
+  size_t tiny0 = 0, tiny_n = 0;
+  size_t small0 = 0, small_n = 0, large0 = 0, large_n = 0;
+  int max_small_n = 0, max_large_n = 0, max_large_ne = 0, max_n = 0;
+  size_t xs_elems = 0, inv0 = 0;
+  double small_flops = 0, small_bytes = 0, inv_flops = 0, gemm0_flops = 0, gemm1_flops = 0, asm_bytes = 0;
+};
+
+// The task lists of the last batch (see run_jobs).
+struct TaskCache {
+  bool valid = false;
+  std::vector<uint64_t> plans;  // identities of the chunk's plans
+  int tsize = 0, trsize = 0, max_levels = 0;
+  bool mixed = false;
+  const void *arena = nullptr, *rarena = nullptr;
+  std::vector<Task> tasks;
+  std::vector<TaskLevel> levels;
+  std::vector<InvTask> inv;
+  std::vector<size_t> inv_piv_off, inv_y_off;
+  size_t inv_piv = 0, inv_y = 0, root0 = 0, rinv0 = 0;
+  int max_root = 0;
+  double root_flops = 0.0, trace_flops = 0.0;
+  const void *piv = nullptr, *y = nullptr, *scale = nullptr, *bad = nullptr, *dinv = nullptr, *dtasks = nullptr;
+};
+
 }  // namespace
 
 struct caroli_ctx {
@@ -184,10 +214,11 @@ struct caroli_ctx {
   Buf arena, root_arena, xs, jobs, tasks, fail, status, tout, part, pert;
   Buf rdesc, rx, rr, rd, rtb, rhb, rt, rerr, rdone;
   Buf inv, ipiv, iy, iscale, ibad;
+  TaskCache tcache;
   Buf gV, gZ, gH, gg, gcs, gsn, gy, gbeta, gcol, gflags;
   double inner_tol = 1e-10;
   int max_iters = 6;
-  double refine_tol = 1e-12;
+  double refine_tol = 1e-10;
   double last_ms = 0.0;
   int64_t last_launches = 0;
   int64_t fallbacks = 0;
@@ -197,6 +228,9 @@ struct caroli_ctx {
 };
 
 namespace {
+
+// Why the last caroli_ctx_create failed (caroli_last_error(NULL)).
+std::string g_create_error = "no context";
 
 int fail_with(caroli_ctx* ctx, int code, const std::string& msg) {
   if (ctx) ctx->err = msg;
@@ -338,9 +372,11 @@ void refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, siz
               drd, dtasks + lr[L].tiny0, (int)lr[L].tiny_n, src);
         });
       if (!lr[L].count) continue;
-      const size_t sm = 2 * (size_t)lr[L].max_n * RCB * sizeof(float2);
+      const size_t sm = (size_t)lr[L].max_n * RCB * sizeof(float2);
+      const unsigned rows = (unsigned)((lr[L].max_n + SW_ROWS - 1) / SW_ROWS);
       launch(K_REF_FWD, 0.0, sweep_bytes * 0.5 / nlev, [&] {
-        refine_forward_kernel<<<dim3((unsigned)lr[L].count, cchunks), 256, sm, s>>>(drd, dtasks + lr[L].first, src);
+        refine_forward_rows_kernel<<<dim3((unsigned)lr[L].count, rows, cchunks), 256, sm, s>>>(
+            drd, dtasks + lr[L].first, src);
       });
     }
     in_pieces(cj, [&](size_t f0, size_t c) {
@@ -357,9 +393,10 @@ void refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, siz
         });
       if (!lr[L].count) continue;
       const size_t sm = (size_t)lr[L].max_n * RCB * sizeof(float2);
+      const unsigned rows = (unsigned)((lr[L].max_n + SW_ROWS - 1) / SW_ROWS);
       launch(K_REF_BWD, 0.0, sweep_bytes * 0.5 / nlev, [&] {
-        refine_backward_kernel<<<dim3((unsigned)lr[L].count, cchunks), 256, sm, s>>>(drd, dtasks + lr[L].first, src,
-                                                                                    dst);
+        refine_backward_rows_kernel<<<dim3((unsigned)lr[L].count, rows, cchunks), 256, sm, s>>>(
+            drd, dtasks + lr[L].first, src, dst);
       });
     }
   };
@@ -552,22 +589,40 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
     CK(cudaMemcpyAsync(djobs, jd.data(), cj * sizeof(JobDesc), cudaMemcpyHostToDevice, s));
 
     // Task lists: per level the small fronts then the large ones (contiguous), then the roots.
-    struct Level {
-      size_t tiny0, tiny_n;
-      size_t small0, small_n, large0, large_n;
-      int max_small_n, max_large_n, max_large_ne, max_n;
-      size_t xs_elems, inv0;
-      double small_flops, small_bytes, inv_flops, gemm0_flops, gemm1_flops, asm_bytes;
-    };
-    std::vector<Task> tasks;
-    std::vector<Level> levels(max_levels);
-    std::vector<InvTask> inv;  // large fronts' pivot blocks per level, then the roots
+    // Built once per distinct batch (the plans of the chunk, precisions and arena addresses) and
+    // kept with its device copies: a repeated batch reuses them without host work.
+    using Level = TaskLevel;
+    TaskCache& tc = ctx->tcache;
+    std::vector<uint64_t> key_plans(cj);
+    for (size_t j = 0; j < cj; ++j) key_plans[j] = specs[begin + j].plan->id;
+    const bool hit = tc.valid && tc.plans == key_plans && tc.tsize == (int)sizeof(T) && tc.trsize == (int)sizeof(TR) &&
+                     tc.mixed == mixed && tc.arena == (const void*)arena && tc.rarena == (const void*)rarena &&
+                     tc.max_levels == max_levels;
+    std::vector<Task>& tasks = tc.tasks;
+    std::vector<Level>& levels = tc.levels;
+    std::vector<InvTask>& inv = tc.inv;  // large fronts' pivot blocks per level, then the roots
     const int small_max = Prec<T>::small_max;
-    size_t inv_piv = 0, inv_y = 0;  // scratch sizes: pivots (entries) and Y blocks (bytes)
-    std::vector<size_t> inv_piv_off, inv_y_off;
+    size_t& inv_piv = tc.inv_piv;  // scratch sizes: pivots (entries) and Y blocks (bytes)
+    size_t& inv_y = tc.inv_y;
+    std::vector<size_t>& inv_piv_off = tc.inv_piv_off;
+    std::vector<size_t>& inv_y_off = tc.inv_y_off;
+    size_t& root0 = tc.root0;
+    size_t& rinv0 = tc.rinv0;
+    int& max_root = tc.max_root;
+    double& root_flops = tc.root_flops;
+    double& trace_flops = tc.trace_flops;
+    if (!hit) {
+    tc.valid = false;
+    tasks.clear();
+    levels.assign(max_levels, Level{});
+    inv.clear();
+    inv_piv = inv_y = 0;
+    inv_piv_off.clear();
+    inv_y_off.clear();
     for (int L = 0; L < max_levels; ++L) {
       Level& lv = levels[L];
-      lv = Level{tasks.size(), 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+      lv = Level{};
+      lv.tiny0 = tasks.size();
       for (size_t j = 0; j < cj; ++j) {
         const auto& fr = specs[begin + j].plan->host.fronts;
         for (size_t k = 0; k + 1 < fr.size(); ++k)
@@ -627,9 +682,10 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
       lv.xs_elems = xo;
       lv.max_n = std::max(std::max(lv.max_small_n, lv.max_large_n), lv.tiny_n ? TINY_MAX : 0);
     }
-    const size_t root0 = tasks.size(), rinv0 = inv.size();
-    int max_root = 0;
-    double root_flops = 0.0, trace_flops = 0.0;
+    root0 = tasks.size();
+    rinv0 = inv.size();
+    max_root = 0;
+    root_flops = trace_flops = 0.0;
     for (size_t j = 0; j < cj; ++j) {
       const auto& P = specs[begin + j].plan->host;
       tasks.push_back({(int32_t)j, P.root, 0});
@@ -650,22 +706,36 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
       inv_y += (size_t)GJ_KB * m * vr;
       inv.push_back(it);
     }
+    }  // !hit
     // Inverse scratch: pivots, the Y blocks (sized for the wider type), scale and flags.
     int32_t* dpiv = static_cast<int32_t*>(ctx->ipiv.get(std::max<size_t>(inv_piv, 1) * sizeof(int32_t)));
     unsigned char* dy = static_cast<unsigned char*>(ctx->iy.get(std::max<size_t>(inv_y, 16)));
     double* dscale = static_cast<double*>(ctx->iscale.get(std::max<size_t>(inv.size(), 1) * sizeof(double)));
     int32_t* dbad = static_cast<int32_t*>(ctx->ibad.get(std::max<size_t>(inv.size(), 1) * sizeof(int32_t)));
-    for (size_t q = 0; q < inv.size(); ++q) {
-      inv[q].piv = dpiv + inv_piv_off[q];
-      inv[q].y = dy + inv_y_off[q];
-      inv[q].scale2 = dscale + q;
-      inv[q].bad = dbad + q;
-    }
     InvTask* dinv = static_cast<InvTask*>(ctx->inv.get(std::max<size_t>(inv.size(), 1) * sizeof(InvTask)));
-    if (!inv.empty())
-      CK(cudaMemcpyAsync(dinv, inv.data(), inv.size() * sizeof(InvTask), cudaMemcpyHostToDevice, s));
     Task* dtasks = static_cast<Task*>(ctx->tasks.get(tasks.size() * sizeof(Task)));
-    CK(cudaMemcpyAsync(dtasks, tasks.data(), tasks.size() * sizeof(Task), cudaMemcpyHostToDevice, s));
+    const bool same_scratch = hit && tc.piv == dpiv && tc.y == dy && tc.scale == dscale && tc.bad == dbad &&
+                              tc.dinv == dinv && tc.dtasks == dtasks;
+    if (!same_scratch) {
+      for (size_t q = 0; q < inv.size(); ++q) {
+        inv[q].piv = dpiv + inv_piv_off[q];
+        inv[q].y = dy + inv_y_off[q];
+        inv[q].scale2 = dscale + q;
+        inv[q].bad = dbad + q;
+      }
+      if (!inv.empty())
+        CK(cudaMemcpyAsync(dinv, inv.data(), inv.size() * sizeof(InvTask), cudaMemcpyHostToDevice, s));
+      CK(cudaMemcpyAsync(dtasks, tasks.data(), tasks.size() * sizeof(Task), cudaMemcpyHostToDevice, s));
+      tc.piv = dpiv; tc.y = dy; tc.scale = dscale; tc.bad = dbad; tc.dinv = dinv; tc.dtasks = dtasks;
+    }
+    tc.plans = key_plans;
+    tc.tsize = (int)sizeof(T);
+    tc.trsize = (int)sizeof(TR);
+    tc.mixed = mixed;
+    tc.arena = arena;
+    tc.rarena = rarena;
+    tc.max_levels = max_levels;
+    tc.valid = true;
     size_t xs_max = 1;
     for (auto& lv : levels) xs_max = std::max(xs_max, lv.xs_elems);
     V* xs = static_cast<V*>(ctx->xs.get(xs_max * vb));
@@ -971,6 +1041,8 @@ int caroli_ctx_create(int device_ordinal, caroli_ctx** out) {
     size_t free_b = 0, total_b = 0;
     CK(cudaMemGetInfo(&free_b, &total_b));
     ctx->mem_budget = free_b / 2;
+    int optin = 0;
+    CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_ordinal));
     for (auto* k : {(const void*)small_front_kernel<double, false>, (const void*)small_front_kernel<float, false>,
                     (const void*)small_front_kernel<double, true>, (const void*)small_front_kernel<float, true>,
                     (const void*)pivot_block_kernel<double>, (const void*)pivot_block_kernel<float>,
@@ -978,9 +1050,16 @@ int caroli_ctx_create(int device_ordinal, caroli_ctx** out) {
                     (const void*)tiny_front_kernel<double, false>, (const void*)tiny_front_kernel<double, true>,
                     (const void*)tiny_front_kernel<float, false>, (const void*)tiny_front_kernel<float, true>,
                     (const void*)refine_forward_kernel, (const void*)refine_backward_kernel,
-                    (const void*)refine_root_kernel})
-      CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_LIMIT));
+                    (const void*)refine_forward_rows_kernel, (const void*)refine_backward_rows_kernel,
+                    (const void*)refine_root_kernel}) {
+      // Dynamic shared memory up to SMEM_LIMIT, less what the kernel declares statically.
+      cudaFuncAttributes fa;
+      CK(cudaFuncGetAttributes(&fa, k));
+      const int room = std::min<int>(SMEM_LIMIT, optin - (int)fa.sharedSizeBytes);
+      CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, room));
+    }
   } catch (const CudaError& e) {
+    g_create_error = std::string(e.what) + ": " + cudaGetErrorString(e.e);
     return CAROLI_ECUDA;
   }
   *out = ctx.release();
@@ -1006,7 +1085,7 @@ void caroli_ctx_destroy(caroli_ctx* ctx) {
   delete ctx;
 }
 
-const char* caroli_last_error(const caroli_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+const char* caroli_last_error(const caroli_ctx* ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
 
 int caroli_plan_upload(caroli_ctx* ctx, int64_t n, const int64_t* row_ptr, const uint32_t* cols, int64_t nsites,
                        int dim, const int64_t* cells, const int64_t* site_offsets, const int64_t* site_orbitals,

@@ -74,10 +74,13 @@ template <typename V> __device__ __forceinline__ V cfma(V acc, V a, V b) {
   acc.y = fma(a.x, b.y, fma(a.y, b.x, acc.y));
   return acc;
 }
+// |a|^2 in the precision of a (comparisons of pivot candidates; FP64 is 1/64 rate on GB300).
+template <typename V> __device__ __forceinline__ auto cnorm(V a) -> decltype(a.x) { return a.x * a.x + a.y * a.y; }
+
 // 1 / a with a scaling step (Smith's method) against overflow of |a|^2.
 template <typename V> __device__ __forceinline__ V cinv(V a) {
   V r;
-  if (fabs((double)a.x) >= fabs((double)a.y)) {
+  if (fabs(a.x) >= fabs(a.y)) {
     auto q = a.y / a.x;
     auto d = a.x + a.y * q;
     r.x = 1 / d; r.y = -q / d;
@@ -202,22 +205,22 @@ __device__ bool gj_sweep(typename Cx<T>::V* F, int64_t ld, int n, int ne, double
                          int* perturbed = nullptr) {
   using V = typename Cx<T>::V;
   const int tid = threadIdx.x, nt = blockDim.x;
-  double local = 0.0;
+  T local = 0;
   for (int64_t idx = tid; idx < (int64_t)ne * ne; idx += nt) {
     int i = (int)(idx % ne), j = (int)(idx / ne);
-    local = fmax(local, cabs2(F[i + j * ld]));
+    local = fmax(local, cnorm(F[i + j * ld]));
   }
-  const double scale2 = block_max(local, redv);
+  const double scale2 = block_max((double)local, redv);
   const double thresh = tol * tol * scale2;
   for (int k = 0; k < ne; ++k) {
-    double best = -1.0;
+    T best = -1;
     int bi = 0x7fffffff;
     for (int i = k + tid; i < ne; i += nt) {
-      double m = cabs2(F[i + k * ld]);
+      const T m = cnorm(F[i + k * ld]);
       if (m > best) { best = m; bi = i; }
     }
     double big;
-    int p = block_argmax(best, bi, redv, redi, &big);
+    int p = block_argmax((double)best, bi, redv, redi, &big);
     if (!(big > thresh) || p >= ne) {
       if (!perturb) return false;
       // NaN or an empty column: nothing sensible to perturb.

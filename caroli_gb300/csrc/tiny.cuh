@@ -49,20 +49,22 @@ __global__ void __launch_bounds__(256) tiny_front_kernel(const JobDesc* __restri
   __syncwarp();
   V* out = static_cast<V*>(J.arena) + f.arena_off;
   if (ne > 0) {
-    double scale2 = 0.0;
+    T s2 = 0;
     if (lane < ne)
-      for (int j = 0; j < ne; ++j) scale2 = fmax(scale2, cabs2(F[lane + j * LD]));
-    for (int o = 16; o > 0; o >>= 1) scale2 = fmax(scale2, __shfl_xor_sync(0xffffffffu, scale2, o));
+      for (int j = 0; j < ne; ++j) s2 = fmax(s2, cnorm(F[lane + j * LD]));
+    for (int o = 16; o > 0; o >>= 1) s2 = fmax(s2, __shfl_xor_sync(0xffffffffu, s2, o));
+    const double scale2 = (double)s2;
     const double thresh = tol * tol * scale2;
     int mypiv = 0;  // lane k keeps piv[k]
     for (int k = 0; k < ne; ++k) {
-      double best = (lane >= k && lane < ne) ? cabs2(F[lane + k * LD]) : -1.0;
+      T bt = (lane >= k && lane < ne) ? cnorm(F[lane + k * LD]) : (T)-1;
       int bi = (lane >= k && lane < ne) ? lane : 0x7fffffff;
       for (int o = 16; o > 0; o >>= 1) {
-        const double b2 = __shfl_xor_sync(0xffffffffu, best, o);
+        const T b2 = __shfl_xor_sync(0xffffffffu, bt, o);
         const int i2 = __shfl_xor_sync(0xffffffffu, bi, o);
-        argmax_pair(best, bi, b2, i2);
+        if (b2 > bt || (b2 == bt && i2 < bi)) { bt = b2; bi = i2; }
       }
+      const double best = (double)bt;
       int p = bi;
       if (!(best > thresh) || p >= ne) {
         if (!perturb || !(best >= 0.0) || !(scale2 > 0.0) || p >= ne) {

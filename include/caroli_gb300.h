@@ -53,6 +53,7 @@ enum {
 
 int caroli_ctx_create(int device_ordinal, caroli_ctx** out);
 void caroli_ctx_destroy(caroli_ctx* ctx);
+/* Message of the last failed call on `ctx`; with NULL, why the last caroli_ctx_create failed. */
 const char* caroli_last_error(const caroli_ctx* ctx);
 
 /* Two-terminal system (NestedTwoTerminal::from_model). All arrays are copied.
