@@ -37,6 +37,8 @@ SIGNATURES = {
     "caroli_region_begin": (ctypes.c_int, [P]),
     "caroli_region_end": (ctypes.c_int, [P, P, P]),
     "caroli_solve_batch_noalloc": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P]),
+    "caroli_derivs_upload": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P]),
+    "caroli_transmission_with_grad": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P]),
     "caroli_kernel_classes": (ctypes.c_int, []),
     "caroli_last_job_info": (ctypes.c_int, [P, I64, P, P, P, P]),
     "caroli_kernel_class_name": (ctypes.c_char_p, [ctypes.c_int]),
@@ -203,6 +205,26 @@ class Plan:
         a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
         self.ctx.check(self.ctx.lib.caroli_last_phases(self.ctx.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
         return a.value, b.value, c.value
+
+    def upload_derivs(self, derivs):
+        """``derivs[c][k]``: dH/dp_k values of configuration c on the pattern."""
+        d = np.ascontiguousarray(np.asarray(derivs, dtype=np.complex128))
+        nparams = d.shape[1] if d.ndim == 3 else 0
+        self.ctx.check(self.ctx.lib.caroli_derivs_upload(self.ctx.h, self.id, nparams, ptr(d) if nparams else None))
+        self.nparams = nparams
+
+    def solve_grad(self, slots, configs, n):
+        slots = np.ascontiguousarray(slots, np.int32)
+        configs = np.ascontiguousarray(configs, np.int32)
+        cnt = len(slots)
+        t = np.zeros(cnt)
+        st = np.zeros(cnt, np.int32)
+        dv = np.zeros((cnt, n))
+        npar = getattr(self, "nparams", 0)
+        dp = np.zeros((cnt, max(npar, 1)))
+        self.ctx.check(self.ctx.lib.caroli_transmission_with_grad(self.ctx.h, self.id, cnt, ptr(slots), ptr(configs),
+                                                                  ptr(t), ptr(st), ptr(dv), ptr(dp) if npar else None))
+        return t, st, dv, dp[:, :npar]
 
     def last_job_info(self):
         cnt = ctypes.c_int64()

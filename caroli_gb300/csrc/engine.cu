@@ -125,11 +125,14 @@ struct System {
   std::vector<DevBlock> blocks;
   double2* vals = nullptr;
   int nconfigs = 0;
+  double2* dvals = nullptr;  // dH/dp of every configuration: [config][param][nnz]
+  int nparams = 0;
   std::vector<SigmaSlot> slots;
   ~System() {
     for (auto& p : plans) p->release();
     for (auto& b : blocks) b.release();
     cudaFree(vals);
+    cudaFree(dvals);
     for (auto& s : slots)
       for (auto* v : {&s.sl, &s.sr, &s.gl, &s.gr, &s.wr})
         for (auto* p : *v) cudaFree(p);
@@ -169,6 +172,19 @@ struct KStat {
 struct JobSpec {
   int block, slot, config;
   const DevPlan* plan;
+};
+
+// Device state of one refinement (forward, or the adjoint of the gradient).
+struct RefineBufs {
+  Buf rdesc, rx, rr, rd, rtb, rhb, rt, rerr, rdone;
+  Buf gV, gZ, gH, gg, gcs, gsn, gy, gbeta, gcol, gflags;
+};
+
+// A gradient request: d H / d p values of every configuration, and the per-job outputs.
+struct GradRequest {
+  const double2* dvals = nullptr;  // [config][param][nnz]
+  int nparams = 0;
+  int64_t nnz = 0;
 };
 
 // One tree level of a batch: its fronts split by size class, and their algorithmic work.
@@ -212,10 +228,10 @@ struct caroli_ctx {
   std::string err;
   std::vector<std::unique_ptr<System>> systems;
   Buf arena, root_arena, xs, jobs, tasks, fail, status, tout, part, pert;
-  Buf rdesc, rx, rr, rd, rtb, rhb, rt, rerr, rdone;
+  RefineBufs rb[2];  // forward and adjoint refinement state
   Buf inv, ipiv, iy, iscale, ibad;
   TaskCache tcache;
-  Buf gV, gZ, gH, gg, gcs, gsn, gy, gbeta, gcol, gflags;
+  Buf grhs, gptr, gdv, gdp;
   double inner_tol = 1e-10;
   int max_iters = 6;
   double refine_tol = 1e-10;
@@ -272,11 +288,12 @@ struct LevelRange {
 
 // FP64 iterative refinement of the jobs [begin, begin + cj) after their f32 factorization.
 template <typename LaunchT>
-void refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, size_t begin, size_t cj,
-            const std::vector<LevelRange>& lr, int max_root, const Task* dtasks, const std::vector<JobDesc>& jd,
-            const float2* arena, const std::vector<size_t>& arena_off, const float2* rarena,
-            const std::vector<size_t>& root_off, LaunchT& launch, std::vector<double>& th, std::vector<double>& eh,
-            std::vector<int32_t>& sh, std::vector<int32_t>& ih) {
+RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, size_t begin, size_t cj,
+                   const std::vector<LevelRange>& lr, int max_root, const Task* dtasks, const std::vector<JobDesc>& jd,
+                   const float2* arena, const std::vector<size_t>& arena_off, const float2* rarena,
+                   const std::vector<size_t>& root_off, LaunchT& launch, std::vector<double>& th,
+                   std::vector<double>& eh, std::vector<int32_t>& sh, std::vector<int32_t>& ih, RefineBufs& rb,
+                   int adjoint, const std::vector<const double2*>& rhs) {
   cudaStream_t s = ctx->stream;
   std::vector<RefineDesc> rdh(cj);
   size_t xo = 0, to = 0, ho = 0;
@@ -301,27 +318,27 @@ void refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, siz
     }
     resid_flops += 8.0 * c * ((double)B.nnz + (double)P.nl * P.nl + (double)P.nr * P.nr);
   }
-  double2* rx = static_cast<double2*>(ctx->rx.get(std::max<size_t>(xo, 1) * sizeof(double2)));
-  double2* rr = static_cast<double2*>(ctx->rr.get(std::max<size_t>(xo, 1) * sizeof(double2)));
-  float2* rdv = static_cast<float2*>(ctx->rd.get(std::max<size_t>(xo, 1) * sizeof(float2)));
-  float2* rtb = static_cast<float2*>(ctx->rtb.get(std::max<size_t>(to, 1) * sizeof(float2)));
-  float2* rhb = static_cast<float2*>(ctx->rhb.get(std::max<size_t>(ho, 1) * sizeof(float2)));
-  double* rt_out = static_cast<double*>(ctx->rt.get(cj * sizeof(double)));
-  double* rerr = static_cast<double*>(ctx->rerr.get(cj * sizeof(double)));
-  int32_t* rdone = static_cast<int32_t*>(ctx->rdone.get(cj * sizeof(int32_t)));
+  double2* rx = static_cast<double2*>(rb.rx.get(std::max<size_t>(xo, 1) * sizeof(double2)));
+  double2* rr = static_cast<double2*>(rb.rr.get(std::max<size_t>(xo, 1) * sizeof(double2)));
+  float2* rdv = static_cast<float2*>(rb.rd.get(std::max<size_t>(xo, 1) * sizeof(float2)));
+  float2* rtb = static_cast<float2*>(rb.rtb.get(std::max<size_t>(to, 1) * sizeof(float2)));
+  float2* rhb = static_cast<float2*>(rb.rhb.get(std::max<size_t>(ho, 1) * sizeof(float2)));
+  double* rt_out = static_cast<double*>(rb.rt.get(cj * sizeof(double)));
+  double* rerr = static_cast<double*>(rb.rerr.get(cj * sizeof(double)));
+  int32_t* rdone = static_cast<int32_t*>(rb.rdone.get(cj * sizeof(int32_t)));
   CK(cudaMemsetAsync(rt_out, 0, cj * sizeof(double), s));
   CK(cudaMemsetAsync(rerr, 0, cj * sizeof(double), s));
   const size_t M = GM_M;
-  double2* gV = static_cast<double2*>(ctx->gV.get(std::max<size_t>(xo, 1) * (M + 1) * sizeof(double2)));
-  float2* gZ = static_cast<float2*>(ctx->gZ.get(std::max<size_t>(xo, 1) * M * sizeof(float2)));
-  double2* gH = static_cast<double2*>(ctx->gH.get(std::max<size_t>(co, 1) * (M + 1) * M * sizeof(double2)));
-  double2* gg = static_cast<double2*>(ctx->gg.get(std::max<size_t>(co, 1) * (M + 1) * sizeof(double2)));
-  double* gcs = static_cast<double*>(ctx->gcs.get(std::max<size_t>(co, 1) * M * sizeof(double)));
-  double2* gsn = static_cast<double2*>(ctx->gsn.get(std::max<size_t>(co, 1) * M * sizeof(double2)));
-  double2* gy = static_cast<double2*>(ctx->gy.get(std::max<size_t>(co, 1) * M * sizeof(double2)));
-  double* gbeta = static_cast<double*>(ctx->gbeta.get(std::max<size_t>(co, 1) * sizeof(double)));
-  int32_t* gcol = static_cast<int32_t*>(ctx->gcol.get(std::max<size_t>(co, 1) * sizeof(int32_t)));
-  int32_t* gflags = static_cast<int32_t*>(ctx->gflags.get(cj * sizeof(int32_t)));
+  double2* gV = static_cast<double2*>(rb.gV.get(std::max<size_t>(xo, 1) * (M + 1) * sizeof(double2)));
+  float2* gZ = static_cast<float2*>(rb.gZ.get(std::max<size_t>(xo, 1) * M * sizeof(float2)));
+  double2* gH = static_cast<double2*>(rb.gH.get(std::max<size_t>(co, 1) * (M + 1) * M * sizeof(double2)));
+  double2* gg = static_cast<double2*>(rb.gg.get(std::max<size_t>(co, 1) * (M + 1) * sizeof(double2)));
+  double* gcs = static_cast<double*>(rb.gcs.get(std::max<size_t>(co, 1) * M * sizeof(double)));
+  double2* gsn = static_cast<double2*>(rb.gsn.get(std::max<size_t>(co, 1) * M * sizeof(double2)));
+  double2* gy = static_cast<double2*>(rb.gy.get(std::max<size_t>(co, 1) * M * sizeof(double2)));
+  double* gbeta = static_cast<double*>(rb.gbeta.get(std::max<size_t>(co, 1) * sizeof(double)));
+  int32_t* gcol = static_cast<int32_t*>(rb.gcol.get(std::max<size_t>(co, 1) * sizeof(int32_t)));
+  int32_t* gflags = static_cast<int32_t*>(rb.gflags.get(cj * sizeof(int32_t)));
   for (size_t j = 0; j < cj; ++j) {
     const JobSpec& sp = specs[begin + j];
     const DevPlan& P = *sp.plan;
@@ -352,8 +369,10 @@ void refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, siz
     R.beta = gbeta + coffs[j];
     R.col_done = gcol + coffs[j];
     R.done = R.c == 0 ? 1 : 0;  // no channel: T = 0
+    R.adjoint = adjoint;
+    R.rhs = adjoint ? rhs[j] : nullptr;
   }
-  RefineDesc* drd = static_cast<RefineDesc*>(ctx->rdesc.get(cj * sizeof(RefineDesc)));
+  RefineDesc* drd = static_cast<RefineDesc*>(rb.rdesc.get(cj * sizeof(RefineDesc)));
   CK(cudaMemcpyAsync(drd, rdh.data(), cj * sizeof(RefineDesc), cudaMemcpyHostToDevice, s));
   const unsigned cchunks = (unsigned)std::max(1, (cmax + RCB - 1) / RCB);
   in_pieces(cj, [&](size_t f0, size_t c) {
@@ -453,16 +472,22 @@ void refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, siz
     if (all) break;
   }
   CK(cudaEventRecord(ctx->ev1, s));
-  CK(cudaMemcpyAsync(th.data(), rt_out, cj * sizeof(double), cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(eh.data(), rerr, cj * sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (!adjoint) {
+    CK(cudaMemcpyAsync(th.data(), rt_out, cj * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(eh.data(), rerr, cj * sizeof(double), cudaMemcpyDeviceToHost, s));
+  }
   std::vector<RefineDesc> fin(cj);
   CK(cudaMemcpyAsync(fin.data(), drd, cj * sizeof(RefineDesc), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   for (size_t j = 0; j < cj; ++j) {
-    ih[j] = fin[j].iters;
-    if (rdh[j].c == 0) { th[j] = 0.0; eh[j] = 0.0; continue; }
+    ih[j] = std::max(ih[j], fin[j].iters);
+    if (rdh[j].c == 0) {
+      if (!adjoint) { th[j] = 0.0; eh[j] = 0.0; }
+      continue;
+    }
     if (!fin[j].done || fin[j].stalled) sh[j] = ST_REFINE_STALLED;
   }
+  return drd;
 }
 
 enum Mode { MODE_DOUBLE = 0, MODE_SINGLE = 1, MODE_MIXED = 2 };
@@ -472,6 +497,7 @@ struct JobOut {
   int32_t status = ST_OK;
   int32_t iters = 0;
   int32_t perturbed = 0;
+  std::vector<double> dv, dp;  // gradient: dT/dV of the block's orbitals (block order), dT/dp
   std::vector<uint8_t> fail;
 };
 
@@ -519,10 +545,91 @@ struct Launcher {
   }
 };
 
+// Adjoint solve and gradient of the jobs [begin, begin + cj) after their forward refinement:
+// A^† z_j = Γ_L x_j on the left slice, then dT/dV_a = 2 Re Σ_j x_j[a] conj(z_j[a]) and
+// dT/dp = 2 Re Σ_j z_j^† (dH/dp) x_j. The tree fronts are Hermitian (only the root carries Σ), so
+// the same f32 factors precondition the adjoint with the root inverse conjugate-transposed.
+template <typename LaunchT>
+void gradient(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, size_t begin, size_t cj,
+              const std::vector<LevelRange>& lr, int max_root, const Task* dtasks, const std::vector<JobDesc>& jd,
+              const float2* arena, const std::vector<size_t>& arena_off, const float2* rarena,
+              const std::vector<size_t>& root_off, LaunchT& launch, std::vector<double>& th, std::vector<double>& eh,
+              std::vector<int32_t>& sh, std::vector<int32_t>& ih, RefineDesc* fwd, const GradRequest& grad,
+              std::vector<JobOut>& out) {
+  cudaStream_t s = ctx->stream;
+  std::vector<size_t> roff(cj), doff(cj);
+  size_t ro = 0, dvo = 0;
+  int max_blk = 0;
+  for (size_t j = 0; j < cj; ++j) {
+    const JobSpec& sp = specs[begin + j];
+    const int nblk = sys->blocks[sp.block].nblk;
+    const int c = sys->slots[sp.slot].channels[sp.block];
+    roff[j] = ro;
+    ro += (size_t)nblk * c;
+    doff[j] = dvo;
+    dvo += (size_t)nblk;
+    max_blk = std::max(max_blk, nblk);
+  }
+  double2* rhs = static_cast<double2*>(ctx->grhs.get(std::max<size_t>(ro, 1) * sizeof(double2)));
+  double* dv = static_cast<double*>(ctx->gdv.get(std::max<size_t>(dvo, 1) * sizeof(double)));
+  double* dp = static_cast<double*>(ctx->gdp.get(std::max<size_t>(cj * std::max(grad.nparams, 1), 1) * sizeof(double)));
+  // Pointer tables: rhs per job, dv per job, dH per job.
+  std::vector<const void*> ptrs(3 * cj);
+  std::vector<const double2*> rhs_ptr(cj);
+  for (size_t j = 0; j < cj; ++j) {
+    const JobSpec& sp = specs[begin + j];
+    rhs_ptr[j] = rhs + roff[j];
+    ptrs[j] = rhs + roff[j];
+    ptrs[cj + j] = dv + doff[j];
+    ptrs[2 * cj + j] = grad.dvals ? grad.dvals + (size_t)sp.config * grad.nparams * grad.nnz : nullptr;
+  }
+  void** dptrs = static_cast<void**>(ctx->gptr.get(3 * cj * sizeof(void*)));
+  CK(cudaMemcpyAsync(dptrs, ptrs.data(), 3 * cj * sizeof(void*), cudaMemcpyHostToDevice, s));
+  const unsigned rows = (unsigned)((max_blk + 255) / 256);
+  in_pieces(cj, [&](size_t f0, size_t c) {
+    launch(K_REF_RES, 0.0, 0.0, [&] {
+      grad_rhs_kernel<<<dim3((unsigned)c, rows), 256, 0, s>>>(fwd + f0, reinterpret_cast<double2* const*>(dptrs) + f0);
+    });
+  });
+  std::vector<double> tz(cj), ez(cj);
+  RefineDesc* adj = refine(ctx, sys, specs, begin, cj, lr, max_root, dtasks, jd, arena, arena_off, rarena, root_off,
+                           launch, tz, ez, sh, ih, ctx->rb[1], 1, rhs_ptr);
+  in_pieces(cj, [&](size_t f0, size_t c) {
+    launch(K_REF_RES, 0.0, 0.0, [&] {
+      grad_v_kernel<<<dim3((unsigned)c, rows), 256, 0, s>>>(fwd + f0, adj + f0,
+                                                            reinterpret_cast<double* const*>(dptrs + cj) + f0);
+    });
+  });
+  if (grad.nparams > 0 && grad.dvals)
+    in_pieces(cj, [&](size_t f0, size_t c) {
+      launch(K_REF_RES, 0.0, 0.0, [&] {
+        grad_p_kernel<<<dim3((unsigned)c, (unsigned)grad.nparams), 256, 0, s>>>(
+            fwd + f0, adj + f0, reinterpret_cast<const double2* const*>(dptrs + 2 * cj) + f0, grad.nnz,
+            dp + f0 * grad.nparams, grad.nparams);
+      });
+    });
+  std::vector<double> dvh(dvo), dph(cj * std::max(grad.nparams, 1));
+  CK(cudaMemcpyAsync(dvh.data(), dv, dvo * sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (grad.nparams > 0 && grad.dvals)
+    CK(cudaMemcpyAsync(dph.data(), dp, cj * grad.nparams * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  for (size_t j = 0; j < cj; ++j) {
+    JobOut& o = out[begin + j];
+    const int nblk = sys->blocks[specs[begin + j].block].nblk;
+    o.dv.assign(dvh.begin() + doff[j], dvh.begin() + doff[j] + nblk);
+    o.dp.assign(grad.nparams, 0.0);
+    if (grad.dvals)
+      for (int k = 0; k < grad.nparams; ++k) o.dp[k] = dph[j * grad.nparams + k];
+  }
+  (void)th;
+  (void)eh;
+}
+
 // Runs `specs` in `mode`: complex f64 fronts (DOUBLE), complex f32 fronts under an f64 root
 // (SINGLE), or complex f32 factors refined in FP64 (MIXED). T: front precision, TR: root precision.
 template <typename T, typename TR>
-void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, Mode mode, std::vector<JobOut>& out) {
+void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, Mode mode, std::vector<JobOut>& out,
+              const GradRequest* grad = nullptr) {
   using V = typename Cx<T>::V;
   using VR = typename Cx<TR>::V;
   cudaStream_t s = ctx->stream;
@@ -840,8 +947,10 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
       if constexpr (std::is_same<T, float>::value && std::is_same<TR, float>::value) {
         std::vector<LevelRange> lr;
         for (const Level& lv : levels) lr.push_back({lv.tiny0, lv.tiny_n, lv.small0, lv.small_n + lv.large_n, lv.max_n});
-        refine(ctx, sys, specs, begin, cj, lr, max_root, dtasks, jd, arena, arena_off, rarena, root_off, launch, th,
-               eh, sh, ih);
+        RefineDesc* fwd = refine(ctx, sys, specs, begin, cj, lr, max_root, dtasks, jd, arena, arena_off, rarena,
+                                 root_off, launch, th, eh, sh, ih, ctx->rb[0], 0, {});
+        if (grad) gradient(ctx, sys, specs, begin, cj, lr, max_root, dtasks, jd, arena, arena_off, rarena, root_off,
+                           launch, th, eh, sh, ih, fwd, *grad, out);
       }
     }
     std::vector<int32_t> sdev(cj);
@@ -1212,6 +1321,78 @@ int caroli_values_upload(caroli_ctx* ctx, int plan_id, int nconfigs, const doubl
     return CAROLI_OK;
   } catch (const CudaError& e) {
     return fail_with(ctx, e.e == cudaErrorMemoryAllocation ? CAROLI_ENOMEM : CAROLI_ECUDA, cudaGetErrorString(e.e));
+  }
+}
+
+int caroli_derivs_upload(caroli_ctx* ctx, int plan_id, int nparams, const double* values) {
+  System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
+  if (!sys || nparams < 0 || (nparams > 0 && !values) || sys->nconfigs <= 0)
+    return fail_with(ctx, CAROLI_EINVAL, "caroli_derivs_upload: bad arguments (upload the values first)");
+  try {
+    CK(cudaSetDevice(ctx->device));
+    cudaFree(sys->dvals);
+    sys->dvals = nullptr;
+    const size_t nnz = (size_t)sys->desc.row_ptr[sys->desc.n];
+    if (nparams > 0) sys->dvals = upload_c64(values, nnz * (size_t)nparams * sys->nconfigs, ctx->stream);
+    CK(cudaStreamSynchronize(ctx->stream));
+    sys->nparams = nparams;
+    return CAROLI_OK;
+  } catch (const CudaError& e) {
+    return fail_with(ctx, e.e == cudaErrorMemoryAllocation ? CAROLI_ENOMEM : CAROLI_ECUDA, cudaGetErrorString(e.e));
+  }
+}
+
+int caroli_transmission_with_grad(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots,
+                                  const int32_t* configs, double* t, int32_t* status, double* dt_dv, double* dt_dp) {
+  System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
+  if (!sys || count < 0 || (count > 0 && (!slots || !configs || !t || !status || !dt_dv)))
+    return fail_with(ctx, CAROLI_EINVAL, "caroli_transmission_with_grad: bad arguments");
+  if (!sys->vals) return fail_with(ctx, CAROLI_EINVAL, "no H values uploaded");
+  for (int i = 0; i < count; ++i) {
+    if (slots[i] < 0 || slots[i] >= (int)sys->slots.size() || !sys->slots[slots[i]].set)
+      return fail_with(ctx, CAROLI_EINVAL, "energy slot without self-energies");
+    if (configs[i] < 0 || configs[i] >= sys->nconfigs) return fail_with(ctx, CAROLI_EINVAL, "configuration out of range");
+  }
+  try {
+    CK(cudaSetDevice(ctx->device));
+    ctx->last_ms = 0.0;
+    ctx->last_launches = 0;
+    ctx->factor_ms = ctx->root_ms = ctx->tail_ms = 0.0;
+    ctx->refine_iters = 0;
+    ctx->fallbacks = 0;
+    const int nb = (int)sys->plans.size();
+    std::vector<JobSpec> specs;
+    for (int i = 0; i < count; ++i)
+      for (int b = 0; b < nb; ++b) specs.push_back({b, slots[i], configs[i], sys->plans[b].get()});
+    GradRequest g;
+    g.dvals = sys->dvals;
+    g.nparams = sys->dvals ? sys->nparams : 0;
+    g.nnz = sys->desc.row_ptr[sys->desc.n];
+    std::vector<JobOut> jo;
+    run_jobs<float, float>(ctx, sys, specs, MODE_MIXED, jo, &g);
+    const int64_t n = sys->desc.n;
+    for (int i = 0; i < count; ++i) {
+      double sum = 0.0;
+      int32_t st = ST_OK;
+      double* dv = dt_dv + (size_t)i * n;
+      std::fill(dv, dv + n, 0.0);
+      if (dt_dp) std::fill(dt_dp + (size_t)i * g.nparams, dt_dp + (size_t)(i + 1) * g.nparams, 0.0);
+      for (int b = 0; b < nb; ++b) {
+        const JobOut& o = jo[(size_t)i * nb + b];
+        sum += o.t;
+        if (st == ST_OK) st = o.status;
+        const auto& orbs = sys->trees[b].orbitals;
+        for (size_t a = 0; a < o.dv.size() && a < orbs.size(); ++a) dv[orbs[a]] = o.dv[a];
+        if (dt_dp)
+          for (int k = 0; k < g.nparams && k < (int)o.dp.size(); ++k) dt_dp[(size_t)i * g.nparams + k] += o.dp[k];
+      }
+      t[i] = sum;
+      status[i] = st;
+    }
+    return CAROLI_OK;
+  } catch (const CudaError& e) {
+    return fail_with(ctx, e.e == cudaErrorMemoryAllocation ? CAROLI_ENOMEM : CAROLI_ECUDA,
+                     std::string(e.what) + ": " + cudaGetErrorString(e.e));
   }
 }
 

@@ -60,11 +60,22 @@ struct RefineDesc {
   int32_t* col_done;  // per column: the inner solve converged (or the column is empty)
   int32_t inner, inner_done;  // Arnoldi steps of the current outer step; all columns converged
   double inner_res;            // largest relative residual the last inner solve reached
+  // The adjoint solve A^† z = b (gradient): Σ -> Σ^†, the root inverse conjugate-transposed, an
+  // explicit right-hand side `rhs` (nblk x c), and convergence on the whole vector.
+  const double2* rhs;
+  int32_t adjoint, pad2;
 };
 
 constexpr int GM_M = 12;  // Arnoldi steps per outer step
 
 __device__ __forceinline__ float2 f2(double2 v) { return make_float2((float)v.x, (float)v.y); }
+
+// Σ[i, a] of an m x m column-major block, or (Σ^†)[i, a] = conj(Σ[a, i]) for the adjoint.
+__device__ __forceinline__ double2 sigma_at(const double2* sg, int i, int a, int m, int adjoint) {
+  if (!adjoint) return sg[i + (int64_t)a * m];
+  const double2 v = sg[a + (int64_t)i * m];
+  return make_double2(v.x, -v.y);
+}
 
 // Forward sweep of the fronts of one level: grid (tasks, column chunks).
 // The sweeps solve M d = v for v = the residual (src < 0) or the Arnoldi vector V_src, and write
@@ -170,7 +181,13 @@ __global__ void __launch_bounds__(256) refine_root_kernel(RefineDesc* __restrict
 #pragma unroll
     for (int j = 0; j < RCB; ++j) acc[j] = make_float2(0.f, 0.f);
     for (int k = 0; k < m; ++k) {
-      const float2 a = R.root[i + (int64_t)k * m];
+      float2 a;
+      if (R.adjoint) {
+        a = R.root[k + (int64_t)i * m];
+        a.y = -a.y;
+      } else {
+        a = R.root[i + (int64_t)k * m];
+      }
 #pragma unroll
       for (int j = 0; j < RCB; ++j) acc[j] = cfma(acc[j], a, z[k * RCB + j]);
     }
@@ -243,14 +260,15 @@ __global__ void __launch_bounds__(256) refine_residual_kernel(RefineDesc* __rest
   const int li = R.slice_l[i], ri = R.slice_r[i];
   for (int j = 0; j < R.c; ++j) {
     const double2* xj = R.x + (int64_t)j * R.nblk;
-    double2 acc = ri >= 0 ? R.w_r[ri + (int64_t)j * R.nr] : make_double2(0.0, 0.0);
+    double2 acc = R.rhs ? R.rhs[i + (int64_t)j * R.nblk]
+                        : (ri >= 0 ? R.w_r[ri + (int64_t)j * R.nr] : make_double2(0.0, 0.0));
     acc.x -= R.energy * xj[i].x;
     acc.y -= R.energy * xj[i].y;
     for (int q = R.csr_ptr[i]; q < R.csr_ptr[i + 1]; ++q) acc = cfma(acc, R.vals[R.csr_q[q]], xj[R.csr_col[q]]);
     if (li >= 0)
-      for (int a = 0; a < R.nl; ++a) acc = cfma(acc, R.sigma_l[li + (int64_t)a * R.nl], xj[R.left_local[a]]);
+      for (int a = 0; a < R.nl; ++a) acc = cfma(acc, sigma_at(R.sigma_l, li, a, R.nl, R.adjoint), xj[R.left_local[a]]);
     if (ri >= 0)
-      for (int a = 0; a < R.nr; ++a) acc = cfma(acc, R.sigma_r[ri + (int64_t)a * R.nr], xj[R.right_local[a]]);
+      for (int a = 0; a < R.nr; ++a) acc = cfma(acc, sigma_at(R.sigma_r, ri, a, R.nr, R.adjoint), xj[R.right_local[a]]);
     R.r[i + (int64_t)j * R.nblk] = acc;
   }
 }
@@ -270,7 +288,14 @@ __global__ void __launch_bounds__(256) refine_check_kernel(RefineDesc* __restric
     return;
   }
   double tl = 0.0, dn = 0.0, xn = 0.0;
-  for (int idx = threadIdx.x; idx < R.nl * R.c; idx += blockDim.x) {
+  if (R.adjoint)  // every orbital's value matters (dT/dV_a): the correction of the whole vector
+    for (int64_t q = threadIdx.x; q < (int64_t)R.nblk * R.c; q += blockDim.x) {
+      const float2 dv = R.d[q];
+      const double2 xv = R.x[q];
+      dn += (double)dv.x * dv.x + (double)dv.y * dv.y;
+      xn += xv.x * xv.x + xv.y * xv.y;
+    }
+  for (int idx = threadIdx.x; idx < (R.adjoint ? 0 : R.nl * R.c); idx += blockDim.x) {
     const int a = idx % R.nl, j = idx / R.nl;
     const double2* xj = R.x + (int64_t)j * R.nblk;
     const int row = R.left_local[a];
@@ -325,7 +350,7 @@ __global__ void refine_init_kernel(RefineDesc* __restrict__ rd, int njobs) {
     const int i = (int)(q % R.nblk), j = (int)(q / R.nblk);
     const int ri = R.slice_r[i];
     R.x[q] = make_double2(0.0, 0.0);
-    R.r[q] = ri >= 0 ? R.w_r[ri + (int64_t)j * R.nr] : make_double2(0.0, 0.0);
+    R.r[q] = R.rhs ? R.rhs[q] : (ri >= 0 ? R.w_r[ri + (int64_t)j * R.nr] : make_double2(0.0, 0.0));
   }
 }
 
@@ -400,9 +425,9 @@ __global__ void __launch_bounds__(256) gm_matvec_kernel(RefineDesc* __restrict__
     acc.y *= R.energy;
     for (int q = R.csr_ptr[i]; q < R.csr_ptr[i + 1]; ++q) acc = cfms(acc, R.vals[R.csr_q[q]], zd(R.csr_col[q]));
     if (li >= 0)
-      for (int a = 0; a < R.nl; ++a) acc = cfms(acc, R.sigma_l[li + (int64_t)a * R.nl], zd(R.left_local[a]));
+      for (int a = 0; a < R.nl; ++a) acc = cfms(acc, sigma_at(R.sigma_l, li, a, R.nl, R.adjoint), zd(R.left_local[a]));
     if (ri >= 0)
-      for (int a = 0; a < R.nr; ++a) acc = cfms(acc, R.sigma_r[ri + (int64_t)a * R.nr], zd(R.right_local[a]));
+      for (int a = 0; a < R.nr; ++a) acc = cfms(acc, sigma_at(R.sigma_r, ri, a, R.nr, R.adjoint), zd(R.right_local[a]));
     W[i + (int64_t)j * R.nblk] = acc;
   }
 }
@@ -705,6 +730,65 @@ __global__ void __launch_bounds__(256) refine_backward_rows_kernel(RefineDesc* _
       dout[row + (int64_t)(j0 + j) * R.nblk] = make_float2(tv.x - acc[j].x, tv.y - acc[j].y);
     }
   }
+}
+
+}  // namespace caroli
+
+namespace caroli {
+
+// Right-hand side of the adjoint solve: Γ_L x_j on the left slice (x from the forward solve).
+// grid (jobs, row chunks).
+__global__ void __launch_bounds__(256) grad_rhs_kernel(const RefineDesc* __restrict__ fwd, double2* const* rhs) {
+  const RefineDesc& R = fwd[blockIdx.x];
+  const int i = blockIdx.y * 256 + threadIdx.x;
+  if (i >= R.nblk) return;
+  const int li = R.slice_l[i];
+  for (int j = 0; j < R.c; ++j) {
+    double2 acc = make_double2(0.0, 0.0);
+    if (li >= 0) {
+      const double2* xj = R.x + (int64_t)j * R.nblk;
+      for (int b = 0; b < R.nl; ++b) acc = cfma(acc, R.gamma_l[li + (int64_t)b * R.nl], xj[R.left_local[b]]);
+    }
+    rhs[blockIdx.x][i + (int64_t)j * R.nblk] = acc;
+  }
+}
+
+// dT/dV_a = 2 Re Σ_j x_j[a] conj(z_j[a]) for every orbital a of the block.
+__global__ void __launch_bounds__(256) grad_v_kernel(const RefineDesc* __restrict__ fwd, const RefineDesc* __restrict__ adj,
+                                                     double* const* out) {
+  const RefineDesc& X = fwd[blockIdx.x];
+  const RefineDesc& Z = adj[blockIdx.x];
+  const int i = blockIdx.y * 256 + threadIdx.x;
+  if (i >= X.nblk) return;
+  double s = 0.0;
+  for (int j = 0; j < X.c; ++j) {
+    const double2 x = X.x[i + (int64_t)j * X.nblk], z = Z.x[i + (int64_t)j * X.nblk];
+    s += x.x * z.x + x.y * z.y;
+  }
+  out[blockIdx.x][i] = 2.0 * s;  // block-local order
+}
+
+// dT/dp = 2 Re Σ_j z_j^† (dH/dp) x_j for each parameter (dH given as values on the CSR pattern).
+// grid (jobs, parameters); partial sums per CTA in `part`.
+__global__ void __launch_bounds__(256) grad_p_kernel(const RefineDesc* __restrict__ fwd, const RefineDesc* __restrict__ adj,
+                                                     const double2* const* dh, int64_t nnz, double* __restrict__ out,
+                                                     int nparams) {
+  __shared__ double red[32];
+  const RefineDesc& X = fwd[blockIdx.x];
+  const RefineDesc& Z = adj[blockIdx.x];
+  const int k = blockIdx.y;
+  const double2* d = dh[blockIdx.x] + (int64_t)k * nnz;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < X.nblk; i += blockDim.x)
+    for (int j = 0; j < X.c; ++j) {
+      double2 hx = make_double2(0.0, 0.0);
+      const double2* xj = X.x + (int64_t)j * X.nblk;
+      for (int q = X.csr_ptr[i]; q < X.csr_ptr[i + 1]; ++q) hx = cfma(hx, d[X.csr_q[q]], xj[X.csr_col[q]]);
+      const double2 z = Z.x[i + (int64_t)j * X.nblk];
+      s += z.x * hx.x + z.y * hx.y;  // Re(conj(z) hx)
+    }
+  s = block_sum(s, red);
+  if (threadIdx.x == 0) out[(int64_t)blockIdx.x * nparams + k] = 2.0 * s;
 }
 
 }  // namespace caroli

@@ -153,6 +153,25 @@ class NestedTwoTerminal:
             sigmas.append(self.self_energies(e))
         return self.transmissions_with(sigmas, [config] * len(sigmas), precision)
 
+    def set_parameter_derivatives(self, derivs):
+        """dH/dp for gradient parameters: ``derivs[c][k]`` = values of dH/dp_k of configuration c
+        on the system's CSR pattern (e.g. the exchange term divided by J for dT/dJ)."""
+        self.plan().upload_derivs(derivs)
+
+    def transmissions_with_grad(self, sigmas, configs=None):
+        """``(T, status, dT/dV, dT/dp)``: dT/dV for every orbital's on-site potential (n per point)
+        and dT/dp for the parameters of ``set_parameter_derivatives``; mixed precision refined in
+        FP64 (no reference counterpart: the adjoint of ``transmission_with``)."""
+        if configs is None:
+            configs = [0] * len(sigmas)
+        slots = [self._slot(s) for s in sigmas]
+        return self.plan().solve_grad(slots, configs, self.system.n)
+
+    def transmission_with_grad(self, sigma, config=0):
+        t, st, dv, dp = self.transmissions_with_grad([sigma], [config])
+        _result(t[0], st[0], sigma.energy)
+        return float(t[0]), dv[0], dp[0]
+
     def transmissions_checked(self, energies, options: PrecisionOptions, config=0):
         sigmas = {float(e): self.self_energies(e) for e in energies}
 

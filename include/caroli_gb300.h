@@ -15,7 +15,7 @@
  *   caroli_solve_batch                       transmission_with / transmission_with_precision /
  *                                            transmissions                        nested.rs:618-713
  *   caroli_transmission_with_grad            no counterpart: the reference has no derivative code;
- *                                            the adjoint of transmission_with (dT/dV, dT/dJ)
+ *   caroli_derivs_upload                     the adjoint of transmission_with (dT/dV, dT/dJ)
  *   caroli_last_error                        GreenError / GpuError text           caroli-green/src/lib.rs:34-47
  */
 #ifndef CAROLI_GB300_H
@@ -134,6 +134,21 @@ const char* caroli_kernel_class_name(int kclass);
 int caroli_probe_kernel(caroli_ctx* ctx, int kclass);
 int caroli_kernel_stats(caroli_ctx* ctx, int kclass, int64_t* launches, double* flops, double* bytes, double* ms,
                         int reset);
+
+/* Derivatives of H with respect to `nparams` parameters (e.g. the exchange coupling J), per
+ * configuration: values[(c * nparams + k) * nnz + q] as interleaved complex128 on the plan's
+ * pattern. Used by caroli_transmission_with_grad for dT/dp. */
+int caroli_derivs_upload(caroli_ctx* ctx, int plan_id, int nparams, const double* values);
+
+/* T and its gradient (no counterpart in the reference, which has no derivative code): the adjoint
+ * of transmission_with (nested.rs:682). For every instance, dt_dv[i * n + a] = dT/dV_a for the
+ * on-site potential V_a of each orbital a (H -> H + V_a e_a e_a^T; 0 outside the blocks), and
+ * dt_dp[i * nparams + k] = dT/dp_k for the uploaded derivatives (dt_dp may be NULL). Runs the
+ * mixed path: one factorization, the forward solve X = G e_R W_R and one adjoint solve
+ * Z = G^† Γ_L X with the same factors, both refined in FP64; dT/dV_a = 2 Re Σ_j X_aj conj(Z_aj),
+ * dT/dp = 2 Re Σ_j Z_j^† (dH/dp) X_j. */
+int caroli_transmission_with_grad(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots, const int32_t* configs,
+                                  double* t, int32_t* status, double* dt_dv, double* dt_dp);
 
 /* Device time of the last caroli_solve_batch (ms), and kernels it launched. */
 int caroli_last_timing(const caroli_ctx* ctx, double* device_ms, int64_t* launches);

@@ -81,3 +81,33 @@ def oracle_T(sys_, sigma, config=0, precision=0):
     if not hasattr(sys_, "_oracle"):
         sys_._oracle = Oracle(sys_.system)
     return sys_._oracle.transmission(sigma.energy, sys_.system.values[config], sigma.blocks, precision)
+
+
+def gradient_bhz(length, width, configs=1, anderson=0.02, concentration=0.1, exchange=0.3, moments=None,
+                 spin="opposite-g"):
+    """The gradient workload's physics on a ribbon: Anderson disorder W (entry 0) and magnetic
+    impurities (entry 1, isotropic moments by default, as the CLI), with dH/dJ per configuration:
+    the exchange term at J = 1 (H is linear in J)."""
+    from caroli_gb300.system import merge_patterns
+
+    m = bhz()
+    region = Region.cuboid(m.lattice, [length, width, 0])
+    mom = moments or Moments.isotropic()
+
+    def entries(j):
+        return [{"kind": "anderson", "strength": anderson},
+                {"kind": "magnetic", "concentration": concentration, "exchange": j, "moments": mom,
+                 "spin": bhz_spin(spin)}]
+
+    devices = [disordered(m, region, entries(exchange), c) for c in range(configs)]
+    sys_ = NestedTwoTerminal.from_models(devices, m, region, 0)
+    derivs = []
+    for c in range(configs):
+        h1 = disordered(m, region, entries(1.0), c).sparse_hamiltonian(region)
+        h0 = disordered(m, region, entries(0.0), c).sparse_hamiltonian(region)
+        # Both on the system's merged pattern.
+        from caroli_gb300.model import SparseMatrix
+        base = SparseMatrix(sys_.system.n, sys_.system.row_ptr, sys_.system.cols, np.zeros(sys_.system.nnz, complex))
+        _, _, (v1, v0, _) = merge_patterns([h1, h0, base])
+        derivs.append([v1 - v0])
+    return sys_, derivs
