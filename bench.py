@@ -121,6 +121,60 @@ def peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
 
 
+def gradient_workload(length=100, width=40, energies=16):
+    """BHZ 100 x 40 with Anderson disorder W = 0.02 and magnetic impurities (concentration 0.1,
+    J = 0.3, isotropic moments, so the two spin blocks couple: one block of 16 000 orbitals), with
+    dH/dJ = H(J = 1) - H(J = 0) on the system's pattern (H is linear in J); 16 energies."""
+    from caroli_gb300 import NestedTwoTerminal, Region, bhz
+    from caroli_gb300.disorder import Moments, disordered
+    from caroli_gb300.model import SparseMatrix, bhz_spin
+    from caroli_gb300.system import merge_patterns
+
+    m = bhz()
+    region = Region.cuboid(m.lattice, [length, width, 0])
+
+    def entries(j):
+        return [{"kind": "anderson", "strength": 0.02},
+                {"kind": "magnetic", "concentration": 0.1, "exchange": j, "moments": Moments.isotropic(),
+                 "spin": bhz_spin("opposite-g")}]
+
+    sys_ = NestedTwoTerminal.from_models([disordered(m, region, entries(0.3), 0)], m, region, 0)
+    h1 = disordered(m, region, entries(1.0), 0).sparse_hamiltonian(region)
+    h0 = disordered(m, region, entries(0.0), 0).sparse_hamiltonian(region)
+    s = sys_.system
+    base = SparseMatrix(s.n, s.row_ptr, s.cols, np.zeros(s.nnz, complex))
+    _, _, (v1, v0, _) = merge_patterns([h1, h0, base])
+    sys_.set_parameter_derivatives([[v1 - v0]])
+    sigmas = [sys_.self_energies(e) for e in np.linspace(-0.16, 0.16, energies)]
+    return sys_, sigmas
+
+
+def time_gradient(steps):
+    """Device time of T with dT/dV (every orbital) and dT/dJ over the time of T alone, both on the
+    mixed path, on the same 16 points."""
+    from caroli_gb300 import Precision
+    from caroli_gb300.nested import context
+
+    sys_, sigmas = gradient_workload()
+    ctx = context(0)
+    cfg = [0] * len(sigmas)
+    for _ in range(2):
+        sys_.solve_batch(sigmas, cfg, Precision.MIXED)
+        sys_.transmissions_with_grad(sigmas, cfg)
+    ctx.region_begin()
+    for _ in range(steps):
+        t_f, st_f, _ = sys_.solve_batch(sigmas, cfg, Precision.MIXED)
+    fwd_ms, _ = ctx.region_end()
+    ctx.region_begin()
+    for _ in range(steps):
+        t_g, st_g, dv, dp = sys_.transmissions_with_grad(sigmas, cfg)
+    grad_ms, _ = ctx.region_end()
+    return {"value": grad_ms / fwd_ms, "fwd_ms_per_step": fwd_ms / steps, "grad_ms_per_step": grad_ms / steps,
+            "workload": "BHZ 100x40, Anderson W=0.02 + magnetic c=0.1 J=0.3 isotropic, 16 E; dT/dV (16000) + dT/dJ",
+            "max_abs_dT_fwd_vs_grad": float(np.max(np.abs(t_f - t_g))),
+            "status_ok": bool((st_g == 0).all() and (st_f == 0).all())}
+
+
 def cpu_baseline(sys_, pairs, sample, threads):
     """The oracle (C++ restatement of the reference's CPU path) on `sample` instances."""
     from oracle import Oracle
@@ -250,6 +304,9 @@ def run_ours(args):
     roof["launches_per_step"] = d["launches"]
     roof["share_of_step"] = d["ms"] / (ms_max / args.steps)
     kernels = {k: {"ms": round(v["ms"], 3), "launches": v["launches"]} for k, v in probe.items() if v["launches"]}
+    grad = None
+    if rank == 0 and args.gradient:
+        grad = time_gradient(args.steps)
     cpu = None
     if rank == 0 and world == 1 and args.cpu_sample > 0:
         threads = os.cpu_count() or 1
@@ -285,7 +342,8 @@ def run_ours(args):
         "refinement": {"max_iterations": max_iters, "fp64_recomputed_solves": fallbacks,
                        "median_iterations": float(np.median(iters)) if len(iters) else None,
                        "perturbed_pivots_total": int(perturbed.sum()) if len(perturbed) else 0},
-        "grad_fwd_ratio": None,
+        "grad_fwd_ratio": grad["value"] if grad else None,
+        "gradient": grad,
         "e2e": {"value": nsolve * args.steps / (e2e_ms * 1e-3), "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "wall_s": e2e_wall},
         "gpu_launches": int(launches),
@@ -341,9 +399,10 @@ def main():
     ap.add_argument("--width", type=int, default=64)
     ap.add_argument("--configs", type=int, default=8)
     ap.add_argument("--energies", type=int, default=33)
-    ap.add_argument("--cpu-sample", type=int, default=32)
-    ap.add_argument("--ref-sample", type=int, default=32)
+    ap.add_argument("--cpu-sample", type=int, default=264)
+    ap.add_argument("--ref-sample", type=int, default=264)
     ap.add_argument("--profile-run", action="store_true", help="warm-up steps and one step, no timing (profilers)")
+    ap.add_argument("--no-gradient", dest="gradient", action="store_false", help="skip the grad/fwd measurement")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

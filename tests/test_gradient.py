@@ -64,3 +64,41 @@ def test_gradient_sums_to_the_uniform_shift():
         vm[q] -= h
     fd = (_oracle_T_with(sys_, sigma, vp) - _oracle_T_with(sys_, sigma, vm)) / (2 * h)
     assert abs(dv[0].sum() - fd) <= 1e-4 * abs(fd) + 1e-5
+
+
+@pytest.mark.slow
+def test_gradient_workload_64_sites():
+    """The gradient workload (BHZ 100 x 40, Anderson W = 0.02 + magnetic c = 0.1, J = 0.3): dT/dV on
+    64 random orbitals and dT/dJ against central differences (step 1e-6) of the FP64 oracle."""
+    from oracle import Oracle
+
+    sys_, derivs = gradient_bhz(100, 40, configs=1)
+    sys_.set_parameter_derivatives(derivs)
+    sigma = sys_.self_energies(0.03)
+    t, st, dv, dp = sys_.transmissions_with_grad([sigma], [0])
+    assert st[0] == 0
+    orc = Oracle(sys_.system)
+    base = sys_.system.values[0]
+    h = 1e-6
+    sites = np.random.default_rng(11).choice(sys_.system.n, size=64, replace=False)
+    vals = []
+    for a in sites:
+        q = _diag_index(sys_.system, a)
+        for sgn in (1, -1):
+            v = base.copy()
+            v[q] += sgn * h
+            vals.append(v)
+    d = derivs[0][0]
+    vals += [base + h * d, base - h * d]
+    nb = sys_.block_count()
+    blocks = [b for _ in vals for b in range(nb)]
+    ts, sts = orc.solve_batch(blocks, [sigma.energy] * len(blocks), [v for v in vals for _ in range(nb)],
+                              [sigma.blocks[b][0] for _ in vals for b in range(nb)],
+                              [sigma.blocks[b][1] for _ in vals for b in range(nb)], threads=0)
+    assert (sts == 0).all()
+    tt = ts.reshape(len(vals), nb).sum(axis=1)
+    for i, a in enumerate(sites):
+        fd = (tt[2 * i] - tt[2 * i + 1]) / (2 * h)
+        assert abs(dv[0, a] - fd) <= 1e-4 * abs(fd) + 1e-5, (a, dv[0, a], fd)
+    fdj = (tt[-2] - tt[-1]) / (2 * h)
+    assert abs(dp[0, 0] - fdj) <= 1e-4 * abs(fdj) + 1e-5
