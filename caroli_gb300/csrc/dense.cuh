@@ -43,10 +43,8 @@ __global__ void __launch_bounds__(256) inv_scale_kernel(const InvTask* __restric
   const InvTask t = tasks[blockIdx.x];
   const V* A = static_cast<const V*>(t.a);
   T mt = 0;
-  for (int64_t idx = threadIdx.x; idx < (int64_t)t.npiv * t.npiv; idx += blockDim.x) {
-    const int i = (int)(idx % t.npiv), j = (int)(idx / t.npiv);
-    mt = fmax(mt, cnorm(A[i + (int64_t)j * t.ld]));
-  }
+  for (int j = threadIdx.x >> 5; j < t.npiv; j += blockDim.x >> 5)
+    for (int i = threadIdx.x & 31; i < t.npiv; i += 32) mt = fmax(mt, cnorm(A[i + (int64_t)j * t.ld]));
   const double m = block_max((double)mt, red);
   if (threadIdx.x == 0) {
     *t.scale2 = m;
@@ -54,106 +52,133 @@ __global__ void __launch_bounds__(256) inv_scale_kernel(const InvTask* __restric
   }
 }
 
-// Sweeps panel [k0, k0 + kb) of every matrix. Shared memory: the panel (n x kb) when it fits
-// (`staged`), else it is swept in place in global memory.
+// Shared memory of a panel launch: the candidate rows of the panel (m x kb) when they fit, the
+// pivot rows of the steps (kb x kb), the column buffer (2m), pos (m) and the displaced rows (kb),
+// 32 doubles.
+__host__ __device__ inline int64_t panel_work_bytes(int m, int vbytes) {
+  return ((int64_t)GJ_KB * GJ_KB + 2 * (int64_t)m) * vbytes + 32 * 8 + ((int64_t)m + GJ_KB) * 4 + 16;
+}
+__host__ __device__ inline int64_t panel_staged_bytes(int m, int vbytes) {
+  return (int64_t)m * GJ_KB * vbytes + panel_work_bytes(m, vbytes);
+}
+
+// Sweeps panel [k0, k0 + kb) of every matrix, one CTA per matrix:
+//  1. Gauss-Jordan sweep of the m = npiv - k0 candidate rows of the panel columns (in shared
+//     memory when they fit), pivots from those rows: the pivot block P becomes P^-1 and the other
+//     candidate rows -a P^-1;
+//  2. the rows outside the candidates (the pivoted rows above k0, the rows below npiv) receive
+//     their panel entries -a P^-1 by replaying the sweep's elimination steps from the recorded
+//     pivot rows, a thread per row (the same operations, in the same order, as if they had been
+//     swept with the candidates: an explicit P^-1 would lose accuracy on ill-conditioned blocks);
+//  3. the row interchanges reach the other columns: the pivot rows of the rest columns are
+//     copied to Y (the update's right factor) and the rows the interchanges displaced below the
+//     pivot rows are moved; the pivot rows themselves are rewritten by the update.
 template <typename T>
 __global__ void __launch_bounds__(256) inv_panel_kernel(const InvTask* __restrict__ tasks, int k0, double tol,
                                                         int perturb, int smem_bytes) {
   using V = typename Cx<T>::V;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ double redv[32];
-  __shared__ int redi[32];
   const InvTask t = tasks[blockIdx.x];
   const int n = t.n, np = t.npiv;
   if (k0 >= np) return;
   if (*t.bad) return;
   const int kb = min(GJ_KB, np - k0);
+  const int m = np - k0;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
   V* A = static_cast<V*>(t.a);
   const int64_t ld = t.ld;
-  const bool staged = (int64_t)n * kb * (int64_t)sizeof(V) + 2 * (int64_t)n * sizeof(V) <= smem_bytes;
-  V* P;  // panel, column-major with leading dimension pld
-  int64_t pld;
+  const bool staged = panel_staged_bytes(m, (int)sizeof(V)) <= smem_bytes;
+  V* C;  // candidate rows of the panel, leading dimension ldc
+  int64_t ldc;
   V* work = reinterpret_cast<V*>(smem_raw);
   if (staged) {
-    P = work;
-    pld = n;
-    work += (int64_t)n * kb;
-    for (int64_t idx = threadIdx.x; idx < (int64_t)n * kb; idx += blockDim.x) {
-      const int i = (int)(idx % n), c = (int)(idx / n);
-      P[idx] = A[i + (int64_t)(k0 + c) * ld];
-    }
+    C = work;
+    ldc = m;
+    work += (int64_t)m * kb;
+    for (int c = w; c < kb; c += nw)
+      for (int i = lane; i < m; i += 32) C[i + c * ldc] = A[(k0 + i) + (int64_t)(k0 + c) * ld];
+    __syncthreads();
   } else {
-    P = A + (int64_t)k0 * ld;
-    pld = ld;
+    C = A + k0 + (int64_t)k0 * ld;
+    ldc = ld;
   }
-  V* prow = work;      // kb
-  V* colk = work + kb; // n
+  V* prows = work;                                      // kb x kb
+  V* cb = prows + GJ_KB * GJ_KB;                        // 2m
+  double* red = reinterpret_cast<double*>(cb + 2 * m);  // 32
+  int* pos = reinterpret_cast<int*>(red + 32);          // m
+  int* disp = pos + m;                                  // kb
+  __shared__ int piv[GJ_KB];
+  __shared__ int ndisp;
+  for (int i = threadIdx.x; i < m; i += blockDim.x) {
+    cb[i] = C[i];
+    pos[i] = i;
+  }
   __syncthreads();
   const double scale2 = *t.scale2;
-  const double thresh = tol * tol * scale2;
-  for (int kk = 0; kk < kb; ++kk) {
-    const int k = k0 + kk;
-    T best = -1;
-    int bi = 0x7fffffff;
-    for (int i = k + threadIdx.x; i < np; i += blockDim.x) {
-      const T m = cnorm(P[i + kk * pld]);
-      if (m > best) { best = m; bi = i; }
-    }
-    double big;
-    const int p = block_argmax((double)best, bi, redv, redi, &big);
-    if (!(big > thresh) || p >= np) {
-      if (!perturb || !(big >= 0.0) || !(scale2 > 0.0) || p >= np) {
-        if (threadIdx.x == 0) *t.bad = 1;
-        return;
-      }
-      if (threadIdx.x == 0) {
-        V& d = P[p + kk * pld];
-        const double mag = sqrt(big), target = tol * sqrt(scale2);
-        if (mag > 0.0) { d.x = (T)(d.x / mag * target); d.y = (T)(d.y / mag * target); }
-        else { d.x = (T)target; d.y = (T)0; }
-      }
-      __syncthreads();
-    }
-    if (threadIdx.x == 0) t.piv[k] = p;
-    if (p != k) {
-      // Full-row interchange: the panel (staged or not) and every column outside it.
-      for (int c = threadIdx.x; c < kb; c += blockDim.x) {
-        V tmp = P[k + c * pld];
-        P[k + c * pld] = P[p + c * pld];
-        P[p + c * pld] = tmp;
-      }
-      for (int j = threadIdx.x; j < n; j += blockDim.x) {
-        if (j >= k0 && j < k0 + kb) continue;
-        V tmp = A[k + (int64_t)j * ld];
-        A[k + (int64_t)j * ld] = A[p + (int64_t)j * ld];
-        A[p + (int64_t)j * ld] = tmp;
-      }
-    }
-    __syncthreads();
-    const V inv = cinv(P[k + kk * pld]);
-    for (int c = threadIdx.x; c < kb; c += blockDim.x) prow[c] = (c == kk) ? inv : cmul(P[k + c * pld], inv);
-    for (int i = threadIdx.x; i < n; i += blockDim.x) colk[i] = P[i + kk * pld];
-    __syncthreads();
-    for (int64_t idx = threadIdx.x; idx < (int64_t)n * kb; idx += blockDim.x) {
-      const int i = (int)(idx % n), c = (int)(idx / n);
-      V* d = &P[i + c * pld];
-      if (i == k) *d = prow[c];
-      else if (c == kk) *d = cmul(cx<V>(-colk[i].x, -colk[i].y), inv);
-      else *d = cfms(*d, colk[i], prow[c]);
-    }
-    __syncthreads();
+  if (!gj_sweep<T>(C, (int)ldc, m, kb, kb, m, scale2, tol, cb, piv, perturb != 0, nullptr, prows)) {
+    if (threadIdx.x == 0) *t.bad = 1;
+    return;
   }
   if (staged)
-    for (int64_t idx = threadIdx.x; idx < (int64_t)n * kb; idx += blockDim.x) {
-      const int i = (int)(idx % n), c = (int)(idx / n);
-      A[i + (int64_t)(k0 + c) * ld] = P[idx];
+    for (int c = w; c < kb; c += nw)
+      for (int i = lane; i < m; i += 32) A[(k0 + i) + (int64_t)(k0 + c) * ld] = C[i + c * ldc];
+  if (threadIdx.x == 0)
+    for (int k = 0; k < kb; ++k) {
+      t.piv[k0 + k] = k0 + piv[k];
+      const int a = pos[k];
+      pos[k] = pos[piv[k]];
+      pos[piv[k]] = a;
     }
-  // Pivot rows of the rest columns, before the update.
+  if (w == 0) {
+    // Positions at or past kb that hold another row now: each is some piv[k] (they only ever
+    // receive rows from the first kb positions, so there are at most kb), listed once.
+    __syncwarp();
+    const int p = lane < kb ? piv[lane] : -1;
+    const bool moved = lane < kb && p >= kb && pos[p] != p;
+    const unsigned same = __match_any_sync(0xffffffffu, moved ? p : -1 - lane);
+    const bool leader = moved && (__ffs(same) - 1 == lane);
+    const unsigned bal = __ballot_sync(0xffffffffu, leader);
+    if (leader) disp[__popc(bal & ((1u << lane) - 1u))] = p;
+    if (lane == 0) ndisp = __popc(bal);
+  }
+  // 2. Rows outside the candidates: the sweep's steps replayed on each row, a thread per row.
+  const int nout = n - m;
+  for (int r = threadIdx.x; r < nout; r += blockDim.x) {
+    const int row = r < k0 ? r : r + m;
+    V* Ar = A + row + (int64_t)k0 * ld;
+    V a[GJ_KB];
+#pragma unroll
+    for (int c = 0; c < GJ_KB; ++c) a[c] = c < kb ? Ar[(int64_t)c * ld] : cx<V>(0.0, 0.0);
+    for (int k = 0; k < kb; ++k) {
+      const V* pk = prows + k * kb;
+      V ak = a[0];
+#pragma unroll
+      for (int c = 1; c < GJ_KB; ++c)
+        if (c == k) ak = a[c];
+#pragma unroll
+      for (int c = 0; c < GJ_KB; ++c) {
+        if (c >= kb) continue;
+        if (c == k) a[c] = cmul(cx<V>(-ak.x, -ak.y), pk[c]);
+        else a[c] = cfms(a[c], ak, pk[c]);
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < GJ_KB; ++c)
+      if (c < kb) Ar[(int64_t)c * ld] = a[c];
+  }
+  __syncthreads();
+  // 3. Pivot rows of the rest columns into Y; displaced rows into place. A warp per column.
   V* Y = static_cast<V*>(t.y);
-  for (int64_t idx = threadIdx.x; idx < (int64_t)kb * n; idx += blockDim.x) {
-    const int r = (int)(idx % kb), j = (int)(idx / kb);
+  const int nd = ndisp;
+  for (int j = w; j < n; j += nw) {
     if (j >= k0 && j < k0 + kb) continue;
-    Y[r + (int64_t)j * kb] = A[(k0 + r) + (int64_t)j * ld];
+    V* Aj = A + (int64_t)j * ld;
+    V yv = cx<V>(0.0, 0.0), dv = cx<V>(0.0, 0.0);
+    if (lane < kb) yv = Aj[k0 + pos[lane]];
+    if (lane < nd) dv = Aj[k0 + pos[disp[lane]]];
+    __syncwarp();
+    if (lane < kb) Y[lane + (int64_t)j * kb] = yv;
+    if (lane < nd) Aj[k0 + disp[lane]] = dv;
   }
 }
 
@@ -217,11 +242,16 @@ __global__ void __launch_bounds__(256) inv_update_kernel(const InvTask* __restri
     }
 }
 
-// Undo the row interchanges as column interchanges (last first); report refused pivots.
+// Undo the row interchanges as column interchanges (last first), as cycles of the resulting column
+// permutation: every thread moves its own rows, no barrier per interchange. Shared memory: cperm,
+// the cycle list and a visited mark (3 x npiv ints). Reports refused pivots.
+__host__ __device__ inline int64_t finish_bytes(int npiv) { return 3 * (int64_t)npiv * 4 + 16; }
+
 template <typename T>
 __global__ void __launch_bounds__(256) inv_finish_kernel(const InvTask* __restrict__ tasks, const JobDesc* jobs,
                                                          int32_t* __restrict__ status) {
   using V = typename Cx<T>::V;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   const InvTask t = tasks[blockIdx.x];
   if (*t.bad) {
     if (threadIdx.x == 0) {
@@ -230,16 +260,53 @@ __global__ void __launch_bounds__(256) inv_finish_kernel(const InvTask* __restri
     }
     return;
   }
+  const int np = t.npiv;
+  int* cperm = reinterpret_cast<int*>(smem_raw);
+  int* cyc = cperm + np;
+  int* seen = cyc + np;
+  __shared__ int ncyc;
+  for (int j = threadIdx.x; j < np; j += blockDim.x) {
+    cperm[j] = j;
+    seen[j] = 0;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    column_order(t.piv, np, cperm);
+    // Cycles of cperm, each closed by a marked (negative) last entry.
+    int len = 0;
+    for (int j = 0; j < np; ++j) {
+      if (seen[j] || cperm[j] == j) continue;
+      int c = j;
+      do {
+        seen[c] = 1;
+        cyc[len++] = c;
+        c = cperm[c];
+      } while (c != j);
+      cyc[len - 1] = -1 - cyc[len - 1];
+    }
+    ncyc = len;
+  }
+  __syncthreads();
   V* A = static_cast<V*>(t.a);
-  for (int k = t.npiv - 1; k >= 0; --k) {
-    const int p = t.piv[k];
-    if (p != k)
-      for (int i = threadIdx.x; i < t.n; i += blockDim.x) {
-        V a = A[i + (int64_t)k * t.ld];
-        A[i + (int64_t)k * t.ld] = A[i + (int64_t)p * t.ld];
-        A[i + (int64_t)p * t.ld] = a;
+  const int len = ncyc;
+  for (int i = threadIdx.x; i < t.n; i += blockDim.x) {
+    int q = 0;
+    while (q < len) {
+      // Cycle c_0 .. c_L-1 with cperm[c_a] = c_a+1: column c_a takes column c_a+1, the last c_0.
+      const int c0 = cyc[q];
+      const V first = A[i + (int64_t)c0 * t.ld];
+      int cur = c0;
+      while (true) {
+        const int nx = cyc[++q];
+        const bool last = nx < 0;
+        const int c = last ? -1 - nx : nx;
+        A[i + (int64_t)cur * t.ld] = A[i + (int64_t)c * t.ld];
+        cur = c;
+        if (last) break;
       }
-    __syncthreads();
+      A[i + (int64_t)cur * t.ld] = first;
+      ++q;
+    }
   }
 }
 

@@ -265,14 +265,15 @@ template <typename T> struct Prec {
 
 size_t small_smem(int n, size_t vbytes) {
   int ld = n | 1;
-  return (size_t)ld * n * vbytes + 2 * (size_t)n * vbytes + (size_t)((n + 1) & ~1) * 4 + 32 * 8 + 32 * 4 + 16;
+  return (size_t)ld * n * vbytes + 2 * (size_t)n * vbytes + 32 * 8 + 2 * (size_t)n * 4 + 16;
 }
-// Shared memory of a pivot-block launch whose largest block is ne: the staged block when it fits
-// under SMEM_LIMIT, else only the work vectors (the kernel then sweeps in global memory).
-size_t pivot_smem(int ne, size_t vbytes) {
-  size_t work = 2 * (size_t)ne * vbytes + (size_t)((ne + 1) & ~1) * 4 + 32 * 8 + 32 * 4 + 16;
-  size_t staged = (size_t)ne * (ne | 1) * vbytes + work;
-  return staged <= (size_t)SMEM_LIMIT ? staged : work;
+// Shared memory of a panel launch whose largest pivot count is pmax: the staged candidate rows
+// when they fit under SMEM_LIMIT, else only the work vectors (the kernel then sweeps the panel in
+// global memory); 0 when not even those fit.
+size_t panel_smem(int pmax, size_t vbytes) {
+  const int64_t staged = panel_staged_bytes(pmax, (int)vbytes), work = panel_work_bytes(pmax, (int)vbytes);
+  if (staged <= SMEM_LIMIT) return (size_t)staged;
+  return work <= SMEM_LIMIT ? (size_t)work : 0;
 }
 
 // Launches `fn(first, count)` over a task range in pieces of at most 65535 (grid y/z limit).
@@ -855,9 +856,9 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
       using TT = decltype(tag);
       using VV = typename Cx<TT>::V;
       if (!count || nmax <= 0 || pmax <= 0) return;
-      const size_t work = 2 * (size_t)nmax * sizeof(VV);
-      const size_t staged = (size_t)nmax * GJ_KB * sizeof(VV) + work;
-      const size_t sm = staged <= (size_t)SMEM_LIMIT ? staged : work;
+      const size_t sm = panel_smem(pmax, sizeof(VV));
+      const size_t smf = (size_t)finish_bytes(pmax);
+      if (!sm || smf > (size_t)SMEM_LIMIT) throw CudaError{cudaErrorInvalidValue, "front too large for a panel sweep"};
       const int panels = (pmax + GJ_KB - 1) / GJ_KB;
       const double per = flops / (2.0 * panels + 2.0);
       launch(cls, per, 0.0, [&] { inv_scale_kernel<TT><<<(unsigned)count, 256, 0, s>>>(dinv + first); });
@@ -872,7 +873,7 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
           });
         });
       }
-      launch(cls, per, 0.0, [&] { inv_finish_kernel<TT><<<(unsigned)count, 256, 0, s>>>(dinv + first, djobs, status); });
+      launch(cls, per, 0.0, [&] { inv_finish_kernel<TT><<<(unsigned)count, 256, smf, s>>>(dinv + first, djobs, status); });
     };
 
     CK(cudaEventRecord(ctx->ev0, s));
@@ -1154,7 +1155,7 @@ int caroli_ctx_create(int device_ordinal, caroli_ctx** out) {
     CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_ordinal));
     for (auto* k : {(const void*)small_front_kernel<double, false>, (const void*)small_front_kernel<float, false>,
                     (const void*)small_front_kernel<double, true>, (const void*)small_front_kernel<float, true>,
-                    (const void*)pivot_block_kernel<double>, (const void*)pivot_block_kernel<float>,
+                    (const void*)inv_finish_kernel<double>, (const void*)inv_finish_kernel<float>,
                     (const void*)inv_panel_kernel<double>, (const void*)inv_panel_kernel<float>,
                     (const void*)tiny_front_kernel<double, false>, (const void*)tiny_front_kernel<double, true>,
                     (const void*)tiny_front_kernel<float, false>, (const void*)tiny_front_kernel<float, true>,
@@ -1772,8 +1773,8 @@ extern "C" int caroli_solve_batch_noalloc(caroli_ctx* ctx, int plan_id, int coun
     CK(cudaMemcpyAsync(dinv, inv.data(), inv.size() * sizeof(InvTask), cudaMemcpyHostToDevice, s));
     auto sweep = [&](size_t first, size_t cnt, int nmax, int pmax, double tol) {
       if (!cnt) return;
-      const size_t work = 2 * (size_t)nmax * vb, staged = (size_t)nmax * GJ_KB * vb + work;
-      const size_t sm = staged <= (size_t)SMEM_LIMIT ? staged : work;
+      const size_t sm = panel_smem(pmax, vb), smf = (size_t)finish_bytes(pmax);
+      if (!sm || smf > (size_t)SMEM_LIMIT) throw CudaError{cudaErrorInvalidValue, "front too large for a panel sweep"};
       inv_scale_kernel<double><<<(unsigned)cnt, 256, 0, s>>>(dinv + first);
       for (int k0 = 0; k0 < pmax; k0 += GJ_KB) {
         inv_panel_kernel<double><<<(unsigned)cnt, 256, sm, s>>>(dinv + first, k0, tol, 0, (int)sm);
@@ -1782,7 +1783,7 @@ extern "C" int caroli_solve_batch_noalloc(caroli_ctx* ctx, int plan_id, int coun
           inv_update_kernel<double><<<dim3(rt, rt, (unsigned)c), 256, 0, s>>>(dinv + first + f0, k0);
         });
       }
-      inv_finish_kernel<double><<<(unsigned)cnt, 256, 0, s>>>(dinv + first, djobs, dstatus);
+      inv_finish_kernel<double><<<(unsigned)cnt, 256, smf, s>>>(dinv + first, djobs, dstatus);
     };
     for (int L = 0; L < max_levels; ++L) {
       const Lv& v = lv[L];

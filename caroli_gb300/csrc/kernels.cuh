@@ -191,85 +191,110 @@ __device__ __forceinline__ void apply_entries(const JobDesc& J, const FrontDesc&
 }
 
 // ---- Gauss-Jordan sweep -------------------------------------------------------------------------
-// In-place sweep of the leading ne pivots of an n x n matrix F (column-major, leading dimension
-// ld), pivot rows restricted to [k, ne). On exit (columns of the first block unpermuted)
-//   F[0:ne, 0:ne] = F11^-1, F[0:ne, ne:n] = X = F11^-1 F12,
-//   F[ne:n, 0:ne] = W = -F21 F11^-1, F[ne:n, ne:n] = S = F22 - F21 X.
-// Returns false when a pivot is not above tol * max|F11| (uniform in the block).
-// With `perturb`, a pivot below the threshold is replaced by tol * max|F11| in its own direction
-// (static pivoting, counted in *perturbed) instead of refusing the block: the factors then only
-// precondition an iterative refinement that removes the perturbation.
+// Largest value of a warp, ties to the smaller index (the reference keeps the first maximum); NaN
+// never wins, so a column of NaN reports -1 and fails the pivot test.
+template <typename T> __device__ __forceinline__ void warp_argmax(T& v, int& i) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const T v2 = __shfl_xor_sync(0xffffffffu, v, o);
+    const int i2 = __shfl_xor_sync(0xffffffffu, i, o);
+    if (v2 > v || (v2 == v && i2 < i)) { v = v2; i = i2; }
+  }
+}
+
+// In-place Gauss-Jordan sweep of the leading `npiv` columns of a rows x cols matrix F (column-major,
+// leading dimension ld), the pivot of step k chosen among rows [k, cand) of column k. On exit
+// (before the column interchanges) the swept rows hold, for the pivot block P (rows in pivot
+// order) and the other rows a: [P^-1 | P^-1 B] and [-a P^-1 | b - a P^-1 B].
+//
+// One __syncthreads per pivot: warp w owns the columns j = w (mod warps), lane l the rows l,
+// l + 32, ...; column k itself is read from the double buffer `cb` (2 x rows), which the owner of
+// column k + 1 fills while it updates it, so no warp reads a column another warp writes in the
+// same step. The row interchange of step k is folded into the update (row k receives the pivot
+// row, row p the old row k). `cb[0:rows]` must hold column 0 and be visible to the block.
+// piv[k] receives the pivot row of step k; with `prows`, prows[k * cols + j] receives the scaled
+// pivot row of step k (1 / pivot at j = k), from which other rows replay the same elimination.
+//
+// Returns false when a pivot is not above tol * sqrt(scale2) (uniform in the block: every warp
+// searches the same column). With `perturb` such a pivot is replaced by tol * sqrt(scale2) in its
+// own direction (static pivoting, counted in *perturbed) and the sweep goes on: the factors then
+// only precondition an iterative refinement that removes the perturbation.
 template <typename T>
-__device__ bool gj_sweep(typename Cx<T>::V* F, int64_t ld, int n, int ne, double tol, typename Cx<T>::V* prow,
-                         typename Cx<T>::V* colk, int* piv, double* redv, int* redi, bool perturb = false,
-                         int* perturbed = nullptr) {
+__device__ bool gj_sweep(typename Cx<T>::V* F, int ld, int rows, int cols, int npiv, int cand, double scale2,
+                         double tol, typename Cx<T>::V* cb, int* piv, bool perturb, int* perturbed,
+                         typename Cx<T>::V* prows = nullptr) {
   using V = typename Cx<T>::V;
-  const int tid = threadIdx.x, nt = blockDim.x;
-  T local = 0;
-  for (int64_t idx = tid; idx < (int64_t)ne * ne; idx += nt) {
-    int i = (int)(idx % ne), j = (int)(idx / ne);
-    local = fmax(local, cnorm(F[i + j * ld]));
-  }
-  const double scale2 = block_max((double)local, redv);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const double thresh = tol * tol * scale2;
-  for (int k = 0; k < ne; ++k) {
+  for (int k = 0; k < npiv; ++k) {
+    const V* ck = cb + (k & 1) * rows;
+    V* cn = cb + ((k + 1) & 1) * rows;
     T best = -1;
-    int bi = 0x7fffffff;
-    for (int i = k + tid; i < ne; i += nt) {
-      const T m = cnorm(F[i + k * ld]);
-      if (m > best) { best = m; bi = i; }
+    int p = 0x7fffffff;
+    for (int i = k + lane; i < cand; i += 32) {
+      const T m = cnorm(ck[i]);
+      if (m > best) { best = m; p = i; }
     }
-    double big;
-    int p = block_argmax((double)best, bi, redv, redi, &big);
-    if (!(big > thresh) || p >= ne) {
-      if (!perturb) return false;
+    warp_argmax(best, p);
+    const double big = (double)best;
+    V d;
+    if (!(big > thresh) || p >= cand) {
       // NaN or an empty column: nothing sensible to perturb.
-      if (!(big >= 0.0) || !(scale2 > 0.0) || p >= ne) return false;
-      if (tid == 0) {
-        V& d = F[p + k * ld];
-        const double mag = sqrt(big), target = tol * sqrt(scale2);
-        if (mag > 0.0) { d.x = (T)(d.x / mag * target); d.y = (T)(d.y / mag * target); }
-        else { d.x = (T)target; d.y = (T)0; }
-        if (perturbed) atomicAdd(perturbed, 1);
-      }
-      __syncthreads();
+      if (!perturb || !(big >= 0.0) || !(scale2 > 0.0) || p >= cand) return false;
+      d = ck[p];
+      const double mag = sqrt(big), target = tol * sqrt(scale2);
+      if (mag > 0.0) { d.x = (T)(d.x / mag * target); d.y = (T)(d.y / mag * target); }
+      else { d.x = (T)target; d.y = (T)0; }
+      if (threadIdx.x == 0 && perturbed) atomicAdd(perturbed, 1);
+    } else {
+      d = ck[p];
     }
-    if (tid == 0) piv[k] = p;
-    if (p != k)
-      for (int j = tid; j < n; j += nt) {
-        V a = F[k + j * ld];
-        F[k + j * ld] = F[p + j * ld];
-        F[p + j * ld] = a;
+    if (threadIdx.x == 0) piv[k] = p;
+    const V inv = cinv(d);
+    const V ckk = ck[k];  // old row k of column k (moves to row p)
+    for (int j = w; j < cols; j += nw) {
+      V* Fj = F + (int64_t)j * ld;
+      const bool fill = (j == k + 1) && (j < npiv);
+      if (j == k) {
+        if (prows && lane == 0) prows[k * cols + j] = inv;
+        for (int i = lane; i < rows; i += 32) {
+          const V c = (i == p) ? ckk : ck[i];
+          const V nv = (i == k) ? inv : cmul(cx<V>(-c.x, -c.y), inv);
+          Fj[i] = nv;
+        }
+        continue;
       }
-    __syncthreads();
-    const V inv = cinv(F[k + k * ld]);
-    for (int j = tid; j < n; j += nt) prow[j] = (j == k) ? inv : cmul(F[k + j * ld], inv);
-    for (int i = tid; i < n; i += nt) colk[i] = F[i + k * ld];
-    __syncthreads();
-    for (int64_t idx = tid; idx < (int64_t)n * n; idx += nt) {
-      const int i = (int)(idx % n), j = (int)(idx / n);
-      V* d = &F[i + j * ld];
-      if (i == k) *d = prow[j];
-      else if (j == k) *d = cmul(cx<V>(-colk[i].x, -colk[i].y), inv);
-      else *d = cfms(*d, colk[i], prow[j]);
+      const V pr = cmul(Fj[p], inv);
+      const V rk = Fj[k];
+      if (prows && lane == 0) prows[k * cols + j] = pr;
+      __syncwarp();  // rows k and p are read by every lane before their owners write them
+      for (int i = lane; i < rows; i += 32) {
+        V nv;
+        if (i == k) {
+          nv = pr;
+        } else {
+          const V c = (i == p) ? ckk : ck[i];
+          nv = cfms((i == p) ? rk : Fj[i], c, pr);
+        }
+        Fj[i] = nv;
+        if (fill) cn[i] = nv;
+      }
     }
-    __syncthreads();
-  }
-  // Undo the row interchanges as column interchanges of the inverse, last first.
-  for (int k = ne - 1; k >= 0; --k) {
-    int p = piv[k];
-    if (p != k)
-      for (int i = tid; i < n; i += nt) {
-        V a = F[i + k * ld];
-        F[i + k * ld] = F[i + p * ld];
-        F[i + p * ld] = a;
-      }
     __syncthreads();
   }
   return true;
 }
 
+// Column order after undoing the row interchanges of a sweep as column interchanges of the
+// inverse, last first: the result's column j is column cperm[j] of the swept matrix.
+__device__ __forceinline__ void column_order(const int* piv, int npiv, int* cperm) {
+  for (int k = npiv - 1; k >= 0; --k) {
+    const int p = piv[k];
+    if (p != k) { const int a = cperm[k]; cperm[k] = cperm[p]; cperm[p] = a; }
+  }
+}
+
 // ---- small fronts: assembly and elimination in shared memory, one CTA per front ---------------
+// Shared memory: the front (n x (n | 1)), the column buffer (2n), 32 doubles, piv and cperm (n).
 template <typename T, bool KEEP>
 __global__ void __launch_bounds__(256) small_front_kernel(const JobDesc* __restrict__ jobs,
                                                           const Task* __restrict__ tasks, double tol, int perturb,
@@ -278,36 +303,48 @@ __global__ void __launch_bounds__(256) small_front_kernel(const JobDesc* __restr
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const Task t = tasks[blockIdx.x];
   const JobDesc& J = jobs[t.job];
-  const FrontDesc f = J.fronts[t.front];
+  const FrontDesc& f = J.fronts[t.front];
   const int n = f.n, ne = f.ne;
   const int ld = n | 1;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
   V* F = reinterpret_cast<V*>(smem_raw);
-  V* prow = F + (int64_t)ld * n;
-  V* colk = prow + n;
-  int* piv = reinterpret_cast<int*>(colk + n);
-  double* redv = reinterpret_cast<double*>(piv + ((n + 1) & ~1));
-  int* redi = reinterpret_cast<int*>(redv + 32);
-  for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
-    int i = idx % n, j = idx / n;
-    F[i + j * ld] = gather<T>(J, f, i, j, false);
-  }
+  V* cb = F + (int64_t)ld * n;
+  double* red = reinterpret_cast<double*>(cb + 2 * n);
+  int* piv = reinterpret_cast<int*>(red + 32);
+  int* cperm = piv + n;
+  for (int j = w; j < n; j += nw)
+    for (int i = lane; i < n; i += 32) F[i + j * ld] = gather<T>(J, f, i, j, false);
   __syncthreads();
   apply_entries<T>(J, f, F, ld, 0, n);
   __syncthreads();
   V* out = static_cast<V*>(J.arena) + f.arena_off;
   if (ne == 0) {
-    for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) out[idx] = F[idx % n + (idx / n) * ld];
+    for (int j = w; j < n; j += nw)
+      for (int i = lane; i < n; i += 32) out[i + (int64_t)j * n] = F[i + j * ld];
     return;
   }
-  bool ok = gj_sweep<T>(F, ld, n, ne, tol, prow, colk, piv, redv, redi, perturb != 0, perturbed ? perturbed + t.job : nullptr);
+  T local = 0;
+  for (int j = w; j < ne; j += nw)
+    for (int i = lane; i < ne; i += 32) local = fmax(local, cnorm(F[i + j * ld]));
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    cb[i] = F[i];
+    cperm[i] = i;
+  }
+  const double scale2 = block_max((double)local, red);  // also publishes cb
+  const bool ok = gj_sweep<T>(F, ld, n, n, ne, ne, scale2, tol, cb, piv, perturb != 0,
+                              perturbed ? perturbed + t.job : nullptr);
   if (!ok) {
     if (threadIdx.x == 0) J.fail[t.front] = 1;
     return;
   }
-  for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
-    int i = idx % n, j = idx / n;
-    if (!KEEP && (i < ne || j < ne)) continue;
-    out[i + (int64_t)j * n] = F[i + j * ld];
+  if (threadIdx.x == 0) column_order(piv, ne, cperm);
+  __syncthreads();
+  for (int j = w; j < n; j += nw) {
+    const V* Fj = F + cperm[j] * ld;
+    for (int i = lane; i < n; i += 32) {
+      if (!KEEP && (i < ne || j < ne)) continue;
+      out[i + (int64_t)j * n] = Fj[i];
+    }
   }
 }
 
@@ -320,159 +357,16 @@ __global__ void __launch_bounds__(256) assemble_kernel(const JobDesc* __restrict
   using V = typename Cx<T>::V;
   const Task t = tasks[blockIdx.y];
   const JobDesc& J = jobs[t.job];
-  const FrontDesc f = J.fronts[t.front];
+  const FrontDesc& f = J.fronts[t.front];
   const int n = f.n;
   const int c0 = blockIdx.x * 32;
   if (c0 >= n) return;
   const int c1 = min(n, c0 + 32);
   V* F = is_root ? static_cast<V*>(J.root_arena) : static_cast<V*>(J.arena) + f.arena_off;
-  for (int64_t idx = threadIdx.x; idx < (int64_t)n * (c1 - c0); idx += blockDim.x) {
-    int i = (int)(idx % n), j = c0 + (int)(idx / n);
-    F[i + (int64_t)j * n] = gather<TC, T>(J, f, i, j, is_root != 0);
-  }
+  for (int j = c0 + (threadIdx.x >> 5); j < c1; j += blockDim.x >> 5)
+    for (int i = threadIdx.x & 31; i < n; i += 32) F[i + (int64_t)j * n] = gather<TC, T>(J, f, i, j, is_root != 0);
   __syncthreads();
   apply_entries<T>(J, f, F, n, c0, c1);
-}
-
-// Sweep of the pivot block F11 of a large front (or the whole root front), one CTA per front.
-// The block is staged in shared memory when it fits, else swept in place (L2-resident).
-template <typename T>
-__global__ void __launch_bounds__(1024) pivot_block_kernel(const JobDesc* __restrict__ jobs,
-                                                           const Task* __restrict__ tasks, double tol,
-                                                           int smem_bytes, int is_root,
-                                                           int32_t* __restrict__ root_status, int perturb,
-                                                           int* __restrict__ perturbed) {
-  using V = typename Cx<T>::V;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const Task t = tasks[blockIdx.x];
-  const JobDesc& J = jobs[t.job];
-  const FrontDesc f = J.fronts[t.front];
-  const int n = f.n;
-  const int ne = is_root ? n : f.ne;
-  if (ne == 0) return;
-  V* G = is_root ? static_cast<V*>(J.root_arena) : static_cast<V*>(J.arena) + f.arena_off;
-  // Stage the block in shared memory only when it fits in what this launch allocated.
-  const int64_t extra = 2 * (int64_t)ne * sizeof(V) + ((ne + 1) & ~1) * 4 + 32 * 8 + 32 * 4 + 16;
-  const bool staged = (int64_t)ne * (ne | 1) * (int64_t)sizeof(V) + extra <= smem_bytes;
-  V* buf = reinterpret_cast<V*>(smem_raw);
-  V* F = G;
-  int64_t ld = n;
-  int64_t off = staged ? (int64_t)ne * (ne | 1) : 0;
-  if (staged) {
-    ld = ne | 1;
-    F = buf;
-    for (int64_t idx = threadIdx.x; idx < (int64_t)ne * ne; idx += blockDim.x) {
-      int i = (int)(idx % ne), j = (int)(idx / ne);
-      F[i + j * ld] = G[i + (int64_t)j * n];
-    }
-    __syncthreads();
-  }
-  V* prow = buf + off;
-  V* colk = prow + ne;
-  int* piv = reinterpret_cast<int*>(colk + ne);
-  double* redv = reinterpret_cast<double*>(piv + ((ne + 1) & ~1));
-  int* redi = reinterpret_cast<int*>(redv + 32);
-  bool ok = gj_sweep<T>(F, ld, ne, ne, tol, prow, colk, piv, redv, redi, perturb != 0, perturbed ? perturbed + t.job : nullptr);
-  if (!ok) {
-    if (threadIdx.x == 0) {
-      if (is_root) root_status[t.job] = ST_SINGULAR;
-      else J.fail[t.front] = 1;
-    }
-    return;
-  }
-  if (staged)
-    for (int64_t idx = threadIdx.x; idx < (int64_t)ne * ne; idx += blockDim.x) {
-      int i = (int)(idx % ne), j = (int)(idx / ne);
-      G[i + (int64_t)j * n] = F[i + j * ld];
-    }
-}
-
-// Batched complex GEMM on the fronts of a level:
-//   mode 0: X = F11^-1 F12 into the level scratch (ld ne)
-//   mode 1: F22 -= F21 X
-// 64 x 64 tiles, 256 threads, 4 x 4 complex results per thread.
-template <typename T>
-__global__ void __launch_bounds__(256) front_gemm_kernel(const JobDesc* __restrict__ jobs, const Task* __restrict__ tasks,
-                                                         typename Cx<T>::V* __restrict__ xs, int mode) {
-  using V = typename Cx<T>::V;
-  constexpr int BM = 64, BN = 64, BK = 16;
-  __shared__ V As[BK][BM];
-  __shared__ V Bs[BK][BN + 1];
-  const Task t = tasks[blockIdx.z];
-  const JobDesc& J = jobs[t.job];
-  const FrontDesc f = J.fronts[t.front];
-  const int n = f.n, ne = f.ne, nb = n - ne;
-  if (ne == 0 || nb == 0) return;
-  V* F = static_cast<V*>(J.arena) + f.arena_off;
-  V* X = xs + t.xoff;
-  const V *A, *B;
-  V* C;
-  int M, N, K;
-  int64_t lda, ldb, ldc;
-  if (mode == 0) { A = F; lda = n; B = F + (int64_t)ne * n; ldb = n; C = X; ldc = ne; M = ne; N = nb; K = ne; }
-  else { A = F + ne; lda = n; B = X; ldb = ne; C = F + ne + (int64_t)ne * n; ldc = n; M = nb; N = nb; K = ne; }
-  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
-  if (m0 >= M || n0 >= N) return;
-  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  V acc[4][4];
-#pragma unroll
-  for (int r = 0; r < 4; ++r)
-#pragma unroll
-    for (int c = 0; c < 4; ++c) acc[r][c] = cx<V>(0.0, 0.0);
-  for (int k0 = 0; k0 < K; k0 += BK) {
-    for (int idx = threadIdx.x; idx < BM * BK; idx += 256) {
-      int i = idx % BM, k = idx / BM;
-      int gi = m0 + i, gk = k0 + k;
-      As[k][i] = (gi < M && gk < K) ? A[gi + (int64_t)gk * lda] : cx<V>(0.0, 0.0);
-    }
-    for (int idx = threadIdx.x; idx < BK * BN; idx += 256) {
-      int k = idx % BK, j = idx / BK;
-      int gk = k0 + k, gj = n0 + j;
-      Bs[k][j] = (gk < K && gj < N) ? B[gk + (int64_t)gj * ldb] : cx<V>(0.0, 0.0);
-    }
-    __syncthreads();
-#pragma unroll 4
-    for (int k = 0; k < BK; ++k) {
-      V a[4], b[4];
-#pragma unroll
-      for (int r = 0; r < 4; ++r) a[r] = As[k][tx + 16 * r];
-#pragma unroll
-      for (int c = 0; c < 4; ++c) b[c] = Bs[k][ty + 16 * c];
-#pragma unroll
-      for (int r = 0; r < 4; ++r)
-#pragma unroll
-        for (int c = 0; c < 4; ++c) acc[r][c] = cfma(acc[r][c], a[r], b[c]);
-    }
-    __syncthreads();
-  }
-#pragma unroll
-  for (int r = 0; r < 4; ++r)
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      int gi = m0 + tx + 16 * r, gj = n0 + ty + 16 * c;
-      if (gi < M && gj < N) {
-        V* d = &C[gi + (int64_t)gj * ldc];
-        if (mode == 0) *d = acc[r][c];
-        else *d = csub(*d, acc[r][c]);
-      }
-    }
-}
-
-// X from the level scratch into its place in the front (F12).
-template <typename T>
-__global__ void __launch_bounds__(256) store_x_kernel(const JobDesc* __restrict__ jobs, const Task* __restrict__ tasks,
-                                                      const typename Cx<T>::V* __restrict__ xs) {
-  using V = typename Cx<T>::V;
-  const Task t = tasks[blockIdx.y];
-  const JobDesc& J = jobs[t.job];
-  const FrontDesc f = J.fronts[t.front];
-  const int n = f.n, ne = f.ne, nb = n - ne;
-  V* F = static_cast<V*>(J.arena) + f.arena_off;
-  const V* X = xs + t.xoff;
-  for (int64_t idx = blockIdx.x * 256 + threadIdx.x; idx < (int64_t)ne * nb; idx += (int64_t)gridDim.x * 256) {
-    int i = (int)(idx % ne), j = (int)(idx / ne);
-    F[i + (int64_t)(ne + j) * n] = X[idx];
-  }
 }
 
 // ---- root: Caroli trace -------------------------------------------------------------------------

@@ -93,3 +93,27 @@ def test_mixed_bench_w32(problem):
     for s, tm in zip(sigmas, t):
         ref = oracle_T(sys_, s)
         assert abs(tm - ref) <= 1e-8, (problem, s.energy, tm, ref)
+
+
+def test_magnetic_200x64_double_and_mixed_match_oracle():
+    """The full-size magnetic workload (BHZ 200 x 64, c = 0.2, J = 0.4, eight configurations) at the
+    band edge E = -0.16, where ill-conditioned pivot blocks occur: FP64 and mixed both within 1e-8
+    of the oracle."""
+    from oracle import Oracle
+
+    sys_ = magnetic_bhz(200, 64, configs=8)
+    s = sys_.self_energies(-0.16)
+    cfg = list(range(8))
+    t64, st64, _ = sys_.solve_batch([s] * 8, cfg, Precision.DOUBLE)
+    tm, stm, _ = sys_.solve_batch([s] * 8, cfg, Precision.MIXED)
+    assert (st64 == 0).all() and (stm == 0).all()
+    orc = Oracle(sys_.system)
+    nb = sys_.block_count()
+    blocks = [b for _ in cfg for b in range(nb)]
+    ref, st = orc.solve_batch(blocks, [s.energy] * len(blocks), [sys_.system.values[c] for c in cfg for _ in range(nb)],
+                              [s.blocks[b][0] for _ in cfg for b in range(nb)],
+                              [s.blocks[b][1] for _ in cfg for b in range(nb)], threads=0)
+    assert (st == 0).all()
+    ref = ref.reshape(8, nb).sum(axis=1)
+    assert np.abs(t64 - ref).max() <= 1e-8, np.abs(t64 - ref)
+    assert np.abs(tm - ref).max() <= 1e-8, np.abs(tm - ref)
