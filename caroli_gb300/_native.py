@@ -41,6 +41,8 @@ SIGNATURES = {
     "caroli_transmission_with_grad": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P]),
     "caroli_kernel_classes": (ctypes.c_int, []),
     "caroli_last_job_info": (ctypes.c_int, [P, I64, P, P, P, P]),
+    "caroli_last_refine_steps": (ctypes.c_int, [P, P, P]),
+    "caroli_set_refine_options": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_double, ctypes.c_double]),
     "caroli_kernel_class_name": (ctypes.c_char_p, [ctypes.c_int]),
     "caroli_probe_kernel": (ctypes.c_int, [P, ctypes.c_int]),
     "caroli_kernel_stats": (ctypes.c_int, [P, ctypes.c_int, P, P, P, P, ctypes.c_int]),
@@ -98,6 +100,10 @@ class Context:
         ms, n = ctypes.c_double(), ctypes.c_int64()
         self.check(self.lib.caroli_region_end(self.h, ctypes.byref(ms), ctypes.byref(n)))
         return ms.value, n.value
+
+    def set_refine_options(self, max_iters=6, tol=1e-10, inner_tol=1e-10):
+        """Mixed-precision refinement controls (``caroli_set_refine_options``)."""
+        self.check(self.lib.caroli_set_refine_options(self.h, int(max_iters), float(tol), float(inner_tol)))
 
     def kernel_classes(self):
         return [self.lib.caroli_kernel_class_name(k).decode() for k in range(self.lib.caroli_kernel_classes())]
@@ -200,6 +206,12 @@ class Plan:
         fb, it = ctypes.c_int64(), ctypes.c_int64()
         self.ctx.check(self.ctx.lib.caroli_last_stats(self.ctx.h, ctypes.byref(fb), ctypes.byref(it)))
         return fb.value, it.value
+
+    def last_refine_steps(self):
+        """(GMRES steps summed over the block solves, steps the batch launched) of the last solve."""
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        self.ctx.check(self.ctx.lib.caroli_last_refine_steps(self.ctx.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
 
     def last_phases(self):
         a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()

@@ -24,6 +24,7 @@
 #include "refine.cuh"
 #include "dense.cuh"
 #include "tiny.cuh"
+#include "sweep.cuh"
 
 using namespace caroli;
 
@@ -65,11 +66,15 @@ struct DevPlan {
   uint8_t* own = nullptr;
   Entry* entries = nullptr;
   int32_t* vidx = nullptr;
+  SweepRow* srows = nullptr;
   void upload(cudaStream_t s) {
     fronts = dalloc<FrontDesc>(host.fronts.size());
     vidx = dalloc<int32_t>(std::max<size_t>(1, host.vidx.size()));
     if (!host.vidx.empty())
       CK(cudaMemcpyAsync(vidx, host.vidx.data(), host.vidx.size() * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    srows = dalloc<SweepRow>(std::max<size_t>(1, host.srows.size()));
+    if (!host.srows.empty())
+      CK(cudaMemcpyAsync(srows, host.srows.data(), host.srows.size() * sizeof(SweepRow), cudaMemcpyHostToDevice, s));
     maps = dalloc<int32_t>(std::max<size_t>(1, host.maps.size()));
     own = dalloc<uint8_t>(std::max<size_t>(1, host.own.size()));
     entries = dalloc<Entry>(std::max<size_t>(1, host.entries.size()));
@@ -83,8 +88,8 @@ struct DevPlan {
     CK(cudaStreamSynchronize(s));
   }
   void release() {
-    cudaFree(fronts); cudaFree(maps); cudaFree(own); cudaFree(entries); cudaFree(vidx);
-    fronts = nullptr; maps = nullptr; own = nullptr; entries = nullptr; vidx = nullptr;
+    cudaFree(fronts); cudaFree(maps); cudaFree(own); cudaFree(entries); cudaFree(vidx); cudaFree(srows);
+    fronts = nullptr; maps = nullptr; own = nullptr; entries = nullptr; vidx = nullptr; srows = nullptr;
   }
 };
 
@@ -178,6 +183,7 @@ struct JobSpec {
 struct RefineBufs {
   Buf rdesc, rx, rr, rd, rtb, rhb, rt, rerr, rdone;
   Buf gV, gZ, gH, gg, gcs, gsn, gy, gbeta, gcol, gflags;
+  Buf segs, ctasks, ccount, cjobs;  // task lists compacted to the solves still iterating
 };
 
 // A gradient request: d H / d p values of every configuration, and the per-job outputs.
@@ -239,6 +245,8 @@ struct caroli_ctx {
   int64_t last_launches = 0;
   int64_t fallbacks = 0;
   int64_t refine_iters = 0;
+  int64_t refine_job_steps = 0;    // Arnoldi steps summed over the solves
+  int64_t refine_batch_steps = 0;  // Arnoldi steps launched for the batch (the slowest solve's)
   std::vector<int32_t> job_iters, job_perturbed, job_status;
   size_t mem_budget = 0;
 };
@@ -285,6 +293,7 @@ struct LevelRange {
   size_t tiny0, tiny_n;  // fronts of at most TINY_MAX variables (one warp each)
   size_t first, count;   // the others
   int max_n;
+  int max_ne;            // bound on the eliminated variables of the others
 };
 
 // FP64 iterative refinement of the jobs [begin, begin + cj) after their f32 factorization.
@@ -347,7 +356,7 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
     const SigmaSlot& sg = sys->slots[sp.slot];
     RefineDesc& R = rdh[j];
     std::memset(&R, 0, sizeof(R));
-    R.fronts = P.fronts; R.maps = P.maps; R.own = P.own; R.vidx = P.vidx;
+    R.fronts = P.fronts; R.maps = P.maps; R.own = P.own; R.vidx = P.vidx; R.srows = P.srows;
     R.arena = arena + arena_off[j];
     R.root = rarena + root_off[j];
     R.csr_ptr = B.csr_ptr; R.csr_col = B.csr_col; R.csr_q = B.csr_q;
@@ -375,7 +384,9 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
   }
   RefineDesc* drd = static_cast<RefineDesc*>(rb.rdesc.get(cj * sizeof(RefineDesc)));
   CK(cudaMemcpyAsync(drd, rdh.data(), cj * sizeof(RefineDesc), cudaMemcpyHostToDevice, s));
-  const unsigned cchunks = (unsigned)std::max(1, (cmax + RCB - 1) / RCB);
+  // Right-hand-side columns per CTA: the batch's largest channel count, rounded up to 1, 2, 4, 8.
+  const int cbw = cmax <= 1 ? 1 : cmax <= 2 ? 2 : cmax <= 4 ? 4 : 8;
+  const unsigned cchunks = (unsigned)std::max(1, (cmax + cbw - 1) / cbw);
   in_pieces(cj, [&](size_t f0, size_t c) {
     launch(K_REF_RES, 0.0, 0.0, [&] { refine_init_kernel<<<dim3(16, (unsigned)c), 256, 0, s>>>(drd + f0, (int)c); });
   });
@@ -383,41 +394,85 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
   const int nlev = (int)lr.size();
   const unsigned rows = (unsigned)((max_blk + 255) / 256);
   const unsigned cols = (unsigned)std::max(1, cmax);
-  // Preconditioner application M^-1 V_k -> Z_k (src = dst = k).
-  auto sweep = [&](int src, int dst) {
+  // Task segments (per level: tiny fronts, then the others) and their compacted copies.
+  const int nseg = 2 * nlev;
+  std::vector<TaskSeg> segs(nseg);
+  int64_t seg_max = 0;
+  for (int L = 0; L < nlev; ++L) {
+    segs[2 * L] = {(int64_t)lr[L].tiny0, (int64_t)lr[L].tiny_n};
+    segs[2 * L + 1] = {(int64_t)lr[L].first, (int64_t)lr[L].count};
+    seg_max = std::max<int64_t>(seg_max, std::max(lr[L].tiny_n, lr[L].count));
+  }
+  size_t ntask_all = 0;
+  for (const auto& sg : segs) ntask_all = std::max<size_t>(ntask_all, (size_t)(sg.first + sg.count));
+  TaskSeg* dsegs = static_cast<TaskSeg*>(rb.segs.get(nseg * sizeof(TaskSeg)));
+  Task* ctasks = static_cast<Task*>(rb.ctasks.get(std::max<size_t>(ntask_all, 1) * sizeof(Task)));
+  int32_t* ccount = static_cast<int32_t*>(rb.ccount.get((nseg + 1) * sizeof(int32_t)));
+  int32_t* cjobs = static_cast<int32_t*>(rb.cjobs.get(cj * sizeof(int32_t)));
+  CK(cudaMemcpyAsync(dsegs, segs.data(), nseg * sizeof(TaskSeg), cudaMemcpyHostToDevice, s));
+  std::vector<int32_t> hcount(nseg + 1, 0);
+  // Compacts the lists to the solves still iterating; the counts reach the host with the next
+  // synchronisation.
+  auto compact = [&](int inner) {
+    CK(cudaMemsetAsync(ccount, 0, (nseg + 1) * sizeof(int32_t), s));
+    const unsigned gx = (unsigned)std::max<int64_t>(1, (std::max<int64_t>(seg_max, (int64_t)cj) + 255) / 256);
+    launch(K_REF_GMRES, 0.0, 0.0, [&] {
+      compact_kernel<<<dim3(gx, (unsigned)(nseg + 1)), 256, 0, s>>>(drd, (int)cj, dtasks, dsegs, nseg, ctasks, cjobs,
+                                                                  ccount, inner);
+    });
+    CK(cudaMemcpyAsync(hcount.data(), ccount, (nseg + 1) * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  };
+  compact(0);
+  CK(cudaStreamSynchronize(s));
+  auto sweep_cb = [&](auto cbt, int src, int dst) {
+    constexpr int CB = decltype(cbt)::value;
     for (int L = 0; L < nlev; ++L) {
-      if (lr[L].tiny_n)
+      const int nt = hcount[2 * L], nr = hcount[2 * L + 1];
+      if (nt)
         launch(K_REF_FWD, 0.0, 0.0, [&] {
-          tiny_forward_kernel<<<(unsigned)((lr[L].tiny_n + TINY_WARPS - 1) / TINY_WARPS), 256, 0, s>>>(
-              drd, dtasks + lr[L].tiny0, (int)lr[L].tiny_n, src);
+          sweep_tiny_fwd_kernel<CB><<<dim3((unsigned)((nt + TINY_WARPS - 1) / TINY_WARPS), cchunks), 256, 0, s>>>(
+              drd, ctasks + lr[L].tiny0, nt, src);
         });
-      if (!lr[L].count) continue;
-      const size_t sm = (size_t)lr[L].max_n * RCB * sizeof(float2);
-      const unsigned rows = (unsigned)((lr[L].max_n + SW_ROWS - 1) / SW_ROWS);
-      launch(K_REF_FWD, 0.0, sweep_bytes * 0.5 / nlev, [&] {
-        refine_forward_rows_kernel<<<dim3((unsigned)lr[L].count, rows, cchunks), 256, sm, s>>>(
-            drd, dtasks + lr[L].first, src);
+      if (!nr) continue;
+      const size_t sm = (size_t)std::max(1, lr[L].max_ne) * CB * sizeof(float2);
+      const unsigned tiles = (unsigned)((lr[L].max_n + SW_ROWS - 1) / SW_ROWS);
+      in_pieces((size_t)nr, [&](size_t f0, size_t c) {
+        launch(K_REF_FWD, 0.0, sweep_bytes * 0.5 / nlev, [&] {
+          sweep_rows_fwd_kernel<CB><<<dim3((unsigned)c, tiles, cchunks), 256, sm, s>>>(drd, ctasks + lr[L].first + f0,
+                                                                                     src);
+        });
       });
     }
-    in_pieces(cj, [&](size_t f0, size_t c) {
+    const int nj = hcount[nseg];
+    if (nj)
       launch(K_REF_ROOT, 0.0, 0.0, [&] {
-        refine_root_kernel<<<dim3((unsigned)c, cchunks), 256, (size_t)max_root * RCB * sizeof(float2), s>>>(drd + f0, src,
-                                                                                                        dst);
+        sweep_root_kernel<CB><<<dim3((unsigned)nj, cchunks), 256, (size_t)max_root * CB * sizeof(float2), s>>>(
+            drd, cjobs, src, dst);
       });
-    });
     for (int L = nlev - 1; L >= 0; --L) {
-      if (lr[L].tiny_n)
+      const int nt = hcount[2 * L], nr = hcount[2 * L + 1];
+      if (nt)
         launch(K_REF_BWD, 0.0, 0.0, [&] {
-          tiny_backward_kernel<<<(unsigned)((lr[L].tiny_n + TINY_WARPS - 1) / TINY_WARPS), 256, 0, s>>>(
-              drd, dtasks + lr[L].tiny0, (int)lr[L].tiny_n, src, dst);
+          sweep_tiny_bwd_kernel<CB><<<dim3((unsigned)((nt + TINY_WARPS - 1) / TINY_WARPS), cchunks), 256, 0, s>>>(
+              drd, ctasks + lr[L].tiny0, nt, src, dst);
         });
-      if (!lr[L].count) continue;
-      const size_t sm = (size_t)lr[L].max_n * RCB * sizeof(float2);
-      const unsigned rows = (unsigned)((lr[L].max_n + SW_ROWS - 1) / SW_ROWS);
-      launch(K_REF_BWD, 0.0, sweep_bytes * 0.5 / nlev, [&] {
-        refine_backward_rows_kernel<<<dim3((unsigned)lr[L].count, rows, cchunks), 256, sm, s>>>(
-            drd, dtasks + lr[L].first, src, dst);
+      if (!nr) continue;
+      const size_t sm = (size_t)std::max(1, lr[L].max_n) * CB * sizeof(float2);
+      const unsigned tiles = (unsigned)((std::max(1, lr[L].max_ne) + SW_ROWS - 1) / SW_ROWS);
+      in_pieces((size_t)nr, [&](size_t f0, size_t c) {
+        launch(K_REF_BWD, 0.0, sweep_bytes * 0.5 / nlev, [&] {
+          sweep_rows_bwd_kernel<CB><<<dim3((unsigned)c, tiles, cchunks), 256, sm, s>>>(drd, ctasks + lr[L].first + f0,
+                                                                                     src, dst);
+        });
       });
+    }
+  };
+  auto sweep = [&](int src, int dst) {
+    switch (cbw) {
+      case 1: sweep_cb(std::integral_constant<int, 1>{}, src, dst); break;
+      case 2: sweep_cb(std::integral_constant<int, 2>{}, src, dst); break;
+      case 4: sweep_cb(std::integral_constant<int, 4>{}, src, dst); break;
+      default: sweep_cb(std::integral_constant<int, 8>{}, src, dst); break;
     }
   };
   for (int it = 0; it < ctx->max_iters; ++it) {
@@ -426,6 +481,7 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
     });
     for (int k = 0; k < GM_M; ++k) {
       sweep(k, k);
+      ctx->refine_batch_steps += 1;
       in_pieces(cj, [&](size_t f0, size_t c) {
         launch(K_REF_RES, resid_flops * c / cj, 0.0,
                [&] { gm_matvec_kernel<<<dim3((unsigned)c, rows), 256, 0, s>>>(drd + f0, k); });
@@ -444,6 +500,7 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
       launch(K_REF_GMRES, 0.0, 0.0, [&] {
         gm_inner_check_kernel<<<(unsigned)((cj + 127) / 128), 128, 0, s>>>(drd, (int)cj, k, gflags);
       });
+      compact(1);
       CK(cudaMemcpyAsync(dh.data(), gflags, cj * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
       CK(cudaStreamSynchronize(s));
       bool all = true;
@@ -466,6 +523,7 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
     launch(K_REF_CHECK, 0.0, 0.0, [&] {
       refine_check_kernel<<<(unsigned)cj, 256, 0, s>>>(drd, ctx->refine_tol, ctx->max_iters, rt_out, rerr, rdone);
     });
+    compact(0);
     CK(cudaMemcpyAsync(dh.data(), rdone, cj * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     bool all = true;
@@ -482,6 +540,7 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
   CK(cudaStreamSynchronize(s));
   for (size_t j = 0; j < cj; ++j) {
     ih[j] = std::max(ih[j], fin[j].iters);
+    ctx->refine_job_steps += fin[j].steps;
     if (rdh[j].c == 0) {
       if (!adjoint) { th[j] = 0.0; eh[j] = 0.0; }
       continue;
@@ -947,7 +1006,9 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
     } else {
       if constexpr (std::is_same<T, float>::value && std::is_same<TR, float>::value) {
         std::vector<LevelRange> lr;
-        for (const Level& lv : levels) lr.push_back({lv.tiny0, lv.tiny_n, lv.small0, lv.small_n + lv.large_n, lv.max_n});
+        for (const Level& lv : levels)
+          lr.push_back({lv.tiny0, lv.tiny_n, lv.small0, lv.small_n + lv.large_n, lv.max_n,
+                        std::max(lv.max_large_ne, lv.max_small_n)});
         RefineDesc* fwd = refine(ctx, sys, specs, begin, cj, lr, max_root, dtasks, jd, arena, arena_off, rarena,
                                  root_off, launch, th, eh, sh, ih, ctx->rb[0], 0, {});
         if (grad) gradient(ctx, sys, specs, begin, cj, lr, max_root, dtasks, jd, arena, arena_off, rarena, root_off,
@@ -1159,9 +1220,12 @@ int caroli_ctx_create(int device_ordinal, caroli_ctx** out) {
                     (const void*)inv_panel_kernel<double>, (const void*)inv_panel_kernel<float>,
                     (const void*)tiny_front_kernel<double, false>, (const void*)tiny_front_kernel<double, true>,
                     (const void*)tiny_front_kernel<float, false>, (const void*)tiny_front_kernel<float, true>,
-                    (const void*)refine_forward_kernel, (const void*)refine_backward_kernel,
-                    (const void*)refine_forward_rows_kernel, (const void*)refine_backward_rows_kernel,
-                    (const void*)refine_root_kernel}) {
+                    (const void*)sweep_rows_fwd_kernel<1>, (const void*)sweep_rows_fwd_kernel<2>,
+                    (const void*)sweep_rows_fwd_kernel<4>, (const void*)sweep_rows_fwd_kernel<8>,
+                    (const void*)sweep_rows_bwd_kernel<1>, (const void*)sweep_rows_bwd_kernel<2>,
+                    (const void*)sweep_rows_bwd_kernel<4>, (const void*)sweep_rows_bwd_kernel<8>,
+                    (const void*)sweep_root_kernel<1>, (const void*)sweep_root_kernel<2>,
+                    (const void*)sweep_root_kernel<4>, (const void*)sweep_root_kernel<8>}) {
       // Dynamic shared memory up to SMEM_LIMIT, less what the kernel declares statically.
       cudaFuncAttributes fa;
       CK(cudaFuncGetAttributes(&fa, k));
@@ -1361,6 +1425,7 @@ int caroli_transmission_with_grad(caroli_ctx* ctx, int plan_id, int count, const
     ctx->factor_ms = ctx->root_ms = ctx->tail_ms = 0.0;
     ctx->refine_iters = 0;
     ctx->fallbacks = 0;
+    ctx->refine_job_steps = ctx->refine_batch_steps = 0;
     const int nb = (int)sys->plans.size();
     std::vector<JobSpec> specs;
     for (int i = 0; i < count; ++i)
@@ -1477,6 +1542,7 @@ int caroli_solve_batch(caroli_ctx* ctx, int plan_id, int count, const int32_t* s
     std::vector<JobOut> jo;
     ctx->fallbacks = 0;
     ctx->refine_iters = 0;
+    ctx->refine_job_steps = ctx->refine_batch_steps = 0;
     solve_jobs(ctx, sys, specs, (Mode)precision, jo);
     ctx->job_iters.clear();
     ctx->job_perturbed.clear();
@@ -1533,6 +1599,23 @@ int caroli_last_stats(const caroli_ctx* ctx, int64_t* fallbacks, int64_t* max_re
   if (!ctx) return CAROLI_EINVAL;
   if (fallbacks) *fallbacks = ctx->fallbacks;
   if (max_refine_iters) *max_refine_iters = ctx->refine_iters;
+  return CAROLI_OK;
+}
+
+int caroli_last_refine_steps(const caroli_ctx* ctx, int64_t* job_steps, int64_t* batch_steps) {
+  if (!ctx) return CAROLI_EINVAL;
+  if (job_steps) *job_steps = ctx->refine_job_steps;
+  if (batch_steps) *batch_steps = ctx->refine_batch_steps;
+  return CAROLI_OK;
+}
+
+int caroli_set_refine_options(caroli_ctx* ctx, int max_iters, double tol, double inner_tol) {
+  if (!ctx) return CAROLI_EINVAL;
+  if (max_iters < 1 || max_iters > 64 || !(tol > 0.0 && tol < 1.0) || !(inner_tol > 0.0 && inner_tol < 1.0))
+    return fail_with(ctx, CAROLI_EINVAL, "refinement options out of range (1 <= max_iters <= 64, 0 < tol < 1)");
+  ctx->max_iters = max_iters;
+  ctx->refine_tol = tol;
+  ctx->inner_tol = inner_tol;
   return CAROLI_OK;
 }
 

@@ -279,6 +279,23 @@ FrontPlan make_plan(const SystemDesc& d, const BlockTree& t, const std::vector<u
   p.arena_elems = arena;
   p.max_n = std::max<int64_t>(p.max_n, r.n);
   p.vars[nn] = std::move(vars);
+  // Sweep gather rows of every front (the children's hoff are final now).
+  p.srows.resize(p.vidx.size());
+  for (size_t k = 0; k <= nn; ++k) {
+    const FrontDesc& f = p.fronts[k];
+    for (int32_t i = 0; i < f.n; ++i) {
+      SweepRow& g = p.srows[f.var_off + i];
+      g.var = p.vidx[f.var_off + i];
+      g.own = p.own[f.own_off + i] ? g.var : -1;
+      g.h0 = g.h1 = -1;
+      for (int c = 0; c < f.nchild; ++c) {
+        const int32_t a = p.maps[f.map_off[c] + i];
+        if (a < 0) continue;
+        const int32_t h = (int32_t)(p.fronts[f.child[c]].hoff + a);
+        if (c == 0) g.h0 = h; else g.h1 = h;
+      }
+    }
+  }
   p.root = (int32_t)nn;
   p.levels = lvl + 1;
   p.nd = (int32_t)del.size();

@@ -82,6 +82,14 @@ struct BlockTree {
   std::vector<int32_t> left_local, right_local;
 };
 
+// Where a refinement sweep finds row i of a front (one 16-byte load per row): `own` = block-local
+// row of the right-hand side when the variable is the front's own separator variable, else -1;
+// `h0`, `h1` = rows of the children's handed vectors in the update buffer (child hoff + index in
+// the child's handed block), else -1; `var` = block-local row of the variable.
+struct SweepRow {
+  int32_t own, h0, h1, var;
+};
+
 struct FrontPlan {
   std::vector<FrontDesc> fronts;  // tree fronts in post-order, then the root
   std::vector<int32_t> maps;
@@ -89,6 +97,7 @@ struct FrontPlan {
   std::vector<Entry> entries;
   std::vector<std::vector<int64_t>> vars;  // variables of each front (elim then rest)
   std::vector<int32_t> vidx;               // block-local index of each front variable
+  std::vector<SweepRow> srows;             // parallel to vidx
   int64_t sum_ne = 0, sum_nb = 0;          // rows of the forward and update buffers
   int32_t levels = 0;                      // the root runs at level `levels - 1`
   int64_t arena_elems = 0;

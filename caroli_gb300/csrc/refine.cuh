@@ -17,13 +17,12 @@
 
 namespace caroli {
 
-constexpr int RCB = 8;  // right-hand-side columns per CTA in the tree sweeps
-
 struct RefineDesc {
   const FrontDesc* fronts;
   const int32_t* maps;
   const uint8_t* own;
   const int32_t* vidx;
+  const SweepRow* srows;  // per front row: where the sweeps find its right-hand side
   const float2* arena;  // f32 factors
   const float2* root;   // f32 root inverse (m x m)
   const int32_t* csr_ptr;
@@ -59,6 +58,7 @@ struct RefineDesc {
   double* beta; // per column: |r_j|
   int32_t* col_done;  // per column: the inner solve converged (or the column is empty)
   int32_t inner, inner_done;  // Arnoldi steps of the current outer step; all columns converged
+  int32_t steps;              // preconditioner applications (Arnoldi steps) over all outer steps
   double inner_res;            // largest relative residual the last inner solve reached
   // The adjoint solve A^† z = b (gradient): Σ -> Σ^†, the root inverse conjugate-transposed, an
   // explicit right-hand side `rhs` (nblk x c), and convergence on the whole vector.
@@ -85,157 +85,6 @@ __device__ __forceinline__ const double2* sweep_src(const RefineDesc& R, int src
 }
 __device__ __forceinline__ float2* sweep_dst(const RefineDesc& R, int dst) {
   return dst < 0 ? R.d : R.Z + (int64_t)dst * R.nblk * R.c;
-}
-
-__global__ void __launch_bounds__(256) refine_forward_kernel(RefineDesc* __restrict__ rd, const Task* __restrict__ tasks,
-                                                             int src) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const Task tk = tasks[blockIdx.x];
-  const RefineDesc& R = rd[tk.job];
-  if (R.done || (src >= 0 && R.inner_done)) return;
-  const double2* rin = sweep_src(R, src);
-  const int j0 = blockIdx.y * RCB;
-  const int cb = min(RCB, R.c - j0);
-  if (cb <= 0) return;
-  const FrontDesc f = R.fronts[tk.front];
-  const int n = f.n, ne = f.ne, nb = n - ne;
-  float2* z = reinterpret_cast<float2*>(smem_raw);  // n x RCB, row-major
-  float2* ts = z + (size_t)n * RCB;                  // ne x RCB
-  const float2* F = R.arena + f.arena_off;
-  for (int idx = threadIdx.x; idx < n * cb; idx += blockDim.x) {
-    const int p = idx / cb, j = idx % cb;
-    float2 v = make_float2(0.f, 0.f);
-    if (R.own[f.own_off + p]) v = f2(rin[R.vidx[f.var_off + p] + (int64_t)(j0 + j) * R.nblk]);
-    for (int c = 0; c < f.nchild; ++c) {
-      const int a = R.maps[f.map_off[c] + p];
-      if (a >= 0) {
-        const FrontDesc& cf = R.fronts[f.child[c]];
-        float2 h = R.hb[(cf.hoff + a) + (int64_t)(j0 + j) * R.sum_nb];
-        v.x += h.x; v.y += h.y;
-      }
-    }
-    z[p * RCB + j] = v;
-  }
-  __syncthreads();
-  for (int i = threadIdx.x; i < ne; i += blockDim.x) {
-    float2 acc[RCB];
-#pragma unroll
-    for (int j = 0; j < RCB; ++j) acc[j] = make_float2(0.f, 0.f);
-    for (int k = 0; k < ne; ++k) {
-      const float2 a = F[i + (int64_t)k * n];
-#pragma unroll
-      for (int j = 0; j < RCB; ++j) acc[j] = cfma(acc[j], a, z[k * RCB + j]);
-    }
-#pragma unroll
-    for (int j = 0; j < RCB; ++j) {
-      ts[i * RCB + j] = acc[j];
-      if (j < cb) R.tb[(f.toff + i) + (int64_t)(j0 + j) * R.sum_ne] = acc[j];
-    }
-  }
-  __syncthreads();
-  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
-    float2 acc[RCB];
-#pragma unroll
-    for (int j = 0; j < RCB; ++j) acc[j] = z[(ne + i) * RCB + j];
-    for (int k = 0; k < ne; ++k) {
-      const float2 a = F[(ne + i) + (int64_t)k * n];
-#pragma unroll
-      for (int j = 0; j < RCB; ++j) acc[j] = cfma(acc[j], a, z[k * RCB + j]);
-    }
-#pragma unroll
-    for (int j = 0; j < RCB; ++j)
-      if (j < cb) R.hb[(f.hoff + i) + (int64_t)(j0 + j) * R.sum_nb] = acc[j];
-  }
-}
-
-// Root: x = F_root^-1 z on the root's variables. grid (jobs, column chunks).
-__global__ void __launch_bounds__(256) refine_root_kernel(RefineDesc* __restrict__ rd, int src, int dst) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const RefineDesc& R = rd[blockIdx.x];
-  if (R.done || (src >= 0 && R.inner_done)) return;
-  const double2* rin = sweep_src(R, src);
-  float2* dout = sweep_dst(R, dst);
-  const int j0 = blockIdx.y * RCB;
-  const int cb = min(RCB, R.c - j0);
-  if (cb <= 0) return;
-  const FrontDesc f = R.fronts[R.root_front];
-  const int m = f.n;
-  float2* z = reinterpret_cast<float2*>(smem_raw);
-  for (int idx = threadIdx.x; idx < m * cb; idx += blockDim.x) {
-    const int p = idx / cb, j = idx % cb;
-    float2 v = make_float2(0.f, 0.f);
-    if (R.own[f.own_off + p]) v = f2(rin[R.vidx[f.var_off + p] + (int64_t)(j0 + j) * R.nblk]);
-    for (int c = 0; c < f.nchild; ++c) {
-      const int a = R.maps[f.map_off[c] + p];
-      if (a >= 0) {
-        const FrontDesc& cf = R.fronts[f.child[c]];
-        float2 h = R.hb[(cf.hoff + a) + (int64_t)(j0 + j) * R.sum_nb];
-        v.x += h.x; v.y += h.y;
-      }
-    }
-    z[p * RCB + j] = v;
-  }
-  __syncthreads();
-  for (int i = threadIdx.x; i < m; i += blockDim.x) {
-    float2 acc[RCB];
-#pragma unroll
-    for (int j = 0; j < RCB; ++j) acc[j] = make_float2(0.f, 0.f);
-    for (int k = 0; k < m; ++k) {
-      float2 a;
-      if (R.adjoint) {
-        a = R.root[k + (int64_t)i * m];
-        a.y = -a.y;
-      } else {
-        a = R.root[i + (int64_t)k * m];
-      }
-#pragma unroll
-      for (int j = 0; j < RCB; ++j) acc[j] = cfma(acc[j], a, z[k * RCB + j]);
-    }
-    const int row = R.vidx[f.var_off + i];
-#pragma unroll
-    for (int j = 0; j < RCB; ++j)
-      if (j < cb) dout[row + (int64_t)(j0 + j) * R.nblk] = acc[j];
-  }
-}
-
-// Backward sweep of one level (top-down): x_e = t - X x_b.
-__global__ void __launch_bounds__(256) refine_backward_kernel(RefineDesc* __restrict__ rd, const Task* __restrict__ tasks,
-                                                              int src, int dst) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const Task tk = tasks[blockIdx.x];
-  const RefineDesc& R = rd[tk.job];
-  if (R.done || (src >= 0 && R.inner_done)) return;
-  float2* dout = sweep_dst(R, dst);
-  const int j0 = blockIdx.y * RCB;
-  const int cb = min(RCB, R.c - j0);
-  if (cb <= 0) return;
-  const FrontDesc f = R.fronts[tk.front];
-  const int n = f.n, ne = f.ne, nb = n - ne;
-  if (ne == 0) return;
-  float2* xb = reinterpret_cast<float2*>(smem_raw);  // nb x RCB
-  const float2* F = R.arena + f.arena_off;
-  for (int idx = threadIdx.x; idx < nb * cb; idx += blockDim.x) {
-    const int p = idx / cb, j = idx % cb;
-    xb[p * RCB + j] = dout[R.vidx[f.var_off + ne + p] + (int64_t)(j0 + j) * R.nblk];
-  }
-  for (int idx = threadIdx.x; idx < nb * RCB; idx += blockDim.x)
-    if (idx % RCB >= cb) xb[idx] = make_float2(0.f, 0.f);
-  __syncthreads();
-  for (int i = threadIdx.x; i < ne; i += blockDim.x) {
-    float2 acc[RCB];
-#pragma unroll
-    for (int j = 0; j < RCB; ++j)
-      acc[j] = j < cb ? R.tb[(f.toff + i) + (int64_t)(j0 + j) * R.sum_ne] : make_float2(0.f, 0.f);
-    for (int k = 0; k < nb; ++k) {
-      const float2 a = F[i + (int64_t)(ne + k) * n];
-#pragma unroll
-      for (int j = 0; j < RCB; ++j) acc[j] = cfms(acc[j], a, xb[k * RCB + j]);
-    }
-    const int row = R.vidx[f.var_off + i];
-#pragma unroll
-    for (int j = 0; j < RCB; ++j)
-      if (j < cb) dout[row + (int64_t)(j0 + j) * R.nblk] = acc[j];
-  }
 }
 
 // x += d, then the FP64 residual r = B - A x of every row: grid (jobs, row chunks of 256).
@@ -533,6 +382,7 @@ __global__ void gm_inner_check_kernel(RefineDesc* __restrict__ rd, int njobs, in
   if (R.done) { flags[job] = 1; return; }
   if (R.inner_done) { flags[job] = 1; return; }
   R.inner = k + 1;
+  R.steps += 1;
   bool all = true;
   for (int j = 0; j < R.c; ++j) all &= R.col_done[j] != 0;
   if (all || k + 1 >= GM_M) R.inner_done = 1;
@@ -598,138 +448,6 @@ __global__ void gm_residual_kernel(RefineDesc* __restrict__ rd, int njobs) {
     worst = fmax(worst, res);
   }
   R.inner_res = worst;
-}
-
-}  // namespace caroli
-
-namespace caroli {
-
-// Row-split sweeps for fronts above TINY_MAX: a CTA takes 64 rows of one front (blockIdx.y) and
-// four threads per row split the inner dimension; partial sums meet in shared memory. A front of
-// n rows spans ceil(n / 64) CTAs, which keeps the top levels (few, large fronts) busy.
-constexpr int SW_ROWS = 64, SW_SLICES = 4;
-
-// out_r = (r < ne ? 0 : z_r) + sum_{k < ne} F[r, k] z_k : t for r < ne, h for r >= ne.
-__global__ void __launch_bounds__(256) refine_forward_rows_kernel(RefineDesc* __restrict__ rd,
-                                                                  const Task* __restrict__ tasks, int src) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ float2 part[SW_SLICES - 1][SW_ROWS][RCB];
-  const Task tk = tasks[blockIdx.x];
-  const RefineDesc& R = rd[tk.job];
-  if (R.done || (src >= 0 && R.inner_done)) return;
-  const FrontDesc f = R.fronts[tk.front];
-  const int n = f.n, ne = f.ne;
-  const int r0 = blockIdx.y * SW_ROWS;
-  if (r0 >= n) return;
-  const int j0 = blockIdx.z * RCB;
-  const int cb = min(RCB, R.c - j0);
-  if (cb <= 0) return;
-  const double2* rin = sweep_src(R, src);
-  float2* z = reinterpret_cast<float2*>(smem_raw);  // n x RCB
-  for (int idx = threadIdx.x; idx < n * RCB; idx += blockDim.x) {
-    const int p = idx / RCB, j = idx % RCB;
-    float2 v = make_float2(0.f, 0.f);
-    if (j < cb) {
-      if (R.own[f.own_off + p]) v = f2(rin[R.vidx[f.var_off + p] + (int64_t)(j0 + j) * R.nblk]);
-      for (int c = 0; c < f.nchild; ++c) {
-        const int a = R.maps[f.map_off[c] + p];
-        if (a >= 0) {
-          const FrontDesc& cf = R.fronts[f.child[c]];
-          const float2 h = R.hb[(cf.hoff + a) + (int64_t)(j0 + j) * R.sum_nb];
-          v.x += h.x; v.y += h.y;
-        }
-      }
-    }
-    z[idx] = v;
-  }
-  __syncthreads();
-  const int lr = threadIdx.x % SW_ROWS, sl = threadIdx.x / SW_ROWS;
-  const int r = r0 + lr;
-  const float2* F = R.arena + f.arena_off;
-  float2 acc[RCB];
-#pragma unroll
-  for (int j = 0; j < RCB; ++j) acc[j] = make_float2(0.f, 0.f);
-  if (r < n) {
-    const int kper = (ne + SW_SLICES - 1) / SW_SLICES;
-    const int k1 = min(ne, (sl + 1) * kper);
-#pragma unroll 4
-    for (int k = sl * kper; k < k1; ++k) {
-      const float2 a = F[r + (int64_t)k * n];
-#pragma unroll
-      for (int j = 0; j < RCB; ++j) acc[j] = cfma(acc[j], a, z[k * RCB + j]);
-    }
-  }
-  if (sl > 0)
-#pragma unroll
-    for (int j = 0; j < RCB; ++j) part[sl - 1][lr][j] = acc[j];
-  __syncthreads();
-  if (sl == 0 && r < n) {
-#pragma unroll
-    for (int j = 0; j < RCB; ++j) {
-      for (int q = 0; q < SW_SLICES - 1; ++q) { acc[j].x += part[q][lr][j].x; acc[j].y += part[q][lr][j].y; }
-      if (j >= cb) continue;
-      if (r < ne) {
-        R.tb[(f.toff + r) + (int64_t)(j0 + j) * R.sum_ne] = acc[j];
-      } else {
-        const float2 zr = z[r * RCB + j];
-        R.hb[(f.hoff + r - ne) + (int64_t)(j0 + j) * R.sum_nb] = make_float2(acc[j].x + zr.x, acc[j].y + zr.y);
-      }
-    }
-  }
-}
-
-// x_r = t_r - sum_{k < nb} X[r, k] x_b,k for the rows r < ne.
-__global__ void __launch_bounds__(256) refine_backward_rows_kernel(RefineDesc* __restrict__ rd,
-                                                                   const Task* __restrict__ tasks, int src, int dst) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ float2 part[SW_SLICES - 1][SW_ROWS][RCB];
-  const Task tk = tasks[blockIdx.x];
-  const RefineDesc& R = rd[tk.job];
-  if (R.done || (src >= 0 && R.inner_done)) return;
-  const FrontDesc f = R.fronts[tk.front];
-  const int n = f.n, ne = f.ne, nb = n - ne;
-  const int r0 = blockIdx.y * SW_ROWS;
-  if (r0 >= ne) return;
-  const int j0 = blockIdx.z * RCB;
-  const int cb = min(RCB, R.c - j0);
-  if (cb <= 0) return;
-  float2* dout = sweep_dst(R, dst);
-  float2* xb = reinterpret_cast<float2*>(smem_raw);  // nb x RCB
-  for (int idx = threadIdx.x; idx < nb * RCB; idx += blockDim.x) {
-    const int p = idx / RCB, j = idx % RCB;
-    xb[idx] = j < cb ? dout[R.vidx[f.var_off + ne + p] + (int64_t)(j0 + j) * R.nblk] : make_float2(0.f, 0.f);
-  }
-  __syncthreads();
-  const int lr = threadIdx.x % SW_ROWS, sl = threadIdx.x / SW_ROWS;
-  const int r = r0 + lr;
-  const float2* F = R.arena + f.arena_off;
-  float2 acc[RCB];
-#pragma unroll
-  for (int j = 0; j < RCB; ++j) acc[j] = make_float2(0.f, 0.f);
-  if (r < ne) {
-    const int kper = (nb + SW_SLICES - 1) / SW_SLICES;
-    const int k1 = min(nb, (sl + 1) * kper);
-#pragma unroll 4
-    for (int k = sl * kper; k < k1; ++k) {
-      const float2 a = F[r + (int64_t)(ne + k) * n];
-#pragma unroll
-      for (int j = 0; j < RCB; ++j) acc[j] = cfma(acc[j], a, xb[k * RCB + j]);
-    }
-  }
-  if (sl > 0)
-#pragma unroll
-    for (int j = 0; j < RCB; ++j) part[sl - 1][lr][j] = acc[j];
-  __syncthreads();
-  if (sl == 0 && r < ne) {
-    const int row = R.vidx[f.var_off + r];
-#pragma unroll
-    for (int j = 0; j < RCB; ++j) {
-      for (int q = 0; q < SW_SLICES - 1; ++q) { acc[j].x += part[q][lr][j].x; acc[j].y += part[q][lr][j].y; }
-      if (j >= cb) continue;
-      const float2 tv = R.tb[(f.toff + r) + (int64_t)(j0 + j) * R.sum_ne];
-      dout[row + (int64_t)(j0 + j) * R.nblk] = make_float2(tv.x - acc[j].x, tv.y - acc[j].y);
-    }
-  }
 }
 
 }  // namespace caroli

@@ -4,8 +4,7 @@
 // Lane i owns row i of the front; the warp synchronises with __syncwarp only.
 //
 // tiny_front_kernel is small_front_kernel (same assembly, same Gauss-Jordan sweep and pivot test,
-// same factor layout [F11^-1 X; W S]); tiny_forward/backward_kernel are the refinement sweeps of
-// refine.cuh for these fronts.
+// same factor layout [F11^-1 X; W S]).
 #pragma once
 #include "kernels.cuh"
 #include "refine.cuh"
@@ -117,109 +116,6 @@ __global__ void __launch_bounds__(256) tiny_front_kernel(const JobDesc* __restri
       if (ne > 0 && !KEEP && (lane < ne || j < ne)) continue;
       out[lane + (int64_t)j * n] = F[lane + j * LD];
     }
-}
-
-// Forward sweep for tiny fronts: t = F11^-1 z_e, h = z_b + W z_e.
-__global__ void __launch_bounds__(256) tiny_forward_kernel(RefineDesc* __restrict__ rd, const Task* __restrict__ tasks,
-                                                           int ntasks, int src) {
-  __shared__ float2 Zs[TINY_WARPS][TINY_MAX * RCB];
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int ti = blockIdx.x * TINY_WARPS + w;
-  if (ti >= ntasks) return;
-  const Task tk = tasks[ti];
-  const RefineDesc& R = rd[tk.job];
-  if (R.done || (src >= 0 && R.inner_done)) return;
-  const double2* rin = sweep_src(R, src);
-  const FrontDesc f = R.fronts[tk.front];
-  const int n = f.n, ne = f.ne, nb = n - ne;
-  const float2* F = R.arena + f.arena_off;
-  float2* z = Zs[w];
-  for (int j0 = 0; j0 < R.c; j0 += RCB) {
-    const int cb = min(RCB, R.c - j0);
-    if (lane < n) {
-      const bool own = R.own[f.own_off + lane];
-      const int row = R.vidx[f.var_off + lane];
-      int ca[2] = {-1, -1};
-      for (int c = 0; c < f.nchild; ++c) ca[c] = R.maps[f.map_off[c] + lane];
-      for (int j = 0; j < RCB; ++j) {
-        float2 v = make_float2(0.f, 0.f);
-        if (j < cb) {
-          if (own) v = f2(rin[row + (int64_t)(j0 + j) * R.nblk]);
-          for (int c = 0; c < f.nchild; ++c)
-            if (ca[c] >= 0) {
-              const FrontDesc& cf = R.fronts[f.child[c]];
-              const float2 h = R.hb[(cf.hoff + ca[c]) + (int64_t)(j0 + j) * R.sum_nb];
-              v.x += h.x; v.y += h.y;
-            }
-        }
-        z[lane * RCB + j] = v;
-      }
-    }
-    __syncwarp();
-    if (lane < n) {
-      float2 acc[RCB];
-      const bool top = lane < ne;
-#pragma unroll
-      for (int j = 0; j < RCB; ++j) acc[j] = top ? make_float2(0.f, 0.f) : z[lane * RCB + j];
-      // Row `lane` of [F11^-1; W] times z_e.
-      for (int k = 0; k < ne; ++k) {
-        const float2 a = F[lane + (int64_t)k * n];
-#pragma unroll
-        for (int j = 0; j < RCB; ++j) acc[j] = cfma(acc[j], a, z[k * RCB + j]);
-      }
-#pragma unroll
-      for (int j = 0; j < RCB; ++j) {
-        if (j >= cb) continue;
-        if (top) R.tb[(f.toff + lane) + (int64_t)(j0 + j) * R.sum_ne] = acc[j];
-        else R.hb[(f.hoff + lane - ne) + (int64_t)(j0 + j) * R.sum_nb] = acc[j];
-      }
-    }
-    __syncwarp();
-  }
-  (void)nb;
-}
-
-// Backward sweep for tiny fronts: x_e = t - X x_b.
-__global__ void __launch_bounds__(256) tiny_backward_kernel(RefineDesc* __restrict__ rd, const Task* __restrict__ tasks,
-                                                            int ntasks, int src, int dst) {
-  __shared__ float2 Xs[TINY_WARPS][TINY_MAX * RCB];
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int ti = blockIdx.x * TINY_WARPS + w;
-  if (ti >= ntasks) return;
-  const Task tk = tasks[ti];
-  const RefineDesc& R = rd[tk.job];
-  if (R.done || (src >= 0 && R.inner_done)) return;
-  float2* dout = sweep_dst(R, dst);
-  const FrontDesc f = R.fronts[tk.front];
-  const int n = f.n, ne = f.ne, nb = n - ne;
-  if (ne == 0) return;
-  const float2* F = R.arena + f.arena_off;
-  float2* xb = Xs[w];
-  for (int j0 = 0; j0 < R.c; j0 += RCB) {
-    const int cb = min(RCB, R.c - j0);
-    if (lane < nb) {
-      const int row = R.vidx[f.var_off + ne + lane];
-      for (int j = 0; j < RCB; ++j)
-        xb[lane * RCB + j] = j < cb ? dout[row + (int64_t)(j0 + j) * R.nblk] : make_float2(0.f, 0.f);
-    }
-    __syncwarp();
-    if (lane < ne) {
-      float2 acc[RCB];
-#pragma unroll
-      for (int j = 0; j < RCB; ++j)
-        acc[j] = j < cb ? R.tb[(f.toff + lane) + (int64_t)(j0 + j) * R.sum_ne] : make_float2(0.f, 0.f);
-      for (int k = 0; k < nb; ++k) {
-        const float2 a = F[lane + (int64_t)(ne + k) * n];
-#pragma unroll
-        for (int j = 0; j < RCB; ++j) acc[j] = cfms(acc[j], a, xb[k * RCB + j]);
-      }
-      const int row = R.vidx[f.var_off + lane];
-#pragma unroll
-      for (int j = 0; j < RCB; ++j)
-        if (j < cb) dout[row + (int64_t)(j0 + j) * R.nblk] = acc[j];
-    }
-    __syncwarp();
-  }
 }
 
 }  // namespace caroli

@@ -164,6 +164,18 @@ int caroli_last_stats(const caroli_ctx* ctx, int64_t* fallbacks, int64_t* max_re
 int caroli_last_job_info(const caroli_ctx* ctx, int64_t capacity, int32_t* iters, int32_t* perturbed,
                          int32_t* status, int64_t* count);
 
+/* Of the last caroli_solve_batch in CAROLI_MIXED: preconditioner applications (GMRES steps, one
+ * forward and backward sweep each) summed over the block solves, and the steps the batch launched
+ * (a step runs while any solve of the batch still iterates). No reference counterpart: the
+ * reference has no iterative refinement. */
+int caroli_last_refine_steps(const caroli_ctx* ctx, int64_t* job_steps, int64_t* batch_steps);
+
+/* Refinement controls of CAROLI_MIXED (defaults 6, 1e-10, 1e-10): at most max_iters outer steps
+ * (FP64 residual, GMRES on the f32 factors), done when the estimated relative error of the left
+ * slice of the solution is at most tol; each GMRES runs until its residual falls by inner_tol.
+ * No reference counterpart (precision::PrecisionOptions covers only the double recomputation). */
+int caroli_set_refine_options(caroli_ctx* ctx, int max_iters, double tol, double inner_tol);
+
 /* Device time of the last caroli_solve_batch split into the tree factorization, the root
  * inverse, and the rest (trace, or refinement and double-precision recomputations), in ms. */
 int caroli_last_phases(const caroli_ctx* ctx, double* factor_ms, double* root_ms, double* tail_ms);
