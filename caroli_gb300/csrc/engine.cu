@@ -197,7 +197,10 @@ struct GradRequest {
 struct TaskLevel {
   size_t tiny0 = 0, tiny_n = 0;
   size_t small0 = 0, small_n = 0, large0 = 0, large_n = 0;
-  int max_small_n = 0, max_large_n = 0, max_large_ne = 0, max_n = 0;
+  int max_small_n = 0, max_small_ne = 0, max_large_n = 0, max_large_ne = 0, max_n = 0;
+  // Small fronts in size buckets (one launch each, shared memory sized to the bucket).
+  size_t sb0[3] = {0, 0, 0}, sbn[3] = {0, 0, 0};
+  int sb_n[3] = {0, 0, 0}, sb_ne[3] = {0, 0, 0};
   size_t xs_elems = 0, inv0 = 0;
   double small_flops = 0, small_bytes = 0, inv_flops = 0, gemm0_flops = 0, gemm1_flops = 0, asm_bytes = 0;
 };
@@ -271,10 +274,6 @@ template <typename T> struct Prec {
   static constexpr double tol = sizeof(T) == 8 ? PIVOT_TOL_F64 : PIVOT_TOL_F32;
 };
 
-size_t small_smem(int n, size_t vbytes) {
-  int ld = n | 1;
-  return (size_t)ld * n * vbytes + 2 * (size_t)n * vbytes + 32 * 8 + 2 * (size_t)n * 4 + 16;
-}
 // Shared memory of a panel launch whose largest pivot count is pmax: the staged candidate rows
 // when they fit under SMEM_LIMIT, else only the work vectors (the kernel then sweeps the panel in
 // global memory); 0 when not even those fit.
@@ -801,16 +800,27 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
       }
       lv.tiny_n = tasks.size() - lv.tiny0;
       lv.small0 = tasks.size();
-      for (size_t j = 0; j < cj; ++j) {
-        const auto& fr = specs[begin + j].plan->host.fronts;
-        for (size_t k = 0; k + 1 < fr.size(); ++k)
-          if (fr[k].level == L && fr[k].n > TINY_MAX && fr[k].n <= small_max) {
-            tasks.push_back({(int32_t)j, (int32_t)k, 0});
-            const double ne = fr[k].ne, nb = fr[k].n - fr[k].ne;
-            lv.max_small_n = std::max(lv.max_small_n, fr[k].n);
-            lv.small_flops += 8.0 / 3 * ne * ne * ne + 8 * ne * ne * nb + 8 * nb * nb * ne;
-            lv.small_bytes += ((double)fr[k].n * fr[k].n * (mixed ? 1.0 : nb * nb / std::max(1.0, (double)fr[k].n * fr[k].n))) * vb;
-          }
+      const int bucket_hi[3] = {48, 64, small_max};
+      for (int b = 0; b < 3; ++b) {
+        const int lo = b == 0 ? TINY_MAX : bucket_hi[b - 1], hi = bucket_hi[b];
+        lv.sb0[b] = tasks.size();
+        for (size_t j = 0; j < cj; ++j) {
+          const auto& fr = specs[begin + j].plan->host.fronts;
+          for (size_t k = 0; k + 1 < fr.size(); ++k)
+            if (fr[k].level == L && fr[k].n > lo && fr[k].n <= hi) {
+              tasks.push_back({(int32_t)j, (int32_t)k, 0});
+              const double ne = fr[k].ne, nb = fr[k].n - fr[k].ne;
+              lv.max_small_n = std::max(lv.max_small_n, fr[k].n);
+              lv.max_small_ne = std::max(lv.max_small_ne, fr[k].ne);
+              lv.sb_n[b] = std::max(lv.sb_n[b], fr[k].n);
+              lv.sb_ne[b] = std::max(lv.sb_ne[b], fr[k].ne);
+              lv.small_flops += 8.0 / 3 * ne * ne * ne + 8 * ne * ne * nb + 8 * nb * nb * ne;
+              lv.small_bytes +=
+                  ((double)fr[k].n * fr[k].n * (mixed ? 1.0 : nb * nb / std::max(1.0, (double)fr[k].n * fr[k].n))) * vb;
+            }
+        }
+        lv.sbn[b] = tasks.size() - lv.sb0[b];
+        if (hi >= small_max) break;
       }
       lv.small_n = tasks.size() - lv.small0;
       lv.large0 = tasks.size();
@@ -951,15 +961,17 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
                                                                             Prec<T>::tol, perturb, pert);
         });
       }
-      if (lv.small_n) {
-        const size_t sm = small_smem(lv.max_small_n, vb);
-        launch(K_SMALL, lv.small_flops, lv.small_bytes, [&] {
+      for (int b = 0; b < 3; ++b) {
+        if (!lv.sbn[b]) continue;
+        const size_t sm = small_smem_bytes(lv.sb_n[b], lv.sb_ne[b], vb);
+        const unsigned nblk = (unsigned)lv.sbn[b];
+        const Task* st = dtasks + lv.sb0[b];
+        const double share = (double)lv.sbn[b] / (double)lv.small_n;
+        launch(K_SMALL, lv.small_flops * share, lv.small_bytes * share, [&] {
           if (mixed)
-            small_front_kernel<T, true><<<(unsigned)lv.small_n, 256, sm, s>>>(djobs, dtasks + lv.small0, Prec<T>::tol,
-                                                                              perturb, pert);
+            small_front_kernel<T, true><<<nblk, 256, sm, s>>>(djobs, st, Prec<T>::tol, perturb, pert);
           else
-            small_front_kernel<T, false><<<(unsigned)lv.small_n, 256, sm, s>>>(djobs, dtasks + lv.small0,
-                                                                               Prec<T>::tol, perturb, pert);
+            small_front_kernel<T, false><<<nblk, 256, sm, s>>>(djobs, st, Prec<T>::tol, perturb, pert);
         });
       }
       if (lv.large_n) {
@@ -1871,7 +1883,7 @@ extern "C" int caroli_solve_batch_noalloc(caroli_ctx* ctx, int plan_id, int coun
     for (int L = 0; L < max_levels; ++L) {
       const Lv& v = lv[L];
       if (v.sn)
-        small_front_kernel<double, false><<<(unsigned)v.sn, 256, small_smem(v.smax, vb), s>>>(djobs, dtasks + v.s0,
+        small_front_kernel<double, false><<<(unsigned)v.sn, 256, small_smem_bytes(v.smax, v.smax, vb), s>>>(djobs, dtasks + v.s0,
                                                                                               PIVOT_TOL_F64, 0, nullptr);
       if (v.ln) {
         in_pieces(v.ln, [&](size_t f0, size_t c) {

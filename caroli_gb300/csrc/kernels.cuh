@@ -147,34 +147,51 @@ __device__ __forceinline__ int block_argmax(double v, int i, double* redv, int* 
 }
 
 // ---- assembly -----------------------------------------------------------------------------------
-// Element (i, j) of a front before its H entries: the children's handed blocks through their
-// index maps, plus z on the diagonal of the own separator, minus Σ on the root.
-template <typename TC, typename T = TC>
-__device__ __forceinline__ typename Cx<T>::V gather(const JobDesc& J, const FrontDesc& f, int i, int j,
-                                                     bool is_root) {
-  using V = typename Cx<T>::V;
-  using VC = typename Cx<TC>::V;
-  const VC* arena = static_cast<const VC*>(J.arena);
-  V v = cx<V>(0.0, 0.0);
-  for (int c = 0; c < f.nchild; ++c) {
-    const int32_t* map = J.maps + f.map_off[c];
-    int a = map[i], b = map[j];
-    if (a >= 0 && b >= 0) {
-      const FrontDesc& cf = J.fronts[f.child[c]];
-      VC w = arena[cf.arena_off + f.child_off[c] + a + (int64_t)b * cf.n];
-      v.x += (T)w.x;
-      v.y += (T)w.y;
+// Assembly: element (i, j) of a front before its H entries is the children's handed blocks through
+// their index maps, plus z on the diagonal of the own separator, minus Σ on the root.
+// The children's handed blocks of a front, hoisted out of the per-element assembly loops:
+// element (i, j) = Σ_c S_c[map_c(i), map_c(j)] (both mapped), S_c a column-major block with
+// leading dimension ld[c].
+template <typename TC>
+struct ChildBlocks {
+  const typename Cx<TC>::V* base[2];
+  const int32_t* map[2];
+  int32_t ld[2];
+  int nchild;
+  __device__ __forceinline__ ChildBlocks(const JobDesc& J, const FrontDesc& f) {
+    nchild = f.nchild;
+    const typename Cx<TC>::V* arena = static_cast<const typename Cx<TC>::V*>(J.arena);
+    for (int c = 0; c < 2; ++c) {
+      if (c < nchild) {
+        const FrontDesc& cf = J.fronts[f.child[c]];
+        base[c] = arena + cf.arena_off + f.child_off[c];
+        ld[c] = cf.n;
+        map[c] = J.maps + f.map_off[c];
+      } else {
+        base[c] = nullptr;
+        ld[c] = 0;
+        map[c] = nullptr;
+      }
     }
   }
-  if (i == j && J.own[f.own_off + i]) v.x += (T)J.energy;
-  if (is_root) {
-    int li = i - J.nd, lj = j - J.nd;
-    if (li >= 0 && li < J.nl && lj >= 0 && lj < J.nl) v = csub(v, from64<V>(J.sigma_l[li + (int64_t)lj * J.nl]));
-    li -= J.rpos; lj -= J.rpos;
-    if (li >= 0 && li < J.nr && lj >= 0 && lj < J.nr) v = csub(v, from64<V>(J.sigma_r[li + (int64_t)lj * J.nr]));
+  // Row maps of row i (or column maps of column j): -1 where the child has no such variable.
+  __device__ __forceinline__ void index(int i, int (&a)[2]) const {
+    a[0] = nchild > 0 ? map[0][i] : -1;
+    a[1] = nchild > 1 ? map[1][i] : -1;
   }
-  return v;
-}
+  template <typename T>
+  __device__ __forceinline__ typename Cx<T>::V at(const int (&a)[2], const int (&b)[2]) const {
+    typename Cx<T>::V v = cx<typename Cx<T>::V>(0.0, 0.0);
+#pragma unroll
+    for (int c = 0; c < 2; ++c)
+      if (a[c] >= 0 && b[c] >= 0) {
+        const auto w = base[c][a[c] + (int64_t)b[c] * ld[c]];
+        v.x += (T)w.x;
+        v.y += (T)w.y;
+      }
+    return v;
+  }
+};
 
 template <typename T>
 __device__ __forceinline__ void apply_entries(const JobDesc& J, const FrontDesc& f, typename Cx<T>::V* F, int ld,
@@ -293,8 +310,91 @@ __device__ __forceinline__ void column_order(const int* piv, int npiv, int* cper
   }
 }
 
+// Gauss-Jordan sweep of the leading rows x cols block of F (the pivot candidates of a small front)
+// by the first ceil(cols / 32) warps, a lane per column, synchronised by named barrier 1: same
+// pivots, operations and results as gj_sweep(F, ld, rows, cols, rows, rows, ...). The pivot of
+// step k is the largest |F[i, k]| over i in [k, rows), row k receives the pivot row and row p the
+// old row k, and the scaled pivot row of every step goes to prows (rows x cols). Column k is read
+// from the double buffer cb (2 x rows; cb[0:rows] must hold column 0), which the owner of column
+// k + 1 fills while it updates it. The calling warps must be exactly the first ceil(cols / 32).
+template <typename T>
+__device__ bool gj_sweep_cols(typename Cx<T>::V* F, int ld, int rows, int cols, double scale2, double tol,
+                              typename Cx<T>::V* cb, int* piv, bool perturb, int* perturbed,
+                              typename Cx<T>::V* prows) {
+  using V = typename Cx<T>::V;
+  const int lane = threadIdx.x & 31;
+  const int j = threadIdx.x;  // this lane's column
+  const int nthreads = ((cols + 31) / 32) * 32;
+  const double thresh = tol * tol * scale2;
+  V* Fj = F + (int64_t)j * ld;
+  for (int k = 0; k < rows; ++k) {
+    const V* ck = cb + (k & 1) * rows;
+    V* cn = cb + ((k + 1) & 1) * rows;
+    T best = -1;
+    int p = 0x7fffffff;
+    for (int i = k + lane; i < rows; i += 32) {
+      const T m = cnorm(ck[i]);
+      if (m > best) { best = m; p = i; }
+    }
+    warp_argmax(best, p);
+    const double big = (double)best;
+    V d;
+    if (!(big > thresh) || p >= rows) {
+      if (!perturb || !(big >= 0.0) || !(scale2 > 0.0) || p >= rows) return false;
+      d = ck[p];
+      const double mag = sqrt(big), target = tol * sqrt(scale2);
+      if (mag > 0.0) { d.x = (T)(d.x / mag * target); d.y = (T)(d.y / mag * target); }
+      else { d.x = (T)target; d.y = (T)0; }
+      if (threadIdx.x == 0 && perturbed) atomicAdd(perturbed, 1);
+    } else {
+      d = ck[p];
+    }
+    if (threadIdx.x == 0) piv[k] = p;
+    const V inv = cinv(d);
+    const V ckk = ck[k];
+    if (j < cols) {
+      if (j == k) {
+        prows[k * cols + j] = inv;
+        for (int i = 0; i < rows; ++i) {
+          const V c = (i == p) ? ckk : ck[i];
+          Fj[i] = (i == k) ? inv : cmul(cx<V>(-c.x, -c.y), inv);
+        }
+      } else {
+        const V pr = cmul(Fj[p], inv);
+        const V rk = Fj[k];
+        prows[k * cols + j] = pr;
+        const bool fill = j == k + 1;
+        for (int i = 0; i < rows; ++i) {
+          V nv;
+          if (i == k) {
+            nv = pr;
+          } else {
+            const V c = (i == p) ? ckk : ck[i];
+            nv = cfms((i == p) ? rk : Fj[i], c, pr);
+          }
+          Fj[i] = nv;
+          if (fill) cn[i] = nv;
+        }
+      }
+    }
+    asm volatile("bar.sync 1, %0;" ::"r"(nthreads) : "memory");
+  }
+  return true;
+}
+
 // ---- small fronts: assembly and elimination in shared memory, one CTA per front ---------------
-// Shared memory: the front (n x (n | 1)), the column buffer (2n), 32 doubles, piv and cperm (n).
+// The Gauss-Jordan sweep runs in two phases. The ne separator rows (the pivot candidates) are
+// swept with the block's barriers, recording the scaled pivot row of every step (prows). The
+// nb boundary rows never pivot and never interchange, so each of them then replays the ne steps
+// on its own from prows, a warp per row, without barriers: the same operations in the same order
+// as a sweep of the whole front.
+// Shared memory: the front (n x (n | 1)), prows (ne x n), the column buffer (2n), 32 doubles,
+// piv and cperm (n).
+__host__ __device__ inline size_t small_smem_bytes(int n, int ne, size_t vbytes) {
+  const int ld = n | 1;
+  return ((size_t)ld * n + (size_t)ne * n + 2 * (size_t)n) * vbytes + 32 * 8 + 2 * (size_t)n * 4 + 16;
+}
+
 template <typename T, bool KEEP>
 __global__ void __launch_bounds__(256) small_front_kernel(const JobDesc* __restrict__ jobs,
                                                           const Task* __restrict__ tasks, double tol, int perturb,
@@ -308,12 +408,26 @@ __global__ void __launch_bounds__(256) small_front_kernel(const JobDesc* __restr
   const int ld = n | 1;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
   V* F = reinterpret_cast<V*>(smem_raw);
-  V* cb = F + (int64_t)ld * n;
+  V* prows = F + (int64_t)ld * n;
+  V* cb = prows + (int64_t)ne * n;
   double* red = reinterpret_cast<double*>(cb + 2 * n);
   int* piv = reinterpret_cast<int*>(red + 32);
   int* cperm = piv + n;
-  for (int j = w; j < n; j += nw)
-    for (int i = lane; i < n; i += 32) F[i + j * ld] = gather<T>(J, f, i, j, false);
+  {
+    const ChildBlocks<T> kids(J, f);
+    for (int j = w; j < n; j += nw) {
+      int bj[2];
+      kids.index(j, bj);
+      for (int i = lane; i < n; i += 32) {
+        int ai[2];
+        kids.index(i, ai);
+        F[i + j * ld] = kids.template at<T>(ai, bj);
+      }
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x)
+    if (J.own[f.own_off + i]) F[i + i * ld].x += (T)J.energy;
   __syncthreads();
   apply_entries<T>(J, f, F, ld, 0, n);
   __syncthreads();
@@ -327,15 +441,50 @@ __global__ void __launch_bounds__(256) small_front_kernel(const JobDesc* __restr
   for (int j = w; j < ne; j += nw)
     for (int i = lane; i < ne; i += 32) local = fmax(local, cnorm(F[i + j * ld]));
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    cb[i] = F[i];
+    if (i < ne) cb[i] = F[i];
     cperm[i] = i;
   }
   const double scale2 = block_max((double)local, red);  // also publishes cb
-  const bool ok = gj_sweep<T>(F, ld, n, n, ne, ne, scale2, tol, cb, piv, perturb != 0,
-                              perturbed ? perturbed + t.job : nullptr);
+  // Pivot rows: a lane per column in the first ceil(n / 32) warps (named barrier per pivot); the
+  // other warps wait at the block barrier.
+  __shared__ int ok_flag;
+  if (w < (n + 31) / 32) {
+    const bool okc = gj_sweep_cols<T>(F, ld, ne, n, scale2, tol, cb, piv, perturb != 0,
+                                      perturbed ? perturbed + t.job : nullptr, prows);
+    if (threadIdx.x == 0) ok_flag = okc ? 1 : 0;
+  }
+  __syncthreads();
+  const bool ok = ok_flag != 0;
   if (!ok) {
     if (threadIdx.x == 0) J.fail[t.front] = 1;
     return;
+  }
+  // Boundary rows: the recorded steps replayed, a warp per row (columns lane, lane + 32, lane + 64).
+  constexpr int RQ = 3;
+  for (int i = ne + w; i < n; i += nw) {
+    V r[RQ];
+#pragma unroll
+    for (int q = 0; q < RQ; ++q) {
+      const int col = lane + 32 * q;
+      r[q] = col < n ? F[i + col * ld] : cx<V>(0.0, 0.0);
+    }
+    for (int k = 0; k < ne; ++k) {
+      const int qk = k >> 5;
+      const V src = qk == 0 ? r[0] : (qk == 1 ? r[1] : r[2]);
+      const V a = cx<V>(__shfl_sync(0xffffffffu, src.x, k & 31), __shfl_sync(0xffffffffu, src.y, k & 31));
+      const V* pk = prows + (int64_t)k * n;
+#pragma unroll
+      for (int q = 0; q < RQ; ++q) {
+        const int col = lane + 32 * q;
+        if (col >= n) continue;
+        r[q] = (col == k) ? cmul(cx<V>(-a.x, -a.y), pk[col]) : cfms(r[q], a, pk[col]);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < RQ; ++q) {
+      const int col = lane + 32 * q;
+      if (col < n) F[i + col * ld] = r[q];
+    }
   }
   if (threadIdx.x == 0) column_order(piv, ne, cperm);
   __syncthreads();
@@ -363,8 +512,25 @@ __global__ void __launch_bounds__(256) assemble_kernel(const JobDesc* __restrict
   if (c0 >= n) return;
   const int c1 = min(n, c0 + 32);
   V* F = is_root ? static_cast<V*>(J.root_arena) : static_cast<V*>(J.arena) + f.arena_off;
-  for (int j = c0 + (threadIdx.x >> 5); j < c1; j += blockDim.x >> 5)
-    for (int i = threadIdx.x & 31; i < n; i += 32) F[i + (int64_t)j * n] = gather<TC, T>(J, f, i, j, is_root != 0);
+  const ChildBlocks<TC> kids(J, f);
+  for (int j = c0 + (threadIdx.x >> 5); j < c1; j += blockDim.x >> 5) {
+    int bj[2];
+    kids.index(j, bj);
+    for (int i = threadIdx.x & 31; i < n; i += 32) {
+      int ai[2];
+      kids.index(i, ai);
+      V v = kids.template at<T>(ai, bj);
+      if (i == j && J.own[f.own_off + i]) v.x += (T)J.energy;
+      if (is_root) {
+        int li = i - J.nd, lj = j - J.nd;
+        if (li >= 0 && li < J.nl && lj >= 0 && lj < J.nl) v = csub(v, from64<V>(J.sigma_l[li + (int64_t)lj * J.nl]));
+        li -= J.rpos;
+        lj -= J.rpos;
+        if (li >= 0 && li < J.nr && lj >= 0 && lj < J.nr) v = csub(v, from64<V>(J.sigma_r[li + (int64_t)lj * J.nr]));
+      }
+      F[i + (int64_t)j * n] = v;
+    }
+  }
   __syncthreads();
   apply_entries<T>(J, f, F, n, c0, c1);
 }

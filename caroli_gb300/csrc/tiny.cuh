@@ -30,13 +30,24 @@ __global__ void __launch_bounds__(256) tiny_front_kernel(const JobDesc* __restri
   if (ti >= ntasks) return;
   const Task t = tasks[ti];
   const JobDesc& J = jobs[t.job];
-  const FrontDesc f = J.fronts[t.front];
+  const FrontDesc& f = J.fronts[t.front];
   const int n = f.n, ne = f.ne;
   V* F = reinterpret_cast<V*>(smem_raw) + (size_t)w * (TINY_MAX * LD + TINY_MAX);
   V* prow = F + TINY_MAX * LD;
   // Assembly: lane i builds row i.
-  if (lane < n)
-    for (int j = 0; j < n; ++j) F[lane + j * LD] = gather<T>(J, f, lane, j, false);
+  {
+    const ChildBlocks<T> kids(J, f);
+    int ai[2];
+    kids.index(lane < n ? lane : 0, ai);
+    if (lane < n)
+      for (int j = 0; j < n; ++j) {
+        int bj[2];
+        kids.index(j, bj);
+        V v = kids.template at<T>(ai, bj);
+        if (j == lane && J.own[f.own_off + lane]) v.x += (T)J.energy;
+        F[lane + j * LD] = v;
+      }
+  }
   __syncwarp();
   for (int64_t e = lane; e < f.ent_cnt; e += 32) {
     const Entry en = J.entries[f.ent_off + e];
