@@ -43,6 +43,7 @@ SIGNATURES = {
     "caroli_last_job_info": (ctypes.c_int, [P, I64, P, P, P, P]),
     "caroli_last_refine_steps": (ctypes.c_int, [P, P, P]),
     "caroli_set_refine_options": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_double, ctypes.c_double]),
+    "caroli_set_tensor_cores": (ctypes.c_int, [P, ctypes.c_int]),
     "caroli_kernel_class_name": (ctypes.c_char_p, [ctypes.c_int]),
     "caroli_probe_kernel": (ctypes.c_int, [P, ctypes.c_int]),
     "caroli_kernel_stats": (ctypes.c_int, [P, ctypes.c_int, P, P, P, P, ctypes.c_int]),
@@ -104,6 +105,10 @@ class Context:
     def set_refine_options(self, max_iters=6, tol=1e-10, inner_tol=1e-10):
         """Mixed-precision refinement controls (``caroli_set_refine_options``)."""
         self.check(self.lib.caroli_set_refine_options(self.h, int(max_iters), float(tol), float(inner_tol)))
+
+    def set_tensor_cores(self, enable=True):
+        """f32 rank-32 updates on the tcgen05 tensor cores (True) or the CUDA cores."""
+        self.check(self.lib.caroli_set_tensor_cores(self.h, 1 if enable else 0))
 
     def kernel_classes(self):
         return [self.lib.caroli_kernel_class_name(k).decode() for k in range(self.lib.caroli_kernel_classes())]

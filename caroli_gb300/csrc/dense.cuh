@@ -17,6 +17,7 @@
 // caroli-dense/src/field.rs:79-105 applies unchanged.
 #pragma once
 #include "kernels.cuh"
+#include "tc.cuh"
 
 namespace caroli {
 
@@ -30,11 +31,23 @@ struct InvTask {
   int32_t npiv;     // pivots: the leading npiv rows and columns
   int32_t* piv;     // n entries
   void* y;          // kb x n scratch (pivot rows of the rest columns)
+  void* bt;         // f32 matrices: the same rows as the tensor-core operand B' (see tc_update_kernel)
   double* scale2;   // max |a_ij|^2 of the input
   int32_t* bad;     // set when a pivot is refused
 };
 
 constexpr int GJ_KB = 32;
+
+// Tensor-core update tiles: 64 complex rows (M = 128 real rows) by 64 columns, K = 2 kb <= 64.
+constexpr int TCU_ROWS = 64;
+constexpr int TCU_COLS = 64;
+constexpr int TCU_A_BYTES = 2 * TCU_ROWS * 2 * GJ_KB * 4;  // one of A' hi / lo: M x K f32
+constexpr int TCU_B_BYTES = TCU_COLS * 2 * GJ_KB * 4;      // one of B' hi / lo: N x K f32
+// B' of a matrix of n columns in global memory: per column tile of the rest columns, hi then lo,
+// each in the shared-memory operand layout (copied by one bulk copy).
+__host__ __device__ inline size_t tc_operand_bytes(int n) {
+  return (size_t)((n + TCU_COLS - 1) / TCU_COLS) * 2 * TCU_B_BYTES;
+}
 
 template <typename T>
 __global__ void __launch_bounds__(256) inv_scale_kernel(const InvTask* __restrict__ tasks) {
@@ -179,6 +192,18 @@ __global__ void __launch_bounds__(256) inv_panel_kernel(const InvTask* __restric
     __syncwarp();
     if (lane < kb) Y[lane + (int64_t)j * kb] = yv;
     if (lane < nd) Aj[k0 + disp[lane]] = dv;
+    if (t.bt) {
+      // The same row as B' of the tensor-core update: rest column r, K = 2 c (re), 2 c + 1 (im),
+      // tf32 hi and lo; zero past kb.
+      const int r = j < k0 ? j : j - kb;
+      unsigned char* tile = static_cast<unsigned char*>(t.bt) + (size_t)(r / TCU_COLS) * 2 * TCU_B_BYTES;
+      const uint32_t off = tc::kmajor_offset(r % TCU_COLS, 2 * lane, TCU_COLS);
+      const float2 y = lane < kb ? make_float2((float)yv.x, (float)yv.y) : make_float2(0.f, 0.f);
+      const float2 hi = make_float2(tc::to_tf32(y.x), tc::to_tf32(y.y));
+      *reinterpret_cast<float2*>(tile + off) = hi;
+      *reinterpret_cast<float2*>(tile + TCU_B_BYTES + off) =
+          make_float2(tc::to_tf32(y.x - hi.x), tc::to_tf32(y.y - hi.y));
+    }
   }
 }
 
@@ -242,6 +267,173 @@ __global__ void __launch_bounds__(256) inv_update_kernel(const InvTask* __restri
     }
 }
 
+// Rank-kb update of the rest columns on the tensor cores (f32 data, 3xTF32): the product of
+// inv_update_kernel written as a real GEMM. With P (the swept panel, n x kb) and Y (the pivot rows
+// of the rest columns, kb x rest) complex, the interleaved output rows (re, im) of 64 complex rows
+// are the 128 rows of
+//     D = A' B'^T,  A'[2i][2c] = Re P, A'[2i][2c+1] = -Im P, A'[2i+1][2c] = Im P, A'[2i+1][2c+1] = Re P,
+//                   B'[j][2c] = Re Y[c, j], B'[j][2c+1] = Im Y[c, j],
+// K = 2 kb. Both operands are split into tf32 hi + lo parts and D = lo hi + hi lo + hi hi
+// accumulates in f32 in tensor memory (24 MMAs of 128 x 64 x 8 per 64-column tile), about the
+// accuracy of an f32 product.
+//
+// A CTA takes 64 complex rows of one matrix: all warps stage A' from the panel columns, then
+//   warp 0 (one thread) bulk-copies the B' tiles, written by the panel kernel, into shared memory;
+//   warp 1 (one thread) issues the MMAs, alternating two 64-column accumulators in tensor memory;
+//   warps 2-5 (one per 32-lane quarter of tensor memory) add each finished tile to the old values
+//   (zero on the pivot rows) while the next tile is copied and multiplied.
+// Barriers: bfull (B' copied), bempty (its MMAs done), tfull[a] (accumulator a ready), tempty[a]
+// (accumulator a drained). Every wait is bounded; one that runs out sets ST_TIMEOUT for the
+// solve and stops the CTA after the copies and MMAs it issued have drained.
+// grid (row tiles, matrices), 192 threads.
+constexpr int TCU_THREADS = 192;
+constexpr int TCU_SMEM = 2 * TCU_A_BYTES + 2 * TCU_B_BYTES + 1024;
+constexpr uint32_t TCU_WAIT = 1u << 22;
+
+__global__ void __launch_bounds__(TCU_THREADS) tc_update_kernel(const InvTask* __restrict__ tasks, int k0,
+                                                                int32_t* __restrict__ status) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ uint32_t tslot;
+  __shared__ __align__(8) uint64_t bfull, bempty, tfull[2], tempty[2];
+  __shared__ int abort_flag;
+  const InvTask t = tasks[blockIdx.y];
+  const int n = t.n;
+  if (k0 >= t.npiv || t.bt == nullptr) return;
+  if (*t.bad) return;
+  const int kb = min(GJ_KB, t.npiv - k0);
+  const int rest = n - kb;
+  const int i0 = blockIdx.x * TCU_ROWS;
+  if (i0 >= n || rest <= 0) return;
+  const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+  constexpr int M = 2 * TCU_ROWS;
+  unsigned char* base = reinterpret_cast<unsigned char*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  unsigned char* a_hi = base;
+  unsigned char* a_lo = a_hi + TCU_A_BYTES;
+  unsigned char* b_hi = a_lo + TCU_A_BYTES;
+  unsigned char* b_lo = b_hi + TCU_B_BYTES;
+  float2* A = static_cast<float2*>(t.a);
+  const unsigned char* bt = static_cast<const unsigned char*>(t.bt);
+  const int64_t ld = t.ld;
+  const int tiles = (rest + TCU_COLS - 1) / TCU_COLS;
+  if (w == 0) tc::tmem_alloc(&tslot, 2 * TCU_COLS);
+  if (tid == 0) {
+    tc::mbar_init(&bfull, 1);
+    tc::mbar_init(&bempty, 1);
+    tc::mbar_init(&tfull[0], 1);
+    tc::mbar_init(&tfull[1], 1);
+    tc::mbar_init(&tempty[0], 4);
+    tc::mbar_init(&tempty[1], 4);
+    abort_flag = 0;
+  }
+  // A' from the panel columns of this tile's rows (zero past n and past 2 kb): a complex row and
+  // two complex columns per item, one 16-byte core-matrix row in each of real rows 2i, 2i + 1.
+  for (int idx = tid; idx < TCU_ROWS * (GJ_KB / 2); idx += blockDim.x) {
+    const int i = idx % TCU_ROWS, c = 2 * (idx / TCU_ROWS);
+    float2 p0 = make_float2(0.f, 0.f), p1 = make_float2(0.f, 0.f);
+    if (i0 + i < n) {
+      if (c < kb) p0 = A[(i0 + i) + (int64_t)(k0 + c) * ld];
+      if (c + 1 < kb) p1 = A[(i0 + i) + (int64_t)(k0 + c + 1) * ld];
+    }
+    const uint32_t o0 = tc::kmajor_offset(2 * i, 2 * c, M), o1 = tc::kmajor_offset(2 * i + 1, 2 * c, M);
+    tc::store_split(a_hi + o0, a_lo + o0, make_float4(p0.x, -p0.y, p1.x, -p1.y));
+    tc::store_split(a_hi + o1, a_lo + o1, make_float4(p0.y, p0.x, p1.y, p1.x));
+  }
+  tc::fence_smem_async();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tbase = tslot;
+  volatile int* abort_v = &abort_flag;
+  auto fail = [&]() {
+    *abort_v = 1;
+    status[t.job] = ST_TIMEOUT;
+  };
+  int copies = 0, mma_tiles = 0;  // issued by this thread (producer / MMA issuer)
+  if (w == 0) {
+    if (lane == 0)
+      for (int ct = 0; ct < tiles && !*abort_v; ++ct) {
+        if (ct >= 1 && !tc::mbar_wait(&bempty, (uint32_t)((ct - 1) & 1), TCU_WAIT)) { fail(); break; }
+        tc::mbar_arrive_expect_tx(&bfull, 2 * TCU_B_BYTES);
+        tc::bulk_copy_g2s(b_hi, bt + (size_t)ct * 2 * TCU_B_BYTES, TCU_B_BYTES, &bfull);
+        tc::bulk_copy_g2s(b_lo, bt + (size_t)ct * 2 * TCU_B_BYTES + TCU_B_BYTES, TCU_B_BYTES, &bfull);
+        ++copies;
+      }
+  } else if (w == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = tc::idesc_tf32(M, TCU_COLS);
+      const int slices = (2 * kb + 7) / 8;
+      for (int ct = 0; ct < tiles && !*abort_v; ++ct) {
+        const int a = ct & 1;
+        if (!tc::mbar_wait(&bfull, (uint32_t)(ct & 1), TCU_WAIT)) { fail(); break; }
+        if (ct >= 2 && !tc::mbar_wait(&tempty[a], (uint32_t)(((ct >> 1) - 1) & 1), TCU_WAIT)) { fail(); break; }
+        tc::fence_after_sync();
+        const uint32_t d = tbase + (uint32_t)(a * TCU_COLS);
+        for (int sl = 0; sl < slices; ++sl) {
+          const uint64_t ah = tc::smem_desc(tc::smem_addr(a_hi + sl * M * 32), 128, 256);
+          const uint64_t al = tc::smem_desc(tc::smem_addr(a_lo + sl * M * 32), 128, 256);
+          const uint64_t bh = tc::smem_desc(tc::smem_addr(b_hi + sl * TCU_COLS * 32), 128, 256);
+          const uint64_t bl = tc::smem_desc(tc::smem_addr(b_lo + sl * TCU_COLS * 32), 128, 256);
+          tc::mma_tf32(d, al, bh, idesc, sl > 0);
+          tc::mma_tf32(d, ah, bl, idesc, true);
+          tc::mma_tf32(d, ah, bh, idesc, true);
+        }
+        tc::mma_commit(&bempty);
+        tc::mma_commit(&tfull[a]);
+        ++mma_tiles;
+      }
+    }
+  } else {
+    // Epilogue: this warp's quarter of the 128 real rows; thread row r2, complex row i0 + r2 / 2.
+    const int q = w & 3;
+    const int r2 = 32 * q + lane;
+    const int gi = i0 + (r2 >> 1);
+    const bool row_in = gi < n;
+    const bool pivot_row = gi >= k0 && gi < k0 + kb;
+    float* Af = reinterpret_cast<float*>(A) + (r2 & 1);
+    for (int ct = 0; ct < tiles; ++ct) {
+      const int a = ct & 1, r0 = ct * TCU_COLS;
+      float old[TCU_COLS];
+#pragma unroll
+      for (int j = 0; j < TCU_COLS; ++j) {
+        const int r = r0 + j;
+        old[j] = 0.f;
+        if (row_in && !pivot_row && r < rest) old[j] = Af[2 * (gi + (int64_t)(r < k0 ? r : r + kb) * ld)];
+      }
+      bool ok = !*abort_v && tc::mbar_wait(&tfull[a], (uint32_t)((ct >> 1) & 1), TCU_WAIT);
+      ok = __all_sync(0xffffffffu, ok);
+      if (!ok) {
+        if (lane == 0) fail();
+        break;
+      }
+      tc::fence_after_sync();
+      float v[TCU_COLS];
+#pragma unroll
+      for (int c0 = 0; c0 < TCU_COLS; c0 += 16) {
+        float part[16];
+        tc::tmem_ld16(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(a * TCU_COLS + c0), part);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[c0 + i] = part[i];
+      }
+      tc::tmem_ld_wait();
+      tc::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&tempty[a]);
+#pragma unroll
+      for (int j = 0; j < TCU_COLS; ++j) {
+        const int r = r0 + j;
+        if (row_in && r < rest) Af[2 * (gi + (int64_t)(r < k0 ? r : r + kb) * ld)] = old[j] + v[j];
+      }
+    }
+  }
+  // Drain what this thread issued before tensor memory and shared memory go away.
+  if (*abort_v) {
+    if (w == 0 && lane == 0 && copies > 0) tc::mbar_wait(&bfull, (uint32_t)((copies - 1) & 1), TCU_WAIT);
+    if (w == 1 && lane == 0 && mma_tiles > 0) tc::mbar_wait(&bempty, (uint32_t)((mma_tiles - 1) & 1), TCU_WAIT);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (w == 0) tc::tmem_dealloc(tbase, 2 * TCU_COLS);
+}
 // Undo the row interchanges as column interchanges (last first), as cycles of the resulting column
 // permutation: every thread moves its own rows, no barrier per interchange. Shared memory: cperm,
 // the cycle list and a visited mark (3 x npiv ints). Reports refused pivots.

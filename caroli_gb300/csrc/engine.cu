@@ -215,11 +215,12 @@ struct TaskCache {
   std::vector<Task> tasks;
   std::vector<TaskLevel> levels;
   std::vector<InvTask> inv;
-  std::vector<size_t> inv_piv_off, inv_y_off;
-  size_t inv_piv = 0, inv_y = 0, root0 = 0, rinv0 = 0;
+  std::vector<size_t> inv_piv_off, inv_y_off, inv_bt_off;
+  size_t inv_piv = 0, inv_y = 0, inv_bt = 0, root0 = 0, rinv0 = 0;
   int max_root = 0;
   double root_flops = 0.0, trace_flops = 0.0;
-  const void *piv = nullptr, *y = nullptr, *scale = nullptr, *bad = nullptr, *dinv = nullptr, *dtasks = nullptr;
+  const void *piv = nullptr, *y = nullptr, *bt = nullptr, *scale = nullptr, *bad = nullptr, *dinv = nullptr,
+             *dtasks = nullptr;
 };
 
 }  // namespace
@@ -238,10 +239,11 @@ struct caroli_ctx {
   std::vector<std::unique_ptr<System>> systems;
   Buf arena, root_arena, xs, jobs, tasks, fail, status, tout, part, pert;
   RefineBufs rb[2];  // forward and adjoint refinement state
-  Buf inv, ipiv, iy, iscale, ibad;
+  Buf inv, ipiv, iy, ibt, iscale, ibad;
   TaskCache tcache;
   Buf grhs, gptr, gdv, gdp;
   double inner_tol = 1e-10;
+  bool tensor_cores = true;  // f32 rank-kb updates on tcgen05 (3xTF32); else on the CUDA cores
   int max_iters = 6;
   double refine_tol = 1e-10;
   double last_ms = 0.0;
@@ -770,6 +772,8 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
     const int small_max = Prec<T>::small_max;
     size_t& inv_piv = tc.inv_piv;  // scratch sizes: pivots (entries) and Y blocks (bytes)
     size_t& inv_y = tc.inv_y;
+    size_t& inv_bt = tc.inv_bt;
+    std::vector<size_t>& inv_bt_off = tc.inv_bt_off;
     std::vector<size_t>& inv_piv_off = tc.inv_piv_off;
     std::vector<size_t>& inv_y_off = tc.inv_y_off;
     size_t& root0 = tc.root0;
@@ -782,7 +786,8 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
     tasks.clear();
     levels.assign(max_levels, Level{});
     inv.clear();
-    inv_piv = inv_y = 0;
+    inv_piv = inv_y = inv_bt = 0;
+    inv_bt_off.clear();
     inv_piv_off.clear();
     inv_y_off.clear();
     for (int L = 0; L < max_levels; ++L) {
@@ -849,8 +854,10 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
               it.front = (int32_t)k;
               inv_piv_off.push_back(inv_piv);
               inv_y_off.push_back(inv_y);
+              inv_bt_off.push_back(vb == sizeof(float2) ? inv_bt : SIZE_MAX);
               inv_piv += fr[k].ne;
               inv_y += (size_t)GJ_KB * fr[k].n * vb;
+              if (vb == sizeof(float2)) inv_bt += tc_operand_bytes(fr[k].n);
               inv.push_back(it);
             }
           }
@@ -879,31 +886,35 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
       it.front = -1;
       inv_piv_off.push_back(inv_piv);
       inv_y_off.push_back(inv_y);
+      inv_bt_off.push_back(vr == sizeof(float2) ? inv_bt : SIZE_MAX);
       inv_piv += m;
       inv_y += (size_t)GJ_KB * m * vr;
+      if (vr == sizeof(float2)) inv_bt += tc_operand_bytes(m);
       inv.push_back(it);
     }
     }  // !hit
     // Inverse scratch: pivots, the Y blocks (sized for the wider type), scale and flags.
     int32_t* dpiv = static_cast<int32_t*>(ctx->ipiv.get(std::max<size_t>(inv_piv, 1) * sizeof(int32_t)));
     unsigned char* dy = static_cast<unsigned char*>(ctx->iy.get(std::max<size_t>(inv_y, 16)));
+    unsigned char* dbt = static_cast<unsigned char*>(ctx->ibt.get(std::max<size_t>(inv_bt, 16)));
     double* dscale = static_cast<double*>(ctx->iscale.get(std::max<size_t>(inv.size(), 1) * sizeof(double)));
     int32_t* dbad = static_cast<int32_t*>(ctx->ibad.get(std::max<size_t>(inv.size(), 1) * sizeof(int32_t)));
     InvTask* dinv = static_cast<InvTask*>(ctx->inv.get(std::max<size_t>(inv.size(), 1) * sizeof(InvTask)));
     Task* dtasks = static_cast<Task*>(ctx->tasks.get(tasks.size() * sizeof(Task)));
-    const bool same_scratch = hit && tc.piv == dpiv && tc.y == dy && tc.scale == dscale && tc.bad == dbad &&
-                              tc.dinv == dinv && tc.dtasks == dtasks;
+    const bool same_scratch = hit && tc.piv == dpiv && tc.y == dy && tc.bt == dbt && tc.scale == dscale &&
+                              tc.bad == dbad && tc.dinv == dinv && tc.dtasks == dtasks;
     if (!same_scratch) {
       for (size_t q = 0; q < inv.size(); ++q) {
         inv[q].piv = dpiv + inv_piv_off[q];
         inv[q].y = dy + inv_y_off[q];
+        inv[q].bt = inv_bt_off[q] == SIZE_MAX ? nullptr : dbt + inv_bt_off[q];
         inv[q].scale2 = dscale + q;
         inv[q].bad = dbad + q;
       }
       if (!inv.empty())
         CK(cudaMemcpyAsync(dinv, inv.data(), inv.size() * sizeof(InvTask), cudaMemcpyHostToDevice, s));
       CK(cudaMemcpyAsync(dtasks, tasks.data(), tasks.size() * sizeof(Task), cudaMemcpyHostToDevice, s));
-      tc.piv = dpiv; tc.y = dy; tc.scale = dscale; tc.bad = dbad; tc.dinv = dinv; tc.dtasks = dtasks;
+      tc.piv = dpiv; tc.y = dy; tc.bt = dbt; tc.scale = dscale; tc.bad = dbad; tc.dinv = dinv; tc.dtasks = dtasks;
     }
     tc.plans = key_plans;
     tc.tsize = (int)sizeof(T);
@@ -938,7 +949,11 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
         const unsigned rt = (unsigned)((nmax + 63) / 64);
         in_pieces(count, [&](size_t f0, size_t c) {
           launch(cls, per * c / count, 0.0, [&] {
-            inv_update_kernel<TT><<<dim3(rt, rt, (unsigned)c), 256, 0, s>>>(dinv + first + f0, k0);
+            if (std::is_same<TT, float>::value && ctx->tensor_cores)
+              tc_update_kernel<<<dim3((unsigned)((nmax + TCU_ROWS - 1) / TCU_ROWS), (unsigned)c), TCU_THREADS, TCU_SMEM, s>>>(
+                  dinv + first + f0, k0, status);
+            else
+              inv_update_kernel<TT><<<dim3(rt, rt, (unsigned)c), 256, 0, s>>>(dinv + first + f0, k0);
           });
         });
       }
@@ -1226,7 +1241,8 @@ int caroli_ctx_create(int device_ordinal, caroli_ctx** out) {
     ctx->mem_budget = free_b / 2;
     int optin = 0;
     CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_ordinal));
-    for (auto* k : {(const void*)small_front_kernel<double, false>, (const void*)small_front_kernel<float, false>,
+    for (auto* k : {(const void*)tc_update_kernel,
+                    (const void*)small_front_kernel<double, false>, (const void*)small_front_kernel<float, false>,
                     (const void*)small_front_kernel<double, true>, (const void*)small_front_kernel<float, true>,
                     (const void*)inv_finish_kernel<double>, (const void*)inv_finish_kernel<float>,
                     (const void*)inv_panel_kernel<double>, (const void*)inv_panel_kernel<float>,
@@ -1628,6 +1644,12 @@ int caroli_set_refine_options(caroli_ctx* ctx, int max_iters, double tol, double
   ctx->max_iters = max_iters;
   ctx->refine_tol = tol;
   ctx->inner_tol = inner_tol;
+  return CAROLI_OK;
+}
+
+int caroli_set_tensor_cores(caroli_ctx* ctx, int enable) {
+  if (!ctx) return CAROLI_EINVAL;
+  ctx->tensor_cores = enable != 0;
   return CAROLI_OK;
 }
 

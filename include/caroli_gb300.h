@@ -176,6 +176,10 @@ int caroli_last_refine_steps(const caroli_ctx* ctx, int64_t* job_steps, int64_t*
  * No reference counterpart (precision::PrecisionOptions covers only the double recomputation). */
 int caroli_set_refine_options(caroli_ctx* ctx, int max_iters, double tol, double inner_tol);
 
+/* Rank-32 Schur updates of f32 fronts (CAROLI_MIXED, CAROLI_SINGLE) on the tcgen05 tensor cores
+ * (3xTF32, default 1) or on the CUDA cores (0). No reference counterpart. */
+int caroli_set_tensor_cores(caroli_ctx* ctx, int enable);
+
 /* Device time of the last caroli_solve_batch split into the tree factorization, the root
  * inverse, and the rest (trace, or refinement and double-precision recomputations), in ms. */
 int caroli_last_phases(const caroli_ctx* ctx, double* factor_ms, double* root_ms, double* tail_ms);

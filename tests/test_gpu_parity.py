@@ -117,3 +117,35 @@ def test_magnetic_200x64_double_and_mixed_match_oracle():
     ref = ref.reshape(8, nb).sum(axis=1)
     assert np.abs(t64 - ref).max() <= 1e-8, np.abs(t64 - ref)
     assert np.abs(tm - ref).max() <= 1e-8, np.abs(tm - ref)
+
+
+def test_tensor_core_updates_match_cuda_cores():
+    """The f32 rank-32 updates on tcgen05 (3xTF32) against the same updates on the CUDA cores:
+    unrefined single-precision T is as close to the oracle either way (f32 rounding differs, and
+    near a band edge it moves T by up to ~1e-3), and both mixed-precision results reach the oracle
+    within 1e-8 with about the same refinement effort (GMRES steps over the batch)."""
+    from caroli_gb300.nested import context
+
+    sys_ = magnetic_bhz(60, 48, configs=2)
+    sigmas = [sys_.self_energies(e) for e in (-0.14, 0.02, 0.11)]
+    pairs = [(s, c) for s in sigmas for c in range(2)]
+    S, C = [p[0] for p in pairs], [p[1] for p in pairs]
+    ctx = context(0)
+    out = {}
+    try:
+        for tc in (True, False):
+            ctx.set_tensor_cores(tc)
+            t32, st32, _ = sys_.solve_batch(S, C, Precision.SINGLE)
+            tm, stm, _ = sys_.solve_batch(S, C, Precision.MIXED)
+            assert (st32 == 0).all() and (stm == 0).all()
+            out[tc] = (t32, tm, sys_.plan().last_refine_steps()[0])
+    finally:
+        ctx.set_tensor_cores(True)
+    for k, (s, c) in enumerate(pairs):
+        ref = oracle_T(sys_, s, config=c)
+        e_tc, e_cc = abs(out[True][0][k] - ref), abs(out[False][0][k] - ref)
+        # Unrefined f32 either way (3xTF32 products carry about 4x the rounding of an f32 FMA).
+        assert e_tc <= 1e-2 and e_cc <= 1e-2, (s.energy, c, e_tc, e_cc)
+        a, b = out[True][1][k], out[False][1][k]
+        assert abs(a - ref) <= 1e-8 and abs(b - ref) <= 1e-8, (s.energy, c, a, b, ref)
+    assert out[True][2] <= out[False][2] + 4, (out[True][2], out[False][2])
