@@ -201,7 +201,7 @@ struct TaskLevel {
   // Small fronts in size buckets (one launch each, shared memory sized to the bucket).
   size_t sb0[3] = {0, 0, 0}, sbn[3] = {0, 0, 0};
   int sb_n[3] = {0, 0, 0}, sb_ne[3] = {0, 0, 0};
-  size_t xs_elems = 0, inv0 = 0;
+  size_t inv0 = 0;
   double small_flops = 0, small_bytes = 0, inv_flops = 0, gemm0_flops = 0, gemm1_flops = 0, asm_bytes = 0;
 };
 
@@ -237,7 +237,7 @@ struct caroli_ctx {
   double factor_ms = 0.0, root_ms = 0.0, tail_ms = 0.0;
   std::string err;
   std::vector<std::unique_ptr<System>> systems;
-  Buf arena, root_arena, xs, jobs, tasks, fail, status, tout, part, pert;
+  Buf arena, root_arena, jobs, tasks, fail, status, tout, part, pert;
   RefineBufs rb[2];  // forward and adjoint refinement state
   Buf inv, ipiv, iy, ibt, iscale, ibad;
   TaskCache tcache;
@@ -796,9 +796,10 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
       lv.tiny0 = tasks.size();
       for (size_t j = 0; j < cj; ++j) {
         const auto& fr = specs[begin + j].plan->host.fronts;
+        const FrontDesc* dfr = specs[begin + j].plan->fronts;
         for (size_t k = 0; k + 1 < fr.size(); ++k)
           if (fr[k].level == L && fr[k].n <= TINY_MAX) {
-            tasks.push_back({(int32_t)j, (int32_t)k, 0});
+            tasks.push_back({(int32_t)j, (int32_t)k, dfr + k});
             const double ne = fr[k].ne, nb = fr[k].n - fr[k].ne;
             lv.small_flops += 8.0 / 3 * ne * ne * ne + 8 * ne * ne * nb + 8 * nb * nb * ne;
           }
@@ -811,9 +812,10 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
         lv.sb0[b] = tasks.size();
         for (size_t j = 0; j < cj; ++j) {
           const auto& fr = specs[begin + j].plan->host.fronts;
+          const FrontDesc* dfr = specs[begin + j].plan->fronts;
           for (size_t k = 0; k + 1 < fr.size(); ++k)
             if (fr[k].level == L && fr[k].n > lo && fr[k].n <= hi) {
-              tasks.push_back({(int32_t)j, (int32_t)k, 0});
+              tasks.push_back({(int32_t)j, (int32_t)k, dfr + k});
               const double ne = fr[k].ne, nb = fr[k].n - fr[k].ne;
               lv.max_small_n = std::max(lv.max_small_n, fr[k].n);
               lv.max_small_ne = std::max(lv.max_small_ne, fr[k].ne);
@@ -830,14 +832,13 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
       lv.small_n = tasks.size() - lv.small0;
       lv.large0 = tasks.size();
       lv.inv0 = inv.size();
-      size_t xo = 0;
       for (size_t j = 0; j < cj; ++j) {
         const auto& fr = specs[begin + j].plan->host.fronts;
+        const FrontDesc* dfr = specs[begin + j].plan->fronts;
         for (size_t k = 0; k + 1 < fr.size(); ++k)
           if (fr[k].level == L && fr[k].n > small_max) {
-            tasks.push_back({(int32_t)j, (int32_t)k, (int64_t)xo});
+            tasks.push_back({(int32_t)j, (int32_t)k, dfr + k});
             const double ne = fr[k].ne, nb = fr[k].n - fr[k].ne;
-            xo += (size_t)fr[k].ne * (fr[k].n - fr[k].ne);
             lv.max_large_n = std::max(lv.max_large_n, fr[k].n);
             lv.max_large_ne = std::max(lv.max_large_ne, fr[k].ne);
             lv.inv_flops += 8.0 / 3 * ne * ne * ne;
@@ -863,7 +864,6 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
           }
       }
       lv.large_n = tasks.size() - lv.large0;
-      lv.xs_elems = xo;
       lv.max_n = std::max(std::max(lv.max_small_n, lv.max_large_n), lv.tiny_n ? TINY_MAX : 0);
     }
     root0 = tasks.size();
@@ -872,7 +872,7 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
     root_flops = trace_flops = 0.0;
     for (size_t j = 0; j < cj; ++j) {
       const auto& P = specs[begin + j].plan->host;
-      tasks.push_back({(int32_t)j, P.root, 0});
+      tasks.push_back({(int32_t)j, P.root, specs[begin + j].plan->fronts + P.root});
       const int m = P.fronts[P.root].n;
       max_root = std::max(max_root, m);
       root_flops += 8.0 / 3 * m * (double)m * m + 8.0 * m * (double)m * P.nr;
@@ -924,9 +924,6 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
     tc.rarena = rarena;
     tc.max_levels = max_levels;
     tc.valid = true;
-    size_t xs_max = 1;
-    for (auto& lv : levels) xs_max = std::max(xs_max, lv.xs_elems);
-    V* xs = static_cast<V*>(ctx->xs.get(xs_max * vb));
 
     // Batched blocked inverse of `count` matrices starting at dinv + first, largest n.
     // Batched blocked sweep of `count` fronts starting at dinv + first: largest size nmax, largest
@@ -1001,7 +998,6 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
         inverse(T{}, lv.inv0, ninv, lv.max_large_n, lv.max_large_ne, Prec<T>::tol, perturb, K_PIVOT,
                 lv.inv_flops + lv.gemm0_flops + lv.gemm1_flops);
         (void)mt;
-        (void)xs;
       }
     }
     CK(cudaEventRecord(ctx->evf, s));
@@ -1856,9 +1852,10 @@ extern "C" int caroli_solve_batch_noalloc(caroli_ctx* ctx, int plan_id, int coun
       v = Lv{tasks.size(), 0, 0, 0, 0, 0, 0, 0, 0};
       for (size_t j = 0; j < nj; ++j) {
         const auto& fr = sys->plans[j % nb]->host.fronts;
+        const FrontDesc* dfr = sys->plans[j % nb]->fronts;
         for (size_t k = 0; k + 1 < fr.size(); ++k)
           if (fr[k].level == L && fr[k].n <= SMALL_MAX_F64) {
-            tasks.push_back({(int32_t)j, (int32_t)k, 0});
+            tasks.push_back({(int32_t)j, (int32_t)k, dfr + k});
             v.smax = std::max(v.smax, fr[k].n);
           }
       }
@@ -1867,9 +1864,10 @@ extern "C" int caroli_solve_batch_noalloc(caroli_ctx* ctx, int plan_id, int coun
       v.i0 = inv.size();
       for (size_t j = 0; j < nj; ++j) {
         const auto& fr = sys->plans[j % nb]->host.fronts;
+        const FrontDesc* dfr = sys->plans[j % nb]->fronts;
         for (size_t k = 0; k + 1 < fr.size(); ++k)
           if (fr[k].level == L && fr[k].n > SMALL_MAX_F64) {
-            tasks.push_back({(int32_t)j, (int32_t)k, 0});
+            tasks.push_back({(int32_t)j, (int32_t)k, dfr + k});
             v.lmax = std::max(v.lmax, fr[k].n);
             v.lne = std::max(v.lne, fr[k].ne);
             if (fr[k].ne > 0) add_inv(arena + arena_off[j] + fr[k].arena_off, fr[k].n, fr[k].ne, (int32_t)j, (int32_t)k);
@@ -1881,7 +1879,7 @@ extern "C" int caroli_solve_batch_noalloc(caroli_ctx* ctx, int plan_id, int coun
     const size_t root0 = tasks.size(), rinv0 = inv.size();
     for (size_t j = 0; j < nj; ++j) {
       const FrontPlan& P = sys->plans[j % nb]->host;
-      tasks.push_back({(int32_t)j, P.root, 0});
+      tasks.push_back({(int32_t)j, P.root, sys->plans[j % nb]->fronts + P.root});
       const int m = P.fronts[P.root].n;
       add_inv(rarena + root_off[j], m, m, (int32_t)j, -1);
     }

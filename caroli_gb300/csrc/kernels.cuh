@@ -49,7 +49,7 @@ struct JobDesc {
 
 struct Task {
   int32_t job, front;
-  int64_t xoff;  // offset of the front's X block in the level's scratch (large fronts)
+  const FrontDesc* fd;  // the front's descriptor (device), read without going through the job
 };
 
 template <typename T> struct Cx;
@@ -403,7 +403,7 @@ __global__ void __launch_bounds__(256) small_front_kernel(const JobDesc* __restr
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const Task t = tasks[blockIdx.x];
   const JobDesc& J = jobs[t.job];
-  const FrontDesc& f = J.fronts[t.front];
+  const FrontDesc& f = *t.fd;
   const int n = f.n, ne = f.ne;
   const int ld = n | 1;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -506,7 +506,7 @@ __global__ void __launch_bounds__(256) assemble_kernel(const JobDesc* __restrict
   using V = typename Cx<T>::V;
   const Task t = tasks[blockIdx.y];
   const JobDesc& J = jobs[t.job];
-  const FrontDesc& f = J.fronts[t.front];
+  const FrontDesc& f = *t.fd;
   const int n = f.n;
   const int c0 = blockIdx.x * 32;
   if (c0 >= n) return;

@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(256) sweep_tiny_fwd_kernel(const RefineDesc* _
   const RefineDesc& R = rd[tk.job];
   const int j0 = blockIdx.y * CB;
   if (sweep_idle(R, src) || j0 >= R.c) return;
-  const FrontDesc& f = R.fronts[tk.front];
+  const FrontDesc& f = *tk.fd;
   const int n = f.n, ne = f.ne;
   float2 z[CB];
   if (lane < n) load_z<CB>(R, sweep_src(R, src), R.srows[f.var_off + lane], j0, z);
@@ -94,7 +94,7 @@ __global__ void __launch_bounds__(256) sweep_tiny_bwd_kernel(const RefineDesc* _
   const RefineDesc& R = rd[tk.job];
   const int j0 = blockIdx.y * CB;
   if (sweep_idle(R, src) || j0 >= R.c) return;
-  const FrontDesc& f = R.fronts[tk.front];
+  const FrontDesc& f = *tk.fd;
   const int n = f.n, ne = f.ne, nb = n - ne;
   if (ne == 0) return;
   float2* dout = sweep_dst(R, dst);
@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(256) sweep_rows_fwd_kernel(const RefineDesc* _
   const RefineDesc& R = rd[tk.job];
   const int j0 = blockIdx.z * CB;
   if (sweep_idle(R, src) || j0 >= R.c) return;
-  const FrontDesc& f = R.fronts[tk.front];
+  const FrontDesc& f = *tk.fd;
   const int n = f.n, ne = f.ne;
   const int r0 = blockIdx.y * SW_ROWS;
   if (r0 >= n) return;
@@ -198,7 +198,7 @@ __global__ void __launch_bounds__(256) sweep_rows_bwd_kernel(const RefineDesc* _
   const RefineDesc& R = rd[tk.job];
   const int j0 = blockIdx.z * CB;
   if (sweep_idle(R, src) || j0 >= R.c) return;
-  const FrontDesc& f = R.fronts[tk.front];
+  const FrontDesc& f = *tk.fd;
   const int n = f.n, ne = f.ne, nb = n - ne;
   const int r0 = blockIdx.y * SW_ROWS;
   if (r0 >= ne) return;

@@ -30,7 +30,7 @@ __global__ void __launch_bounds__(256) tiny_front_kernel(const JobDesc* __restri
   if (ti >= ntasks) return;
   const Task t = tasks[ti];
   const JobDesc& J = jobs[t.job];
-  const FrontDesc& f = J.fronts[t.front];
+  const FrontDesc& f = *t.fd;
   const int n = f.n, ne = f.ne;
   V* F = reinterpret_cast<V*>(smem_raw) + (size_t)w * (TINY_MAX * LD + TINY_MAX);
   V* prow = F + TINY_MAX * LD;
