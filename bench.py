@@ -41,7 +41,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "T(E) solves/s, mixed+refined vs FP64 GPU at |ΔT|≤1e-8; grad/fwd time ratio"
 # Kernel classes whose algorithmic work is counted in flops (the rest in bytes).
-FLOP_CLASSES = {"small_front", "large_front", "front_gemm", "root_inverse", "trace", "refine_residual"}
+FLOP_CLASSES = {"large_front_panel", "large_front_update", "root_inverse", "trace", "refine_residual"}
 WORKLOAD = "bhz-magnetic-200x64: BHZ 200x64, magnetic c=0.2 J=0.4 opposite-g polarised, 33 E in [-0.16,0.16] x 8 configs"
 
 

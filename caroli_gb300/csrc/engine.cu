@@ -163,9 +163,9 @@ struct Buf {
 
 // Kernel classes for per-kernel accounting: launches, algorithmic flops and bytes (computed on
 // the host from the task lists), and device time when the class is probed.
-enum KClass { K_SMALL = 0, K_ASSEMBLE, K_PIVOT, K_GEMM, K_STOREX, K_ROOT_ASM, K_ROOT_INV, K_TRACE,
+enum KClass { K_SMALL = 0, K_ASSEMBLE, K_PANEL, K_UPDATE, K_ROOT_ASM, K_ROOT_INV, K_TRACE,
               K_REF_FWD, K_REF_ROOT, K_REF_BWD, K_REF_RES, K_REF_CHECK, K_REF_GMRES, K_COUNT };
-const char* const kclass_names[K_COUNT] = {"small_front", "assemble", "large_front", "front_gemm", "store_x",
+const char* const kclass_names[K_COUNT] = {"small_front", "assemble", "large_front_panel", "large_front_update",
                                            "root_assemble", "root_inverse", "trace", "refine_forward",
                                            "refine_root", "refine_backward", "refine_residual", "refine_check",
                                            "refine_gmres"};
@@ -203,6 +203,9 @@ struct TaskLevel {
   int sb_n[3] = {0, 0, 0}, sb_ne[3] = {0, 0, 0};
   size_t inv0 = 0;
   double small_flops = 0, small_bytes = 0, inv_flops = 0, gemm0_flops = 0, gemm1_flops = 0, asm_bytes = 0;
+  double tiny_flops = 0, tiny_bytes = 0;
+  double upd_flops = 0, upd_bytes = 0;  // the rank-kb updates of the blocked sweep
+  double pan_flops = 0;                 // its panel sweeps (kb steps over n rows of kb columns)
 };
 
 // The task lists of the last batch (see run_jobs).
@@ -801,7 +804,8 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
           if (fr[k].level == L && fr[k].n <= TINY_MAX) {
             tasks.push_back({(int32_t)j, (int32_t)k, dfr + k});
             const double ne = fr[k].ne, nb = fr[k].n - fr[k].ne;
-            lv.small_flops += 8.0 / 3 * ne * ne * ne + 8 * ne * ne * nb + 8 * nb * nb * ne;
+            lv.tiny_flops += 8.0 / 3 * ne * ne * ne + 8 * ne * ne * nb + 8 * nb * nb * ne;
+            lv.tiny_bytes += ((double)fr[k].n * fr[k].n + (mixed ? (double)fr[k].n * fr[k].n : nb * nb)) * vb;
           }
       }
       lv.tiny_n = tasks.size() - lv.tiny0;
@@ -822,8 +826,8 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
               lv.sb_n[b] = std::max(lv.sb_n[b], fr[k].n);
               lv.sb_ne[b] = std::max(lv.sb_ne[b], fr[k].ne);
               lv.small_flops += 8.0 / 3 * ne * ne * ne + 8 * ne * ne * nb + 8 * nb * nb * ne;
-              lv.small_bytes +=
-                  ((double)fr[k].n * fr[k].n * (mixed ? 1.0 : nb * nb / std::max(1.0, (double)fr[k].n * fr[k].n))) * vb;
+              // The front written (mixed keeps all of it, else S) and the children's blocks read.
+              lv.small_bytes += ((double)fr[k].n * fr[k].n + (mixed ? (double)fr[k].n * fr[k].n : nb * nb)) * vb;
             }
         }
         lv.sbn[b] = tasks.size() - lv.sb0[b];
@@ -844,6 +848,12 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
             lv.inv_flops += 8.0 / 3 * ne * ne * ne;
             lv.gemm0_flops += 8 * ne * ne * nb;
             lv.gemm1_flops += 8 * nb * nb * ne;
+            for (int k0 = 0; k0 < fr[k].ne; k0 += GJ_KB) {
+              const double kb = std::min(GJ_KB, fr[k].ne - k0), nn = fr[k].n;
+              lv.upd_flops += 8.0 * nn * (nn - kb) * kb;  // complex n x kb times kb x (n - kb)
+              lv.upd_bytes += 2.0 * nn * (nn - kb) * vb;  // the rest columns read and written
+              lv.pan_flops += 8.0 * nn * kb * kb;
+            }
             lv.asm_bytes += (double)fr[k].n * fr[k].n * vb;
             if (fr[k].ne > 0) {
               InvTask it{};
@@ -928,8 +938,10 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
     // Batched blocked inverse of `count` matrices starting at dinv + first, largest n.
     // Batched blocked sweep of `count` fronts starting at dinv + first: largest size nmax, largest
     // pivot count pmax.
+    // Work attribution (kernel-class accounting): the panel sweeps to `cls` with `flops`, the
+    // rank-kb updates to `ucls` with their flops and bytes.
     auto inverse = [&](auto tag, size_t first, size_t count, int nmax, int pmax, double tol, int perturb, KClass cls,
-                       double flops) {
+                       double flops, KClass ucls, double uflops, double ubytes) {
       using TT = decltype(tag);
       using VV = typename Cx<TT>::V;
       if (!count || nmax <= 0 || pmax <= 0) return;
@@ -937,15 +949,16 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
       const size_t smf = (size_t)finish_bytes(pmax);
       if (!sm || smf > (size_t)SMEM_LIMIT) throw CudaError{cudaErrorInvalidValue, "front too large for a panel sweep"};
       const int panels = (pmax + GJ_KB - 1) / GJ_KB;
-      const double per = flops / (2.0 * panels + 2.0);
-      launch(cls, per, 0.0, [&] { inv_scale_kernel<TT><<<(unsigned)count, 256, 0, s>>>(dinv + first); });
+      const double per = flops / panels;
+      const double uper = uflops / panels, ubper = ubytes / panels;
+      launch(cls, 0.0, 0.0, [&] { inv_scale_kernel<TT><<<(unsigned)count, 256, 0, s>>>(dinv + first); });
       for (int k0 = 0; k0 < pmax; k0 += GJ_KB) {
         launch(cls, per, 0.0, [&] {
           inv_panel_kernel<TT><<<(unsigned)count, 256, sm, s>>>(dinv + first, k0, tol, perturb, (int)sm);
         });
         const unsigned rt = (unsigned)((nmax + 63) / 64);
         in_pieces(count, [&](size_t f0, size_t c) {
-          launch(cls, per * c / count, 0.0, [&] {
+          launch(ucls, uper * c / count, ubper * c / count, [&] {
             if (std::is_same<TT, float>::value && ctx->tensor_cores)
               tc_update_kernel<<<dim3((unsigned)((nmax + TCU_ROWS - 1) / TCU_ROWS), (unsigned)c), TCU_THREADS, TCU_SMEM, s>>>(
                   dinv + first + f0, k0, status);
@@ -954,7 +967,7 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
           });
         });
       }
-      launch(cls, per, 0.0, [&] { inv_finish_kernel<TT><<<(unsigned)count, 256, smf, s>>>(dinv + first, djobs, status); });
+      launch(cls, 0.0, 0.0, [&] { inv_finish_kernel<TT><<<(unsigned)count, 256, smf, s>>>(dinv + first, djobs, status); });
     };
 
     CK(cudaEventRecord(ctx->ev0, s));
@@ -964,7 +977,7 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
       const Level& lv = levels[L];
       if (lv.tiny_n) {
         const unsigned blocks = (unsigned)((lv.tiny_n + TINY_WARPS - 1) / TINY_WARPS);
-        launch(K_SMALL, 0.0, 0.0, [&] {
+        launch(K_SMALL, lv.tiny_flops, lv.tiny_bytes, [&] {
           if (mixed)
             tiny_front_kernel<T, true><<<blocks, 256, tiny_smem<T>(), s>>>(djobs, dtasks + lv.tiny0, (int)lv.tiny_n,
                                                                            Prec<T>::tol, perturb, pert);
@@ -995,8 +1008,8 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
           });
         });
         const size_t ninv = (L + 1 < max_levels ? levels[L + 1].inv0 : rinv0) - lv.inv0;
-        inverse(T{}, lv.inv0, ninv, lv.max_large_n, lv.max_large_ne, Prec<T>::tol, perturb, K_PIVOT,
-                lv.inv_flops + lv.gemm0_flops + lv.gemm1_flops);
+        inverse(T{}, lv.inv0, ninv, lv.max_large_n, lv.max_large_ne, Prec<T>::tol, perturb, K_PANEL, lv.pan_flops,
+                K_UPDATE, lv.upd_flops, lv.upd_bytes);
         (void)mt;
       }
     }
@@ -1010,7 +1023,8 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
         assemble_kernel<T, TR><<<dim3((max_root + 31) / 32, (unsigned)c), 256, 0, s>>>(djobs, rt + f0, 1);
       });
     });
-    inverse(TR{}, rinv0, cj, max_root, max_root, mixed ? Prec<T>::tol * 1e-2 : 0.0, perturb, K_ROOT_INV, root_flops);
+    inverse(TR{}, rinv0, cj, max_root, max_root, mixed ? Prec<T>::tol * 1e-2 : 0.0, perturb, K_ROOT_INV, root_flops,
+            K_ROOT_INV, 0.0, 0.0);
     CK(cudaEventRecord(ctx->evr, s));
     std::vector<double> th(cj), eh(cj, 0.0);
     std::vector<int32_t> sh(cj, ST_OK), ih(cj, 0);
