@@ -112,6 +112,21 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def profiled_traffic(kernel_class):
+    """DRAM bytes per step of a kernel class from the committed ncu summary of this workload
+    (profiles/launches_mixed_bhz200x64.md), or None."""
+    path = os.path.join(ROOT, "profiles", "launches_mixed_bhz200x64.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                parts = line.split()
+                if len(parts) == 4 and parts[0] == "traffic" and parts[1] == kernel_class and parts[3] == "GB":
+                    return float(parts[2]) * 1e9
+    except OSError:
+        pass
+    return None
+
+
 def peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -291,15 +306,18 @@ def run_ours(args):
     dom = max(probe.items(), key=lambda kv: kv[1]["ms"])
     pk = peaks()
     d = dom[1]
+    traffic = profiled_traffic(dom[0])
     if dom[0] in FLOP_CLASSES:
         achieved = d["flops"] / (d["ms"] * 1e-3) / 1e12
         roof = {"kernel": dom[0], "bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
-                "frac": achieved / pk["bf16_tflops"], "traffic": None,
-                "note": f"peak = {pk['source']} bf16 dense; the kernel runs on FP32 CUDA cores"}
+                "frac": achieved / pk["bf16_tflops"], "traffic": traffic,
+                "note": f"peak = {pk['source']} bf16 dense"}
     else:
         achieved = d["bytes"] / (d["ms"] * 1e-3) / 1e9
         roof = {"kernel": dom[0], "bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                "frac": achieved / pk["hbm_gbs"], "traffic": None, "note": f"peak = {pk['source']} HBM copy"}
+                "frac": achieved / pk["hbm_gbs"], "traffic": traffic, "note": f"peak = {pk['source']} HBM copy"}
+    roof["per"] = "step (all launches of the class in one step); traffic from the committed ncu launch list"
+    roof["algorithmic"] = d["bytes"] if roof["bound"] == "hbm" else d["flops"]
     roof["ms_per_step"] = d["ms"]
     roof["launches_per_step"] = d["launches"]
     roof["share_of_step"] = d["ms"] / (ms_max / args.steps)
