@@ -7,13 +7,13 @@ runs in ``libcaroli_gb300.so`` (``csrc/``), reached through the C ABI of
 from .lattice import Lattice, Region, Site
 from .leads import GreenError, LeadSolver, broadening, gamma_root
 from .model import BhzParams, Model, OnSiteMap, SparseMatrix, bhz, bhz_exchange, bhz_spin, cubic, graphene, square
-from .nested import LeadSelfEnergies, NestedTwoTerminal
+from .nested import LeadSelfEnergies, NestedTwoTerminal, solve_systems
 from .precision import Precision, PrecisionOptions, PrecisionReport, checked
 from .system import System, build_system
 
 __all__ = [
     "Lattice", "Region", "Site", "GreenError", "LeadSolver", "broadening", "gamma_root", "BhzParams", "Model",
     "OnSiteMap", "SparseMatrix", "bhz", "bhz_exchange", "bhz_spin", "cubic", "graphene", "square",
-    "LeadSelfEnergies", "NestedTwoTerminal", "Precision", "PrecisionOptions", "PrecisionReport", "checked",
+    "LeadSelfEnergies", "NestedTwoTerminal", "solve_systems", "Precision", "PrecisionOptions", "PrecisionReport", "checked",
     "System", "build_system",
 ]

@@ -44,6 +44,7 @@ SIGNATURES = {
     "caroli_last_refine_steps": (ctypes.c_int, [P, P, P]),
     "caroli_set_refine_options": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_double, ctypes.c_double]),
     "caroli_set_tensor_cores": (ctypes.c_int, [P, ctypes.c_int]),
+    "caroli_solve_multi": (ctypes.c_int, [P, ctypes.c_int, P, P, P, ctypes.c_int, P, P, P]),
     "caroli_kernel_class_name": (ctypes.c_char_p, [ctypes.c_int]),
     "caroli_probe_kernel": (ctypes.c_int, [P, ctypes.c_int]),
     "caroli_kernel_stats": (ctypes.c_int, [P, ctypes.c_int, P, P, P, P, ctypes.c_int]),
@@ -109,6 +110,19 @@ class Context:
     def set_tensor_cores(self, enable=True):
         """f32 rank-32 updates on the tcgen05 tensor cores (True) or the CUDA cores."""
         self.check(self.lib.caroli_set_tensor_cores(self.h, 1 if enable else 0))
+
+    def solve_multi(self, plans, slots, configs, precision=DOUBLE):
+        """T for instances of several plans of this context in one batch (``caroli_solve_multi``)."""
+        ids = np.ascontiguousarray([p.id for p in plans], np.int32)
+        slots = np.ascontiguousarray(slots, np.int32)
+        configs = np.ascontiguousarray(configs, np.int32)
+        n = len(ids)
+        t = np.zeros(n)
+        st = np.zeros(n, np.int32)
+        err = np.zeros(n)
+        self.check(self.lib.caroli_solve_multi(self.h, n, ptr(ids), ptr(slots), ptr(configs), precision, ptr(t),
+                                               ptr(st), ptr(err)))
+        return t, st, err
 
     def kernel_classes(self):
         return [self.lib.caroli_kernel_class_name(k).decode() for k in range(self.lib.caroli_kernel_classes())]

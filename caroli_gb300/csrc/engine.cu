@@ -174,9 +174,12 @@ struct KStat {
   double flops = 0.0, bytes = 0.0, ms = 0.0;
 };
 
+// One block solve of a batch: the system it belongs to (a batch may mix systems), its block,
+// energy slot, configuration and plan.
 struct JobSpec {
   int block, slot, config;
   const DevPlan* plan;
+  System* sys;
 };
 
 // Device state of one refinement (forward, or the adjoint of the gradient).
@@ -318,8 +321,8 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
   for (size_t j = 0; j < cj; ++j) {
     const JobSpec& sp = specs[begin + j];
     const FrontPlan& P = sp.plan->host;
-    const DevBlock& B = sys->blocks[sp.block];
-    const int c = sys->slots[sp.slot].channels[sp.block];
+    const DevBlock& B = sp.sys->blocks[sp.block];
+    const int c = sp.sys->slots[sp.slot].channels[sp.block];
     cmax = std::max(cmax, c);
     max_blk = std::max(max_blk, B.nblk);
     xoffs[j] = xo; xo += (size_t)B.nblk * c;
@@ -356,8 +359,8 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
   for (size_t j = 0; j < cj; ++j) {
     const JobSpec& sp = specs[begin + j];
     const DevPlan& P = *sp.plan;
-    const DevBlock& B = sys->blocks[sp.block];
-    const SigmaSlot& sg = sys->slots[sp.slot];
+    const DevBlock& B = sp.sys->blocks[sp.block];
+    const SigmaSlot& sg = sp.sys->slots[sp.slot];
     RefineDesc& R = rdh[j];
     std::memset(&R, 0, sizeof(R));
     R.fronts = P.fronts; R.maps = P.maps; R.own = P.own; R.vidx = P.vidx; R.srows = P.srows;
@@ -626,8 +629,8 @@ void gradient(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, s
   int max_blk = 0;
   for (size_t j = 0; j < cj; ++j) {
     const JobSpec& sp = specs[begin + j];
-    const int nblk = sys->blocks[sp.block].nblk;
-    const int c = sys->slots[sp.slot].channels[sp.block];
+    const int nblk = sp.sys->blocks[sp.block].nblk;
+    const int c = sp.sys->slots[sp.slot].channels[sp.block];
     roff[j] = ro;
     ro += (size_t)nblk * c;
     doff[j] = dvo;
@@ -679,7 +682,7 @@ void gradient(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, s
   CK(cudaStreamSynchronize(s));
   for (size_t j = 0; j < cj; ++j) {
     JobOut& o = out[begin + j];
-    const int nblk = sys->blocks[specs[begin + j].block].nblk;
+    const int nblk = specs[begin + j].sys->blocks[specs[begin + j].block].nblk;
     o.dv.assign(dvh.begin() + doff[j], dvh.begin() + doff[j] + nblk);
     o.dp.assign(grad.nparams, 0.0);
     if (grad.dvals)
@@ -743,12 +746,12 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
     for (size_t j = 0; j < cj; ++j) {
       const JobSpec& sp = specs[begin + j];
       const DevPlan& P = *sp.plan;
-      const SigmaSlot& sg = sys->slots[sp.slot];
+      const SigmaSlot& sg = sp.sys->slots[sp.slot];
       JobDesc& d = jd[j];
       d.fronts = P.fronts; d.maps = P.maps; d.own = P.own; d.entries = P.entries;
       d.arena = arena + arena_off[j];
       d.root_arena = rarena + root_off[j];
-      d.vals = sys->vals + (size_t)sp.config * sys->desc.row_ptr[sys->desc.n];
+      d.vals = sp.sys->vals + (size_t)sp.config * sp.sys->desc.row_ptr[sp.sys->desc.n];
       d.sigma_l = sg.sl[sp.block]; d.sigma_r = sg.sr[sp.block];
       d.gamma_l = sg.gl[sp.block]; d.gamma_r = sg.gr[sp.block];
       d.fail = fail + fail_off[j];
@@ -1105,19 +1108,19 @@ void solve_with_delays(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>&
   for (size_t j = 0; j < specs.size(); ++j)
     if (out[j].status == ST_PIVOT_DELAYED) {
       pending.push_back(j);
-      delayed[j].assign(sys->trees[specs[j].block].nodes.size(), 0);
+      delayed[j].assign(specs[j].sys->trees[specs[j].block].nodes.size(), 0);
     }
   for (int round = 0; !pending.empty() && round < 64; ++round) {
     std::vector<std::unique_ptr<DevPlan>> plans;
     std::vector<JobSpec> again;
     for (size_t j : pending) {
-      const BlockTree& tree = sys->trees[specs[j].block];
+      const BlockTree& tree = specs[j].sys->trees[specs[j].block];
       for (size_t k = 0; k < tree.nodes.size(); ++k)
         if (k < out[j].fail.size() && out[j].fail[k]) delayed[j][k] = 1;
       auto dp = std::make_unique<DevPlan>();
-      dp->host = make_plan(sys->desc, tree, delayed[j]);
+      dp->host = make_plan(specs[j].sys->desc, tree, delayed[j]);
       dp->upload(ctx->stream);
-      again.push_back({specs[j].block, specs[j].slot, specs[j].config, dp.get()});
+      again.push_back({specs[j].block, specs[j].slot, specs[j].config, dp.get(), specs[j].sys});
       plans.push_back(std::move(dp));
     }
     std::vector<JobOut> res;
@@ -1467,7 +1470,7 @@ int caroli_transmission_with_grad(caroli_ctx* ctx, int plan_id, int count, const
     const int nb = (int)sys->plans.size();
     std::vector<JobSpec> specs;
     for (int i = 0; i < count; ++i)
-      for (int b = 0; b < nb; ++b) specs.push_back({b, slots[i], configs[i], sys->plans[b].get()});
+      for (int b = 0; b < nb; ++b) specs.push_back({b, slots[i], configs[i], sys->plans[b].get(), sys});
     GradRequest g;
     g.dvals = sys->dvals;
     g.nparams = sys->dvals ? sys->nparams : 0;
@@ -1554,15 +1557,23 @@ int caroli_sigma_upload(caroli_ctx* ctx, int plan_id, int slot, double energy, c
   }
 }
 
-int caroli_solve_batch(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots, const int32_t* configs,
-                       int precision, double* t, int32_t* status, double* err) {
-  System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
-  if (!sys || count < 0 || (count > 0 && (!slots || !configs || !t || !status)))
-    return fail_with(ctx, CAROLI_EINVAL, "caroli_solve_batch: bad arguments");
+}  // extern "C"
+
+namespace {
+
+// T of `count` instances (system isys[i], energy slot, configuration) in one batch: the instances
+// may belong to different systems (different sizes and trees); every block solve of every instance
+// goes into the same level-synchronous launches.
+int solve_instances(caroli_ctx* ctx, const std::vector<System*>& isys, int count, const int32_t* slots,
+                    const int32_t* configs, int precision, double* t, int32_t* status, double* err, const char* who) {
+  if (count < 0 || (count > 0 && (!slots || !configs || !t || !status)))
+    return fail_with(ctx, CAROLI_EINVAL, std::string(who) + ": bad arguments");
   if (precision != CAROLI_DOUBLE && precision != CAROLI_SINGLE && precision != CAROLI_MIXED)
     return fail_with(ctx, CAROLI_EINVAL, "unknown precision");
-  if (!sys->vals) return fail_with(ctx, CAROLI_EINVAL, "no H values uploaded");
   for (int i = 0; i < count; ++i) {
+    System* sys = isys[i];
+    if (!sys) return fail_with(ctx, CAROLI_EINVAL, std::string(who) + ": unknown plan");
+    if (!sys->vals) return fail_with(ctx, CAROLI_EINVAL, "no H values uploaded");
     if (slots[i] < 0 || slots[i] >= (int)sys->slots.size() || !sys->slots[slots[i]].set)
       return fail_with(ctx, CAROLI_EINVAL, "energy slot without self-energies");
     if (configs[i] < 0 || configs[i] >= sys->nconfigs) return fail_with(ctx, CAROLI_EINVAL, "configuration out of range");
@@ -1572,16 +1583,20 @@ int caroli_solve_batch(caroli_ctx* ctx, int plan_id, int count, const int32_t* s
     ctx->last_ms = 0.0;
     ctx->last_launches = 0;
     ctx->factor_ms = ctx->root_ms = ctx->tail_ms = 0.0;
-    const int nb = (int)sys->plans.size();
     std::vector<JobSpec> specs;
-    specs.reserve((size_t)count * nb);
-    for (int i = 0; i < count; ++i)
-      for (int b = 0; b < nb; ++b) specs.push_back({b, slots[i], configs[i], sys->plans[b].get()});
+    std::vector<size_t> first(count + 1, 0);
+    for (int i = 0; i < count; ++i) {
+      System* sys = isys[i];
+      first[i] = specs.size();
+      for (int b = 0; b < (int)sys->plans.size(); ++b)
+        specs.push_back({b, slots[i], configs[i], sys->plans[b].get(), sys});
+    }
+    first[count] = specs.size();
     std::vector<JobOut> jo;
     ctx->fallbacks = 0;
     ctx->refine_iters = 0;
     ctx->refine_job_steps = ctx->refine_batch_steps = 0;
-    solve_jobs(ctx, sys, specs, (Mode)precision, jo);
+    solve_jobs(ctx, count ? isys[0] : nullptr, specs, (Mode)precision, jo);
     ctx->job_iters.clear();
     ctx->job_perturbed.clear();
     ctx->job_status.clear();
@@ -1593,8 +1608,8 @@ int caroli_solve_batch(caroli_ctx* ctx, int plan_id, int count, const int32_t* s
     for (int i = 0; i < count; ++i) {
       double sum = 0.0, e = 0.0;
       int32_t st = ST_OK;
-      for (int b = 0; b < nb; ++b) {
-        const JobOut& o = jo[(size_t)i * nb + b];
+      for (size_t q = first[i]; q < first[i + 1]; ++q) {
+        const JobOut& o = jo[q];
         sum += o.t;
         e += o.err;
         if (st == ST_OK) st = o.status >= 100 ? ST_OK : o.status;
@@ -1610,6 +1625,26 @@ int caroli_solve_batch(caroli_ctx* ctx, int plan_id, int count, const int32_t* s
   } catch (const std::exception& e) {
     return fail_with(ctx, CAROLI_EINVAL, e.what());
   }
+}
+
+}  // namespace
+
+extern "C" {
+
+int caroli_solve_batch(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots, const int32_t* configs,
+                       int precision, double* t, int32_t* status, double* err) {
+  System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
+  if (!sys) return fail_with(ctx, CAROLI_EINVAL, "caroli_solve_batch: bad arguments");
+  std::vector<System*> isys(std::max(count, 0), sys);
+  return solve_instances(ctx, isys, count, slots, configs, precision, t, status, err, "caroli_solve_batch");
+}
+
+int caroli_solve_multi(caroli_ctx* ctx, int count, const int32_t* plan_ids, const int32_t* slots,
+                       const int32_t* configs, int precision, double* t, int32_t* status, double* err) {
+  if (!ctx || count < 0 || (count > 0 && !plan_ids)) return fail_with(ctx, CAROLI_EINVAL, "caroli_solve_multi: bad arguments");
+  std::vector<System*> isys(count);
+  for (int i = 0; i < count; ++i) isys[i] = get_system(ctx, plan_ids[i]);
+  return solve_instances(ctx, isys, count, slots, configs, precision, t, status, err, "caroli_solve_multi");
 }
 
 int caroli_last_phases(const caroli_ctx* ctx, double* factor_ms, double* root_ms, double* tail_ms) {

@@ -181,6 +181,21 @@ class NestedTwoTerminal:
         return checked(list(energies), options, run)
 
 
+def solve_systems(items, precision=Precision.MIXED):
+    """``(T, status, err)`` for ``(system, sigma, config)`` items of possibly different systems
+    (sizes, trees, leads) in one GPU batch; every system must be on the same device. The
+    reference calls ``transmission_with`` system by system (nested.rs:682)."""
+    if not items:
+        return np.zeros(0), np.zeros(0, np.int32), np.zeros(0)
+    device = items[0][0].device
+    if any(s.device != device for s, _, _ in items):
+        raise ValueError("solve_systems: systems on different devices")
+    plans = [s.plan() for s, _, _ in items]
+    slots = [s._slot(sig) for s, sig, _ in items]
+    configs = [c for _, _, c in items]
+    return context(device).solve_multi(plans, slots, configs, int(precision))
+
+
 def _result(t, status, energy):
     if status == _native.OK:
         return float(t)

@@ -150,6 +150,14 @@ int caroli_derivs_upload(caroli_ctx* ctx, int plan_id, int nparams, const double
 int caroli_transmission_with_grad(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots, const int32_t* configs,
                                   double* t, int32_t* status, double* dt_dv, double* dt_dp);
 
+/* caroli_solve_batch over instances of several systems (plans) at once: instance i is
+ * (plan_ids[i], slots[i], configs[i]), slots and configurations of that plan. Systems of different
+ * sizes and trees (e.g. ribbons of many widths and lengths) share every level-synchronous launch.
+ * The reference solves each system on its own (NestedTwoTerminal::transmission_with, nested.rs:682);
+ * this batches a caller's loop over systems. */
+int caroli_solve_multi(caroli_ctx* ctx, int count, const int32_t* plan_ids, const int32_t* slots,
+                       const int32_t* configs, int precision, double* t, int32_t* status, double* err);
+
 /* Device time of the last caroli_solve_batch (ms), and kernels it launched. */
 int caroli_last_timing(const caroli_ctx* ctx, double* device_ms, int64_t* launches);
 

@@ -111,3 +111,24 @@ def gradient_bhz(length, width, configs=1, anderson=0.02, concentration=0.1, exc
         _, _, (v1, v0, _) = merge_patterns([h1, h0, base])
         derivs.append([v1 - v0])
     return sys_, derivs
+
+
+def graphene_ribbons(count, seed=1, widths=(8, 24), lengths=(12, 40), w=1.0):
+    """Graphene zigzag ribbons of uneven sizes, as the many-ribbon workload draws them (widths and
+    lengths from xoshiro seed_from_u64(seed), Anderson w(u - 0.5) per site from
+    seed_from_u64(1 000 003 seed + ribbon), the benchmark's convention of caroli-bench/src/main.rs:124),
+    at test sizes. Returns the NestedTwoTerminal of each ribbon."""
+    from caroli_gb300.disorder import Xoshiro256
+
+    rng = Xoshiro256.seed_from_u64(seed)
+    out = []
+    for r in range(count):
+        width = rng.integer(*widths)
+        length = rng.integer(*lengths)
+        clean = graphene()
+        region = Region.cuboid(clean.lattice, [length, width, 0])
+        subs = len(clean.lattice.sublattices)
+        pot = bench_disorder(seed, r, length, width, subs, w)
+        device = clean.with_onsite_term(ScalarPotential(pot, width, subs, 1))
+        out.append(NestedTwoTerminal.from_model(device, clean, region, 0))
+    return out

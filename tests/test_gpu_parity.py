@@ -149,3 +149,22 @@ def test_tensor_core_updates_match_cuda_cores():
         a, b = out[True][1][k], out[False][1][k]
         assert abs(a - ref) <= 1e-8 and abs(b - ref) <= 1e-8, (s.energy, c, a, b, ref)
     assert out[True][2] <= out[False][2] + 4, (out[True][2], out[False][2])
+
+
+def test_uneven_ribbons_in_one_batch():
+    """Ribbons of different widths and lengths (different trees, roots and leads) in one batch:
+    each T equals the oracle's, in FP64 and mixed precision."""
+    from caroli_gb300 import solve_systems
+    from systems import graphene_ribbons
+
+    ribbons = graphene_ribbons(6)
+    items = []
+    for k, sys_ in enumerate(ribbons):
+        for e in (-0.4, 0.1 + 0.05 * k, 0.45):
+            items.append((sys_, sys_.self_energies(e), 0))
+    for precision, tol in ((Precision.DOUBLE, 1e-10), (Precision.MIXED, 1e-8)):
+        t, st, _ = solve_systems(items, precision)
+        assert (st == 0).all(), st
+        for (sys_, s, c), tv in zip(items, t):
+            ref = oracle_T(sys_, s, config=c)
+            assert abs(tv - ref) <= tol * (1 + abs(ref)), (precision, s.energy, tv, ref)
