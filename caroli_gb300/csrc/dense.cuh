@@ -285,8 +285,10 @@ __global__ void __launch_bounds__(256) inv_update_kernel(const InvTask* __restri
 // Barriers: bfull (B' copied), bempty (its MMAs done), tfull[a] (accumulator a ready), tempty[a]
 // (accumulator a drained). Every wait is bounded; one that runs out sets ST_TIMEOUT for the
 // solve and stops the CTA after the copies and MMAs it issued have drained.
-// grid (row tiles, matrices), 192 threads.
+// grid (row tiles, matrices, column groups), 192 threads: a CTA walks TCU_GROUP column tiles,
+// so a few very wide fronts still spread over many CTAs.
 constexpr int TCU_THREADS = 192;
+constexpr int TCU_GROUP = 8;
 constexpr int TCU_SMEM = 2 * TCU_A_BYTES + 2 * TCU_B_BYTES + 1024;
 constexpr uint32_t TCU_WAIT = 1u << 22;
 
@@ -314,7 +316,9 @@ __global__ void __launch_bounds__(TCU_THREADS) tc_update_kernel(const InvTask* _
   float2* A = static_cast<float2*>(t.a);
   const unsigned char* bt = static_cast<const unsigned char*>(t.bt);
   const int64_t ld = t.ld;
-  const int tiles = (rest + TCU_COLS - 1) / TCU_COLS;
+  const int tile0 = blockIdx.z * TCU_GROUP;
+  const int tiles = min((rest + TCU_COLS - 1) / TCU_COLS - tile0, TCU_GROUP);
+  if (tiles <= 0) return;
   if (w == 0) tc::tmem_alloc(&tslot, 2 * TCU_COLS);
   if (tid == 0) {
     tc::mbar_init(&bfull, 1);
@@ -354,8 +358,9 @@ __global__ void __launch_bounds__(TCU_THREADS) tc_update_kernel(const InvTask* _
       for (int ct = 0; ct < tiles && !*abort_v; ++ct) {
         if (ct >= 1 && !tc::mbar_wait(&bempty, (uint32_t)((ct - 1) & 1), TCU_WAIT)) { fail(); break; }
         tc::mbar_arrive_expect_tx(&bfull, 2 * TCU_B_BYTES);
-        tc::bulk_copy_g2s(b_hi, bt + (size_t)ct * 2 * TCU_B_BYTES, TCU_B_BYTES, &bfull);
-        tc::bulk_copy_g2s(b_lo, bt + (size_t)ct * 2 * TCU_B_BYTES + TCU_B_BYTES, TCU_B_BYTES, &bfull);
+        const size_t tile = (size_t)(tile0 + ct) * 2 * TCU_B_BYTES;
+        tc::bulk_copy_g2s(b_hi, bt + tile, TCU_B_BYTES, &bfull);
+        tc::bulk_copy_g2s(b_lo, bt + tile + TCU_B_BYTES, TCU_B_BYTES, &bfull);
         ++copies;
       }
   } else if (w == 1) {
@@ -391,7 +396,7 @@ __global__ void __launch_bounds__(TCU_THREADS) tc_update_kernel(const InvTask* _
     const bool pivot_row = gi >= k0 && gi < k0 + kb;
     float* Af = reinterpret_cast<float*>(A) + (r2 & 1);
     for (int ct = 0; ct < tiles; ++ct) {
-      const int a = ct & 1, r0 = ct * TCU_COLS;
+      const int a = ct & 1, r0 = (tile0 + ct) * TCU_COLS;
       float old[TCU_COLS];
 #pragma unroll
       for (int j = 0; j < TCU_COLS; ++j) {

@@ -35,6 +35,7 @@ constexpr double PIVOT_TOL_F32 = 1e-5;   // caroli-dense/src/field.rs:111
 constexpr int SMALL_MAX_F64 = 64;        // fronts up to this size run in one CTA's shared memory
 constexpr int SMALL_MAX_F32 = 96;
 constexpr int SMEM_LIMIT = 220 * 1024;   // dynamic shared memory a kernel may request
+constexpr int MIXED_MAX_CHANNELS = 96;    // CAROLI_MIXED block solves with more channels run in FP64
 
 struct CudaError {
   cudaError_t e;
@@ -295,6 +296,9 @@ size_t panel_smem(int pmax, size_t vbytes) {
 template <typename F> void in_pieces(size_t count, F fn) {
   for (size_t first = 0; first < count; first += 65535) fn(first, std::min<size_t>(65535, count - first));
 }
+template <typename F> void in_pieces_of(size_t count, size_t piece, F fn) {
+  for (size_t first = 0; first < count; first += piece) fn(first, std::min<size_t>(piece, count - first));
+}
 
 struct LevelRange {
   size_t tiny0, tiny_n;  // fronts of at most TINY_MAX variables (one warp each)
@@ -435,40 +439,43 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
     constexpr int CB = decltype(cbt)::value;
     for (int L = 0; L < nlev; ++L) {
       const int nt = hcount[2 * L], nr = hcount[2 * L + 1];
-      if (nt)
+      in_pieces_of((size_t)nt, (size_t)65535 * TINY_WARPS, [&](size_t f0, size_t c) {  // grid y <= 65535
         launch(K_REF_FWD, 0.0, 0.0, [&] {
-          sweep_tiny_fwd_kernel<CB><<<dim3((unsigned)((nt + TINY_WARPS - 1) / TINY_WARPS), cchunks), 256, 0, s>>>(
-              drd, ctasks + lr[L].tiny0, nt, src);
+          sweep_tiny_fwd_kernel<CB><<<dim3(cchunks, (unsigned)((c + TINY_WARPS - 1) / TINY_WARPS)), 256, 0, s>>>(
+              drd, ctasks + lr[L].tiny0 + f0, (int)c, src);
         });
+      });
       if (!nr) continue;
       const size_t sm = (size_t)std::max(1, lr[L].max_ne) * CB * sizeof(float2);
       const unsigned tiles = (unsigned)((lr[L].max_n + SW_ROWS - 1) / SW_ROWS);
       in_pieces((size_t)nr, [&](size_t f0, size_t c) {
         launch(K_REF_FWD, 0.0, sweep_bytes * 0.5 / nlev, [&] {
-          sweep_rows_fwd_kernel<CB><<<dim3((unsigned)c, tiles, cchunks), 256, sm, s>>>(drd, ctasks + lr[L].first + f0,
+          sweep_rows_fwd_kernel<CB><<<dim3(cchunks, tiles, (unsigned)c), 256, sm, s>>>(drd, ctasks + lr[L].first + f0,
                                                                                      src);
         });
       });
     }
     const int nj = hcount[nseg];
-    if (nj)
+    in_pieces((size_t)nj, [&](size_t f0, size_t c) {
       launch(K_REF_ROOT, 0.0, 0.0, [&] {
-        sweep_root_kernel<CB><<<dim3((unsigned)nj, cchunks), 256, (size_t)max_root * CB * sizeof(float2), s>>>(
-            drd, cjobs, src, dst);
+        sweep_root_kernel<CB><<<dim3(cchunks, (unsigned)c), 256, (size_t)max_root * CB * sizeof(float2), s>>>(
+            drd, cjobs + f0, src, dst);
       });
+    });
     for (int L = nlev - 1; L >= 0; --L) {
       const int nt = hcount[2 * L], nr = hcount[2 * L + 1];
-      if (nt)
+      in_pieces_of((size_t)nt, (size_t)65535 * TINY_WARPS, [&](size_t f0, size_t c) {  // grid y <= 65535
         launch(K_REF_BWD, 0.0, 0.0, [&] {
-          sweep_tiny_bwd_kernel<CB><<<dim3((unsigned)((nt + TINY_WARPS - 1) / TINY_WARPS), cchunks), 256, 0, s>>>(
-              drd, ctasks + lr[L].tiny0, nt, src, dst);
+          sweep_tiny_bwd_kernel<CB><<<dim3(cchunks, (unsigned)((c + TINY_WARPS - 1) / TINY_WARPS)), 256, 0, s>>>(
+              drd, ctasks + lr[L].tiny0 + f0, (int)c, src, dst);
         });
+      });
       if (!nr) continue;
       const size_t sm = (size_t)std::max(1, lr[L].max_n) * CB * sizeof(float2);
       const unsigned tiles = (unsigned)((std::max(1, lr[L].max_ne) + SW_ROWS - 1) / SW_ROWS);
       in_pieces((size_t)nr, [&](size_t f0, size_t c) {
         launch(K_REF_BWD, 0.0, sweep_bytes * 0.5 / nlev, [&] {
-          sweep_rows_bwd_kernel<CB><<<dim3((unsigned)c, tiles, cchunks), 256, sm, s>>>(drd, ctasks + lr[L].first + f0,
+          sweep_rows_bwd_kernel<CB><<<dim3(cchunks, tiles, (unsigned)c), 256, sm, s>>>(drd, ctasks + lr[L].first + f0,
                                                                                      src, dst);
         });
       });
@@ -963,7 +970,9 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
         in_pieces(count, [&](size_t f0, size_t c) {
           launch(ucls, uper * c / count, ubper * c / count, [&] {
             if (std::is_same<TT, float>::value && ctx->tensor_cores)
-              tc_update_kernel<<<dim3((unsigned)((nmax + TCU_ROWS - 1) / TCU_ROWS), (unsigned)c), TCU_THREADS, TCU_SMEM, s>>>(
+              tc_update_kernel<<<dim3((unsigned)((nmax + TCU_ROWS - 1) / TCU_ROWS), (unsigned)c,
+                                      (unsigned)((nmax + TCU_COLS * TCU_GROUP - 1) / (TCU_COLS * TCU_GROUP))),
+                                 TCU_THREADS, TCU_SMEM, s>>>(
                   dinv + first + f0, k0, status);
             else
               inv_update_kernel<TT><<<dim3(rt, rt, (unsigned)c), 256, 0, s>>>(dinv + first + f0, k0);
@@ -1149,12 +1158,35 @@ void solve_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs,
   } else if (mode == MODE_SINGLE) {
     solve_with_delays<float, double>(ctx, sys, specs, mode, out);
   } else {
-    run_jobs<float, float>(ctx, sys, specs, mode, out);
+    // Block solves with many right-lead channels go to the FP64 path directly: the refinement
+    // carries one right-hand side per channel through every sweep, and past MIXED_MAX_CHANNELS
+    // that costs more than the FP64 factorization it replaces (a 32 x 32-site cubic lead has
+    // hundreds of open channels; the two-dimensional ribbons have a few).
+    std::vector<JobSpec> few;
+    std::vector<size_t> few_idx, many_idx;
+    for (size_t j = 0; j < specs.size(); ++j) {
+      const int c = specs[j].sys->slots[specs[j].slot].channels[specs[j].block];
+      if (c > MIXED_MAX_CHANNELS) many_idx.push_back(j);
+      else { few.push_back(specs[j]); few_idx.push_back(j); }
+    }
+    out.assign(specs.size(), JobOut{});
+    if (!few.empty()) {
+      std::vector<JobOut> fo;
+      run_jobs<float, float>(ctx, sys, few, mode, fo);
+      for (size_t q = 0; q < few_idx.size(); ++q) out[few_idx[q]] = std::move(fo[q]);
+    }
+    if (!many_idx.empty()) {
+      std::vector<JobSpec> many;
+      for (size_t j : many_idx) many.push_back(specs[j]);
+      std::vector<JobOut> mo;
+      solve_with_delays<double, double>(ctx, sys, many, MODE_DOUBLE, mo);
+      for (size_t q = 0; q < many_idx.size(); ++q) out[many_idx[q]] = std::move(mo[q]);
+    }
     // Points the reduced precision could not resolve are computed in double precision
     // (precision.rs:102-115 does the same for failed points).
     std::vector<JobSpec> again;
     std::vector<size_t> idx;
-    for (size_t j = 0; j < specs.size(); ++j)
+    for (size_t j : few_idx)
       if (out[j].status != ST_OK) {
         again.push_back(specs[j]);
         idx.push_back(j);

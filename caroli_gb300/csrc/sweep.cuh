@@ -47,11 +47,11 @@ template <int CB>
 __global__ void __launch_bounds__(256) sweep_tiny_fwd_kernel(const RefineDesc* __restrict__ rd,
                                                              const Task* __restrict__ tasks, int ntasks, int src) {
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int ti = blockIdx.x * TINY_WARPS + w;
+  const int ti = blockIdx.y * TINY_WARPS + w;
   if (ti >= ntasks) return;
   const Task tk = tasks[ti];
   const RefineDesc& R = rd[tk.job];
-  const int j0 = blockIdx.y * CB;
+  const int j0 = blockIdx.x * CB;
   if (sweep_idle(R, src) || j0 >= R.c) return;
   const FrontDesc& f = *tk.fd;
   const int n = f.n, ne = f.ne;
@@ -88,11 +88,11 @@ __global__ void __launch_bounds__(256) sweep_tiny_bwd_kernel(const RefineDesc* _
                                                              const Task* __restrict__ tasks, int ntasks, int src,
                                                              int dst) {
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int ti = blockIdx.x * TINY_WARPS + w;
+  const int ti = blockIdx.y * TINY_WARPS + w;
   if (ti >= ntasks) return;
   const Task tk = tasks[ti];
   const RefineDesc& R = rd[tk.job];
-  const int j0 = blockIdx.y * CB;
+  const int j0 = blockIdx.x * CB;
   if (sweep_idle(R, src) || j0 >= R.c) return;
   const FrontDesc& f = *tk.fd;
   const int n = f.n, ne = f.ne, nb = n - ne;
@@ -127,15 +127,16 @@ __global__ void __launch_bounds__(256) sweep_tiny_bwd_kernel(const RefineDesc* _
 }
 
 // ---- larger fronts: row tiles of 64, the inner dimension split four ways -----------------------
-// Forward: grid (tasks, row tiles, column chunks); dynamic shared memory z_e (max ne x CB).
+// Forward: grid (column chunks, row tiles, tasks), the chunks of a tile adjacent so that their
+// re-reads of the same factor rows come from L2; dynamic shared memory z_e (max ne x CB).
 template <int CB>
 __global__ void __launch_bounds__(256) sweep_rows_fwd_kernel(const RefineDesc* __restrict__ rd,
                                                              const Task* __restrict__ tasks, int src) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ float2 part[SW_SLICES - 1][SW_ROWS][CB];
-  const Task tk = tasks[blockIdx.x];
+  const Task tk = tasks[blockIdx.z];
   const RefineDesc& R = rd[tk.job];
-  const int j0 = blockIdx.z * CB;
+  const int j0 = blockIdx.x * CB;
   if (sweep_idle(R, src) || j0 >= R.c) return;
   const FrontDesc& f = *tk.fd;
   const int n = f.n, ne = f.ne;
@@ -187,16 +188,16 @@ __global__ void __launch_bounds__(256) sweep_rows_fwd_kernel(const RefineDesc* _
   }
 }
 
-// Backward: grid (tasks, row tiles of the ne rows, column chunks); dynamic shared memory x_b
+// Backward: grid (column chunks, row tiles of the ne rows, tasks); dynamic shared memory x_b
 // (max nb x CB).
 template <int CB>
 __global__ void __launch_bounds__(256) sweep_rows_bwd_kernel(const RefineDesc* __restrict__ rd,
                                                              const Task* __restrict__ tasks, int src, int dst) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ float2 part[SW_SLICES - 1][SW_ROWS][CB];
-  const Task tk = tasks[blockIdx.x];
+  const Task tk = tasks[blockIdx.z];
   const RefineDesc& R = rd[tk.job];
-  const int j0 = blockIdx.z * CB;
+  const int j0 = blockIdx.x * CB;
   if (sweep_idle(R, src) || j0 >= R.c) return;
   const FrontDesc& f = *tk.fd;
   const int n = f.n, ne = f.ne, nb = n - ne;
@@ -247,13 +248,13 @@ __global__ void __launch_bounds__(256) sweep_rows_bwd_kernel(const RefineDesc* _
 }
 
 // ---- root: x = F_root^-1 z (the conjugate transpose for the adjoint) ---------------------------
-// grid (jobs, column chunks); dynamic shared memory z (m x CB).
+// grid (column chunks, jobs); dynamic shared memory z (m x CB).
 template <int CB>
 __global__ void __launch_bounds__(256) sweep_root_kernel(const RefineDesc* __restrict__ rd, const int32_t* __restrict__ jobs,
                                                          int src, int dst) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const RefineDesc& R = rd[jobs ? jobs[blockIdx.x] : blockIdx.x];
-  const int j0 = blockIdx.y * CB;
+  const RefineDesc& R = rd[jobs ? jobs[blockIdx.y] : blockIdx.y];
+  const int j0 = blockIdx.x * CB;
   if (sweep_idle(R, src) || j0 >= R.c) return;
   const double2* rin = sweep_src(R, src);
   float2* dout = sweep_dst(R, dst);

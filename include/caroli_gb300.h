@@ -48,7 +48,9 @@ enum {
   CAROLI_DOUBLE = 0, /* complex f64 throughout */
   CAROLI_SINGLE = 1, /* complex f32 fronts, f64 root and trace, unrefined (Precision::Single) */
   CAROLI_MIXED = 2   /* complex f32 fronts as a preconditioner of FP64 iterative refinement of the
-                        whole solve (no counterpart; Precision gains a Mixed variant) */
+                        whole solve (no counterpart; Precision gains a Mixed variant). Block solves
+                        whose right lead has more than 96 open channels (one refinement right-hand
+                        side each) take the FP64 path instead, which is faster there. */
 };
 
 int caroli_ctx_create(int device_ordinal, caroli_ctx** out);
