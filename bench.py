@@ -283,10 +283,18 @@ def run_ours(args):
                               for s in sigmas)
     h2d += 2 * 4 * nsolve
     d2h = nsolve * (8 + 4 + 8)
+    def e2e_step():
+        plan.upload_values(values)
+        for slot, s in enumerate(sigmas):
+            plan.upload_sigma(sys_._slot_of[id(s)][0], s.energy, s.blocks, s.w_right())
+        sys_.solve_batch(S, C, Precision.MIXED)
+
+    for _ in range(max(1, args.warmup)):  # untimed: the FP64 comparison above replaced the cached task lists
+        e2e_step()
     ctx.region_begin()
     e0 = time.perf_counter()
     for _ in range(args.steps):
-        plan.upload_values(list(values))
+        plan.upload_values(values)
         for slot, s in enumerate(sigmas):
             plan.upload_sigma(sys_._slot_of[id(s)][0], s.energy, s.blocks, s.w_right())
         sys_.solve_batch(S, C, Precision.MIXED)

@@ -192,7 +192,13 @@ class Plan:
         return n, ne, lv
 
     def upload_values(self, values):
-        v = np.ascontiguousarray(np.stack(values), dtype=np.complex128)
+        """H values of every configuration: an (nconfigs, nnz) complex128 array (used in place
+        when C-contiguous) or a list of per-configuration arrays."""
+        if isinstance(values, np.ndarray) and values.ndim == 2 and values.dtype == np.complex128 \
+                and values.flags.c_contiguous:
+            v = values
+        else:
+            v = np.ascontiguousarray(np.stack(values), dtype=np.complex128)
         self.ctx.check(self.ctx.lib.caroli_values_upload(self.ctx.h, self.id, v.shape[0], ptr(v)))
 
     def upload_sigma(self, slot, energy, sigmas, w_right=None):

@@ -130,6 +130,7 @@ struct System {
   std::vector<std::unique_ptr<DevPlan>> plans;  // static plan per block
   std::vector<DevBlock> blocks;
   double2* vals = nullptr;
+  size_t vals_count = 0;  // elements allocated at vals
   int nconfigs = 0;
   double2* dvals = nullptr;  // dH/dp of every configuration: [config][param][nnz]
   int nparams = 0;
@@ -1450,10 +1451,16 @@ int caroli_values_upload(caroli_ctx* ctx, int plan_id, int nconfigs, const doubl
   if (!sys || nconfigs <= 0 || !values) return fail_with(ctx, CAROLI_EINVAL, "caroli_values_upload: bad arguments");
   try {
     CK(cudaSetDevice(ctx->device));
-    cudaFree(sys->vals);
-    sys->vals = nullptr;
     const size_t nnz = (size_t)sys->desc.row_ptr[sys->desc.n];
-    sys->vals = upload_c64(values, nnz * (size_t)nconfigs, ctx->stream);
+    const size_t count = nnz * (size_t)nconfigs;
+    if (!sys->vals || sys->vals_count != count) {  // the same size re-uses the buffer
+      cudaFree(sys->vals);
+      sys->vals = nullptr;
+      sys->vals_count = 0;
+      sys->vals = dalloc<double2>(std::max<size_t>(count, 1));
+      sys->vals_count = count;
+    }
+    if (count) CK(cudaMemcpyAsync(sys->vals, values, count * sizeof(double2), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     sys->nconfigs = nconfigs;
     return CAROLI_OK;
@@ -1543,12 +1550,30 @@ int caroli_sigma_upload(caroli_ctx* ctx, int plan_id, int slot, double energy, c
     CK(cudaSetDevice(ctx->device));
     if ((int)sys->slots.size() <= slot) sys->slots.resize(slot + 1);
     SigmaSlot& sg = sys->slots[slot];
-    for (auto* v : {&sg.sl, &sg.sr, &sg.gl, &sg.gr, &sg.wr}) {
-      for (auto* p : *v) cudaFree(p);
-      v->clear();
+    // A slot keeps its device buffers (sized by the blocks' lead slices, W_R for up to nr
+    // channels), so uploading the next energy into it only copies.
+    const size_t nblocks = sys->plans.size();
+    if (sg.sl.size() != nblocks) {
+      for (auto* v : {&sg.sl, &sg.sr, &sg.gl, &sg.gr, &sg.wr}) {
+        for (auto* p : *v) cudaFree(p);
+        v->clear();
+      }
+      for (size_t b = 0; b < nblocks; ++b) {
+        const size_t nl = sys->plans[b]->host.nl, nr = sys->plans[b]->host.nr;
+        sg.sl.push_back(dalloc<double2>(std::max<size_t>(nl * nl, 1)));
+        sg.sr.push_back(dalloc<double2>(std::max<size_t>(nr * nr, 1)));
+        sg.gl.push_back(dalloc<double2>(std::max<size_t>(nl * nl, 1)));
+        sg.gr.push_back(dalloc<double2>(std::max<size_t>(nr * nr, 1)));
+        sg.wr.push_back(dalloc<double2>(std::max<size_t>(nr * nr, 1)));
+      }
     }
-    sg.channels.clear();
-    for (size_t b = 0; b < sys->plans.size(); ++b) {
+    sg.channels.assign(nblocks, 0);
+    sg.set = false;
+    std::vector<std::vector<double>> keep;  // host data of the asynchronous copies
+    auto put = [&](double2* d, const double* h, size_t count) {
+      if (count) CK(cudaMemcpyAsync(d, h, count * sizeof(double2), cudaMemcpyHostToDevice, ctx->stream));
+    };
+    for (size_t b = 0; b < nblocks; ++b) {
       const FrontPlan& p = sys->plans[b]->host;
       const size_t nl = p.nl, nr = p.nr;
       // Γ = i (Σ - Σ^†) (caroli-green/src/lib.rs:67-71).
@@ -1573,14 +1598,17 @@ int caroli_sigma_upload(caroli_ctx* ctx, int plan_id, int slot, double energy, c
       } else {
         ch = gamma_factor(gr, nr, wr);
       }
-      sg.channels.push_back(ch);
-      sg.wr.push_back(upload_c64(wr.data(), nr * (size_t)ch, ctx->stream));
-      sg.sl.push_back(upload_c64(sigma_l[b], nl * nl, ctx->stream));
-      sg.sr.push_back(upload_c64(sigma_r[b], nr * nr, ctx->stream));
-      sg.gl.push_back(upload_c64(gl.data(), nl * nl, ctx->stream));
-      sg.gr.push_back(upload_c64(gr.data(), nr * nr, ctx->stream));
-      CK(cudaStreamSynchronize(ctx->stream));
+      sg.channels[b] = ch;
+      put(sg.wr[b], wr.data(), nr * (size_t)ch);
+      put(sg.sl[b], sigma_l[b], nl * nl);
+      put(sg.sr[b], sigma_r[b], nr * nr);
+      put(sg.gl[b], gl.data(), nl * nl);
+      put(sg.gr[b], gr.data(), nr * nr);
+      keep.push_back(std::move(wr));
+      keep.push_back(std::move(gl));
+      keep.push_back(std::move(gr));
     }
+    CK(cudaStreamSynchronize(ctx->stream));
     sg.energy = energy;
     sg.set = true;
     return CAROLI_OK;
