@@ -280,19 +280,20 @@ __global__ void __launch_bounds__(256) inv_update_kernel(const InvTask* __restri
 // A CTA takes 64 complex rows of one matrix: all warps stage A' from the panel columns, then
 //   warp 0 (one thread) bulk-copies the B' tiles, written by the panel kernel, into shared memory;
 //   warp 1 (one thread) issues the MMAs, alternating two 64-column accumulators in tensor memory;
-//   warps 2-5 (one per 32-lane quarter of tensor memory) add each finished tile to the old values
-//   (zero on the pivot rows) while the next tile is copied and multiplied.
+//   warps 2-9 (two per 32-lane quarter of tensor memory, 32 columns each) add each finished tile to
+//   the old values (zero on the pivot rows) while the next tile is copied and multiplied.
 // Barriers: bfull (B' copied), bempty (its MMAs done), tfull[a] (accumulator a ready), tempty[a]
 // (accumulator a drained). Every wait is bounded; one that runs out sets ST_TIMEOUT for the
 // solve and stops the CTA after the copies and MMAs it issued have drained.
-// grid (row tiles, matrices, column groups), 192 threads: a CTA walks TCU_GROUP column tiles,
+// grid (row tiles, matrices, column groups), 320 threads: a CTA walks TCU_GROUP column tiles,
 // so a few very wide fronts still spread over many CTAs.
-constexpr int TCU_THREADS = 192;
+constexpr int TCU_EPI_WARPS = 8;
+constexpr int TCU_THREADS = 32 * (2 + TCU_EPI_WARPS);
 constexpr int TCU_GROUP = 8;
 constexpr int TCU_SMEM = 2 * TCU_A_BYTES + 2 * TCU_B_BYTES + 1024;
 constexpr uint32_t TCU_WAIT = 1u << 22;
 
-__global__ void __launch_bounds__(TCU_THREADS) tc_update_kernel(const InvTask* __restrict__ tasks, int k0,
+__global__ void __launch_bounds__(TCU_THREADS, 2) tc_update_kernel(const InvTask* __restrict__ tasks, int k0,
                                                                 int32_t* __restrict__ status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ uint32_t tslot;
@@ -325,8 +326,8 @@ __global__ void __launch_bounds__(TCU_THREADS) tc_update_kernel(const InvTask* _
     tc::mbar_init(&bempty, 1);
     tc::mbar_init(&tfull[0], 1);
     tc::mbar_init(&tfull[1], 1);
-    tc::mbar_init(&tempty[0], 4);
-    tc::mbar_init(&tempty[1], 4);
+    tc::mbar_init(&tempty[0], TCU_EPI_WARPS);
+    tc::mbar_init(&tempty[1], TCU_EPI_WARPS);
     abort_flag = 0;
   }
   // A' from the panel columns of this tile's rows (zero past n and past 2 kb): a complex row and
@@ -388,18 +389,20 @@ __global__ void __launch_bounds__(TCU_THREADS) tc_update_kernel(const InvTask* _
       }
     }
   } else {
-    // Epilogue: this warp's quarter of the 128 real rows; thread row r2, complex row i0 + r2 / 2.
-    const int q = w & 3;
+    // Epilogue: this warp's quarter of the 128 real rows (thread row r2, complex row i0 + r2 / 2)
+    // and half of the 64 columns of each tile.
+    constexpr int HC = TCU_COLS / 2;
+    const int q = w & 3, h = (w - 2) >> 2;
     const int r2 = 32 * q + lane;
     const int gi = i0 + (r2 >> 1);
     const bool row_in = gi < n;
     const bool pivot_row = gi >= k0 && gi < k0 + kb;
     float* Af = reinterpret_cast<float*>(A) + (r2 & 1);
     for (int ct = 0; ct < tiles; ++ct) {
-      const int a = ct & 1, r0 = (tile0 + ct) * TCU_COLS;
-      float old[TCU_COLS];
+      const int a = ct & 1, r0 = (tile0 + ct) * TCU_COLS + h * HC;
+      float old[HC];
 #pragma unroll
-      for (int j = 0; j < TCU_COLS; ++j) {
+      for (int j = 0; j < HC; ++j) {
         const int r = r0 + j;
         old[j] = 0.f;
         if (row_in && !pivot_row && r < rest) old[j] = Af[2 * (gi + (int64_t)(r < k0 ? r : r + kb) * ld)];
@@ -411,11 +414,11 @@ __global__ void __launch_bounds__(TCU_THREADS) tc_update_kernel(const InvTask* _
         break;
       }
       tc::fence_after_sync();
-      float v[TCU_COLS];
+      float v[HC];
 #pragma unroll
-      for (int c0 = 0; c0 < TCU_COLS; c0 += 16) {
+      for (int c0 = 0; c0 < HC; c0 += 16) {
         float part[16];
-        tc::tmem_ld16(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(a * TCU_COLS + c0), part);
+        tc::tmem_ld16(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(a * TCU_COLS + h * HC + c0), part);
 #pragma unroll
         for (int i = 0; i < 16; ++i) v[c0 + i] = part[i];
       }
@@ -424,7 +427,7 @@ __global__ void __launch_bounds__(TCU_THREADS) tc_update_kernel(const InvTask* _
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(&tempty[a]);
 #pragma unroll
-      for (int j = 0; j < TCU_COLS; ++j) {
+      for (int j = 0; j < HC; ++j) {
         const int r = r0 + j;
         if (row_in && r < rest) Af[2 * (gi + (int64_t)(r < k0 ? r : r + kb) * ld)] = old[j] + v[j];
       }
