@@ -287,7 +287,7 @@ __global__ void __launch_bounds__(256) inv_update_kernel(const InvTask* __restri
 // solve and stops the CTA after the copies and MMAs it issued have drained.
 // grid (row tiles, matrices, column groups), 320 threads: a CTA walks TCU_GROUP column tiles,
 // so a few very wide fronts still spread over many CTAs.
-constexpr int TCU_EPI_WARPS = 8;
+constexpr int TCU_EPI_WARPS = 16;
 constexpr int TCU_THREADS = 32 * (2 + TCU_EPI_WARPS);
 constexpr int TCU_GROUP = 8;
 constexpr int TCU_SMEM = 2 * TCU_A_BYTES + 2 * TCU_B_BYTES + 1024;
@@ -391,7 +391,7 @@ __global__ void __launch_bounds__(TCU_THREADS, 2) tc_update_kernel(const InvTask
   } else {
     // Epilogue: this warp's quarter of the 128 real rows (thread row r2, complex row i0 + r2 / 2)
     // and half of the 64 columns of each tile.
-    constexpr int HC = TCU_COLS / 2;
+    constexpr int HC = TCU_COLS / (TCU_EPI_WARPS / 4);
     const int q = w & 3, h = (w - 2) >> 2;
     const int r2 = 32 * q + lane;
     const int gi = i0 + (r2 >> 1);
