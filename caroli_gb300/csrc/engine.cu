@@ -303,6 +303,7 @@ template <typename F> void in_pieces_of(size_t count, size_t piece, F fn) {
 
 struct LevelRange {
   size_t tiny0, tiny_n;  // fronts of at most TINY_MAX variables (one warp each)
+  size_t mid0, mid_n;    // fronts of at most 64 variables (one warp each, two rows per lane)
   size_t first, count;   // the others
   int max_n;
   int max_ne;            // bound on the eliminated variables of the others
@@ -407,13 +408,14 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
   const unsigned rows = (unsigned)((max_blk + 255) / 256);
   const unsigned cols = (unsigned)std::max(1, cmax);
   // Task segments (per level: tiny fronts, then the others) and their compacted copies.
-  const int nseg = 2 * nlev;
+  const int nseg = 3 * nlev;
   std::vector<TaskSeg> segs(nseg);
   int64_t seg_max = 0;
   for (int L = 0; L < nlev; ++L) {
-    segs[2 * L] = {(int64_t)lr[L].tiny0, (int64_t)lr[L].tiny_n};
-    segs[2 * L + 1] = {(int64_t)lr[L].first, (int64_t)lr[L].count};
-    seg_max = std::max<int64_t>(seg_max, std::max(lr[L].tiny_n, lr[L].count));
+    segs[3 * L] = {(int64_t)lr[L].tiny0, (int64_t)lr[L].tiny_n};
+    segs[3 * L + 1] = {(int64_t)lr[L].mid0, (int64_t)lr[L].mid_n};
+    segs[3 * L + 2] = {(int64_t)lr[L].first, (int64_t)lr[L].count};
+    seg_max = std::max<int64_t>(seg_max, std::max(std::max(lr[L].tiny_n, lr[L].mid_n), lr[L].count));
   }
   size_t ntask_all = 0;
   for (const auto& sg : segs) ntask_all = std::max<size_t>(ntask_all, (size_t)(sg.first + sg.count));
@@ -438,14 +440,29 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
   CK(cudaStreamSynchronize(s));
   auto sweep_cb = [&](auto cbt, int src, int dst) {
     constexpr int CB = decltype(cbt)::value;
-    for (int L = 0; L < nlev; ++L) {
-      const int nt = hcount[2 * L], nr = hcount[2 * L + 1];
-      in_pieces_of((size_t)nt, (size_t)65535 * TINY_WARPS, [&](size_t f0, size_t c) {  // grid y <= 65535
+    // Warp-per-front launches over a segment, at most 65535 blocks of TINY_WARPS (grid y).
+    auto warp_fwd = [&](auto rplt, size_t seg0, int cnt) {
+      constexpr int RPL = decltype(rplt)::value;
+      in_pieces_of((size_t)cnt, (size_t)65535 * TINY_WARPS, [&](size_t f0, size_t c) {
         launch(K_REF_FWD, 0.0, 0.0, [&] {
-          sweep_tiny_fwd_kernel<CB><<<dim3(cchunks, (unsigned)((c + TINY_WARPS - 1) / TINY_WARPS)), 256, 0, s>>>(
-              drd, ctasks + lr[L].tiny0 + f0, (int)c, src);
+          sweep_warp_fwd_kernel<CB, RPL><<<dim3(cchunks, (unsigned)((c + TINY_WARPS - 1) / TINY_WARPS)), 256, 0, s>>>(
+              drd, ctasks + seg0 + f0, (int)c, src);
         });
       });
+    };
+    auto warp_bwd = [&](auto rplt, size_t seg0, int cnt) {
+      constexpr int RPL = decltype(rplt)::value;
+      in_pieces_of((size_t)cnt, (size_t)65535 * TINY_WARPS, [&](size_t f0, size_t c) {
+        launch(K_REF_BWD, 0.0, 0.0, [&] {
+          sweep_warp_bwd_kernel<CB, RPL><<<dim3(cchunks, (unsigned)((c + TINY_WARPS - 1) / TINY_WARPS)), 256, 0, s>>>(
+              drd, ctasks + seg0 + f0, (int)c, src, dst);
+        });
+      });
+    };
+    for (int L = 0; L < nlev; ++L) {
+      const int nt = hcount[3 * L], nm = hcount[3 * L + 1], nr = hcount[3 * L + 2];
+      if (nt) warp_fwd(std::integral_constant<int, 1>{}, lr[L].tiny0, nt);
+      if (nm) warp_fwd(std::integral_constant<int, 2>{}, lr[L].mid0, nm);
       if (!nr) continue;
       const size_t sm = (size_t)std::max(1, lr[L].max_ne) * CB * sizeof(float2);
       const unsigned tiles = (unsigned)((lr[L].max_n + SW_ROWS - 1) / SW_ROWS);
@@ -464,13 +481,9 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
       });
     });
     for (int L = nlev - 1; L >= 0; --L) {
-      const int nt = hcount[2 * L], nr = hcount[2 * L + 1];
-      in_pieces_of((size_t)nt, (size_t)65535 * TINY_WARPS, [&](size_t f0, size_t c) {  // grid y <= 65535
-        launch(K_REF_BWD, 0.0, 0.0, [&] {
-          sweep_tiny_bwd_kernel<CB><<<dim3(cchunks, (unsigned)((c + TINY_WARPS - 1) / TINY_WARPS)), 256, 0, s>>>(
-              drd, ctasks + lr[L].tiny0 + f0, (int)c, src, dst);
-        });
-      });
+      const int nt = hcount[3 * L], nm = hcount[3 * L + 1], nr = hcount[3 * L + 2];
+      if (nt) warp_bwd(std::integral_constant<int, 1>{}, lr[L].tiny0, nt);
+      if (nm) warp_bwd(std::integral_constant<int, 2>{}, lr[L].mid0, nm);
       if (!nr) continue;
       const size_t sm = (size_t)std::max(1, lr[L].max_n) * CB * sizeof(float2);
       const unsigned tiles = (unsigned)((std::max(1, lr[L].max_ne) + SW_ROWS - 1) / SW_ROWS);
@@ -1056,9 +1069,12 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
     } else {
       if constexpr (std::is_same<T, float>::value && std::is_same<TR, float>::value) {
         std::vector<LevelRange> lr;
-        for (const Level& lv : levels)
-          lr.push_back({lv.tiny0, lv.tiny_n, lv.small0, lv.small_n + lv.large_n, lv.max_n,
+        for (const Level& lv : levels) {
+          // The small buckets of at most 64 variables lead the small tasks; the rest follow.
+          const size_t mid = lv.sbn[0] + lv.sbn[1];
+          lr.push_back({lv.tiny0, lv.tiny_n, lv.small0, mid, lv.small0 + mid, lv.small_n - mid + lv.large_n, lv.max_n,
                         std::max(lv.max_large_ne, lv.max_small_n)});
+        }
         RefineDesc* fwd = refine(ctx, sys, specs, begin, cj, lr, max_root, dtasks, jd, arena, arena_off, rarena,
                                  root_off, launch, th, eh, sh, ih, ctx->rb[0], 0, {});
         if (grad) gradient(ctx, sys, specs, begin, cj, lr, max_root, dtasks, jd, arena, arena_off, rarena, root_off,

@@ -7,9 +7,9 @@
 // The sweeps stream each front's factor columns once ([F11^-1; W] forward, X backward) against
 // CB right-hand-side columns (the channels of W_R, mostly one or two), so they are bound by HBM
 // bandwidth and by the latency of the gathers in front of the streams. Each front row finds its
-// sources in one 16-byte SweepRow (built with the plan); fronts of at most TINY_MAX variables run
-// one per warp with the right-hand side in registers (broadcast by shuffles), larger ones as row
-// tiles of 64 with the inner dimension split four ways.
+// sources in one 16-byte SweepRow (built with the plan); fronts of at most 64 variables run one per
+// warp with the right-hand side in registers (broadcast by shuffles), larger ones as row tiles of
+// 64 with the inner dimension split four ways.
 //
 // Tasks come from lists compacted to the solves still iterating (compact_kernel), so a batch in
 // which a few solves need more GMRES steps does not sweep the others' tasks again.
@@ -42,9 +42,21 @@ __device__ __forceinline__ bool sweep_idle(const RefineDesc& R, int src) {
   return R.done || (src >= 0 && R.inner_done);
 }
 
-// ---- fronts of at most TINY_MAX variables: a warp each -----------------------------------------
-template <int CB>
-__global__ void __launch_bounds__(256) sweep_tiny_fwd_kernel(const RefineDesc* __restrict__ rd,
+// ---- fronts of at most 32 RPL variables: a warp each --------------------------------------------
+// Lane l owns rows l, l + 32, ... (RPL rows); the right-hand side of row k comes from lane k % 32 of
+// register k / 32 by a shuffle, so a warp needs no shared memory and no barrier. RPL = 1 serves
+// the tiny fronts (n <= 32), RPL = 2 the fronts up to 64 variables.
+template <int RPL, int CB>
+__device__ __forceinline__ float2 lane_value(const float2 (&v)[RPL][CB], int k, int j) {
+  float2 src = v[0][j];
+#pragma unroll
+  for (int u = 1; u < RPL; ++u)
+    if ((k >> 5) == u) src = v[u][j];
+  return make_float2(__shfl_sync(0xffffffffu, src.x, k & 31), __shfl_sync(0xffffffffu, src.y, k & 31));
+}
+
+template <int CB, int RPL>
+__global__ void __launch_bounds__(256) sweep_warp_fwd_kernel(const RefineDesc* __restrict__ rd,
                                                              const Task* __restrict__ tasks, int ntasks, int src) {
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ti = blockIdx.y * TINY_WARPS + w;
@@ -55,36 +67,47 @@ __global__ void __launch_bounds__(256) sweep_tiny_fwd_kernel(const RefineDesc* _
   if (sweep_idle(R, src) || j0 >= R.c) return;
   const FrontDesc& f = *tk.fd;
   const int n = f.n, ne = f.ne;
-  float2 z[CB];
-  if (lane < n) load_z<CB>(R, sweep_src(R, src), R.srows[f.var_off + lane], j0, z);
-  else
+  const double2* rin = sweep_src(R, src);
+  float2 z[RPL][CB], acc[RPL][CB];
 #pragma unroll
-    for (int j = 0; j < CB; ++j) z[j] = make_float2(0.f, 0.f);
-  float2 acc[CB];
+  for (int u = 0; u < RPL; ++u) {
+    const int r = lane + 32 * u;
+    if (r < n) load_z<CB>(R, rin, R.srows[f.var_off + r], j0, z[u]);
+    else
 #pragma unroll
-  for (int j = 0; j < CB; ++j) acc[j] = lane < ne ? make_float2(0.f, 0.f) : z[j];
-  const float2* F = R.arena + f.arena_off + lane;  // row `lane` of [F11^-1; W]
+      for (int j = 0; j < CB; ++j) z[u][j] = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int j = 0; j < CB; ++j) acc[u][j] = r < ne ? make_float2(0.f, 0.f) : z[u][j];
+  }
+  const float2* F = R.arena + f.arena_off + lane;  // rows lane + 32 u of [F11^-1; W]
 #pragma unroll 4
   for (int k = 0; k < ne; ++k) {
-    const float2 a = lane < n ? F[(int64_t)k * n] : make_float2(0.f, 0.f);
+    float2 a[RPL];
+#pragma unroll
+    for (int u = 0; u < RPL; ++u) a[u] = lane + 32 * u < n ? F[32 * u + (int64_t)k * n] : make_float2(0.f, 0.f);
 #pragma unroll
     for (int j = 0; j < CB; ++j) {
-      const float2 zk = make_float2(__shfl_sync(0xffffffffu, z[j].x, k), __shfl_sync(0xffffffffu, z[j].y, k));
-      acc[j] = cfma(acc[j], a, zk);
+      const float2 zk = lane_value<RPL, CB>(z, k, j);
+#pragma unroll
+      for (int u = 0; u < RPL; ++u) acc[u][j] = cfma(acc[u][j], a[u], zk);
     }
   }
-  if (lane >= n) return;
 #pragma unroll
-  for (int j = 0; j < CB; ++j) {
-    const int col = j0 + j;
-    if (col >= R.c) break;
-    if (lane < ne) R.tb[(f.toff + lane) + (int64_t)col * R.sum_ne] = acc[j];
-    else R.hb[(f.hoff + lane - ne) + (int64_t)col * R.sum_nb] = acc[j];
+  for (int u = 0; u < RPL; ++u) {
+    const int r = lane + 32 * u;
+    if (r >= n) continue;
+#pragma unroll
+    for (int j = 0; j < CB; ++j) {
+      const int col = j0 + j;
+      if (col >= R.c) break;
+      if (r < ne) R.tb[(f.toff + r) + (int64_t)col * R.sum_ne] = acc[u][j];
+      else R.hb[(f.hoff + r - ne) + (int64_t)col * R.sum_nb] = acc[u][j];
+    }
   }
 }
 
-template <int CB>
-__global__ void __launch_bounds__(256) sweep_tiny_bwd_kernel(const RefineDesc* __restrict__ rd,
+template <int CB, int RPL>
+__global__ void __launch_bounds__(256) sweep_warp_bwd_kernel(const RefineDesc* __restrict__ rd,
                                                              const Task* __restrict__ tasks, int ntasks, int src,
                                                              int dst) {
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -98,31 +121,42 @@ __global__ void __launch_bounds__(256) sweep_tiny_bwd_kernel(const RefineDesc* _
   const int n = f.n, ne = f.ne, nb = n - ne;
   if (ne == 0) return;
   float2* dout = sweep_dst(R, dst);
-  float2 xb[CB], acc[CB];
-  const int vb = lane < nb ? R.srows[f.var_off + ne + lane].var : 0;
+  float2 xb[RPL][CB], acc[RPL][CB];
 #pragma unroll
-  for (int j = 0; j < CB; ++j) {
-    const int col = j0 + j;
-    xb[j] = (lane < nb && col < R.c) ? dout[vb + (int64_t)col * R.nblk] : make_float2(0.f, 0.f);
-    acc[j] = (lane < ne && col < R.c) ? R.tb[(f.toff + lane) + (int64_t)col * R.sum_ne] : make_float2(0.f, 0.f);
-  }
-  const float2* F = R.arena + f.arena_off + lane + (int64_t)ne * n;  // row `lane` of X
-#pragma unroll 4
-  for (int p = 0; p < nb; ++p) {
-    const float2 a = lane < ne ? F[(int64_t)p * n] : make_float2(0.f, 0.f);
+  for (int u = 0; u < RPL; ++u) {
+    const int p = lane + 32 * u, r = lane + 32 * u;
+    const int vb = p < nb ? R.srows[f.var_off + ne + p].var : 0;
 #pragma unroll
     for (int j = 0; j < CB; ++j) {
-      const float2 xp = make_float2(__shfl_sync(0xffffffffu, xb[j].x, p), __shfl_sync(0xffffffffu, xb[j].y, p));
-      acc[j] = cfms(acc[j], a, xp);
+      const int col = j0 + j;
+      xb[u][j] = (p < nb && col < R.c) ? dout[vb + (int64_t)col * R.nblk] : make_float2(0.f, 0.f);
+      acc[u][j] = (r < ne && col < R.c) ? R.tb[(f.toff + r) + (int64_t)col * R.sum_ne] : make_float2(0.f, 0.f);
     }
   }
-  if (lane >= ne) return;
-  const int ve = R.srows[f.var_off + lane].var;
+  const float2* F = R.arena + f.arena_off + lane + (int64_t)ne * n;  // rows lane + 32 u of X
+#pragma unroll 4
+  for (int p = 0; p < nb; ++p) {
+    float2 a[RPL];
 #pragma unroll
-  for (int j = 0; j < CB; ++j) {
-    const int col = j0 + j;
-    if (col >= R.c) break;
-    dout[ve + (int64_t)col * R.nblk] = acc[j];
+    for (int u = 0; u < RPL; ++u) a[u] = lane + 32 * u < ne ? F[32 * u + (int64_t)p * n] : make_float2(0.f, 0.f);
+#pragma unroll
+    for (int j = 0; j < CB; ++j) {
+      const float2 xp = lane_value<RPL, CB>(xb, p, j);
+#pragma unroll
+      for (int u = 0; u < RPL; ++u) acc[u][j] = cfms(acc[u][j], a[u], xp);
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < RPL; ++u) {
+    const int r = lane + 32 * u;
+    if (r >= ne) continue;
+    const int ve = R.srows[f.var_off + r].var;
+#pragma unroll
+    for (int j = 0; j < CB; ++j) {
+      const int col = j0 + j;
+      if (col >= R.c) break;
+      dout[ve + (int64_t)col * R.nblk] = acc[u][j];
+    }
   }
 }
 
