@@ -81,13 +81,13 @@ __host__ __device__ inline int64_t panel_staged_bytes(int m, int vbytes) {
 //     candidate rows -a P^-1;
 //  2. the rows outside the candidates (the pivoted rows above k0, the rows below npiv) receive
 //     their panel entries -a P^-1 by replaying the sweep's elimination steps from the recorded
-//     pivot rows, a thread per row (the same operations, in the same order, as if they had been
+//     pivot rows, two lanes per row (the same operations, in the same order, as if they had been
 //     swept with the candidates: an explicit P^-1 would lose accuracy on ill-conditioned blocks);
 //  3. the row interchanges reach the other columns: the pivot rows of the rest columns are
 //     copied to Y (the update's right factor) and the rows the interchanges displaced below the
 //     pivot rows are moved; the pivot rows themselves are rewritten by the update.
 template <typename T>
-__global__ void __launch_bounds__(256) inv_panel_kernel(const InvTask* __restrict__ tasks, int k0, double tol,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) inv_panel_kernel(const InvTask* __restrict__ tasks, int k0, double tol,
                                                         int perturb, int smem_bytes) {
   using V = typename Cx<T>::V;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -154,30 +154,37 @@ __global__ void __launch_bounds__(256) inv_panel_kernel(const InvTask* __restric
     if (leader) disp[__popc(bal & ((1u << lane) - 1u))] = p;
     if (lane == 0) ndisp = __popc(bal);
   }
-  // 2. Rows outside the candidates: the sweep's steps replayed on each row, a thread per row.
+  // 2. Rows outside the candidates: the sweep's steps replayed on each row, two adjacent lanes
+  // per row (16 panel columns each); the entry of step k's column comes from its owner by a shuffle.
   const int nout = n - m;
-  for (int r = threadIdx.x; r < nout; r += blockDim.x) {
+  for (int base = 0; base < 2 * nout; base += blockDim.x) {
+    const int item = base + threadIdx.x;
+    const bool act = item < 2 * nout;
+    const int r = act ? item >> 1 : 0, h = item & 1;
     const int row = r < k0 ? r : r + m;
-    V* Ar = A + row + (int64_t)k0 * ld;
-    V a[GJ_KB];
+    V* Ar = A + row + (int64_t)(k0 + 16 * h) * ld;
+    V a[16];
 #pragma unroll
-    for (int c = 0; c < GJ_KB; ++c) a[c] = c < kb ? Ar[(int64_t)c * ld] : cx<V>(0.0, 0.0);
-    for (int k = 0; k < kb; ++k) {
+    for (int c = 0; c < 16; ++c) a[c] = (act && 16 * h + c < kb) ? Ar[(int64_t)c * ld] : cx<V>(0.0, 0.0);
+#pragma unroll
+    for (int k = 0; k < GJ_KB; ++k) {
+      if (k >= kb) break;
       const V* pk = prows + k * kb;
-      V ak = a[0];
+      const V own = a[k & 15];
+      const int src = (lane & ~1) | (k >> 4);
+      const V ak = cx<V>(__shfl_sync(0xffffffffu, own.x, src), __shfl_sync(0xffffffffu, own.y, src));
 #pragma unroll
-      for (int c = 1; c < GJ_KB; ++c)
-        if (c == k) ak = a[c];
-#pragma unroll
-      for (int c = 0; c < GJ_KB; ++c) {
-        if (c >= kb) continue;
-        if (c == k) a[c] = cmul(cx<V>(-ak.x, -ak.y), pk[c]);
-        else a[c] = cfms(a[c], ak, pk[c]);
+      for (int c = 0; c < 16; ++c) {
+        const int col = 16 * h + c;
+        if (col >= kb) continue;
+        if (col == k) a[c] = cmul(cx<V>(-ak.x, -ak.y), pk[col]);
+        else a[c] = cfms(a[c], ak, pk[col]);
       }
     }
+    if (act)
 #pragma unroll
-    for (int c = 0; c < GJ_KB; ++c)
-      if (c < kb) Ar[(int64_t)c * ld] = a[c];
+      for (int c = 0; c < 16; ++c)
+        if (16 * h + c < kb) Ar[(int64_t)c * ld] = a[c];
   }
   __syncthreads();
   // 3. Pivot rows of the rest columns into Y; displaced rows into place. A warp per column.
