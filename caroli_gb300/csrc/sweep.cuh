@@ -133,17 +133,55 @@ __global__ void __launch_bounds__(256) sweep_warp_bwd_kernel(const RefineDesc* _
       acc[u][j] = (r < ne && col < R.c) ? R.tb[(f.toff + r) + (int64_t)col * R.sum_ne] : make_float2(0.f, 0.f);
     }
   }
-  const float2* F = R.arena + f.arena_off + lane + (int64_t)ne * n;  // rows lane + 32 u of X
-#pragma unroll 4
-  for (int p = 0; p < nb; ++p) {
-    float2 a[RPL];
+  if (ne <= 16) {
+    // Few eliminated rows: lane = r + ne2 s (ne2 = ne rounded up to a power of two, s < 32 / ne2)
+    // sums X[r, p] x_b[p] over p = s (mod 32 / ne2); the slices meet by shuffles at the end.
+    const int ne2 = ne <= 1 ? 1 : ne <= 2 ? 2 : ne <= 4 ? 4 : ne <= 8 ? 8 : 16;
+    const int S = 32 / ne2, r = lane & (ne2 - 1), sl = lane / ne2;
+    const float2* X = R.arena + f.arena_off + r + (int64_t)ne * n;  // row r of X
+    float2 part[CB];
 #pragma unroll
-    for (int u = 0; u < RPL; ++u) a[u] = lane + 32 * u < ne ? F[32 * u + (int64_t)p * n] : make_float2(0.f, 0.f);
+    for (int j = 0; j < CB; ++j) part[j] = make_float2(0.f, 0.f);
+    for (int p0 = 0; p0 < nb; p0 += S) {
+      const int p = p0 + sl;
+      const float2 a = (r < ne && p < nb) ? X[(int64_t)p * n] : make_float2(0.f, 0.f);
+      const int u = p0 >> 5;  // the same for the whole warp: S divides 32
+#pragma unroll
+      for (int j = 0; j < CB; ++j) {
+        float2 src = xb[0][j];
+#pragma unroll
+        for (int q = 1; q < RPL; ++q)
+          if (u == q) src = xb[q][j];
+        const float2 xp = make_float2(__shfl_sync(0xffffffffu, src.x, p & 31), __shfl_sync(0xffffffffu, src.y, p & 31));
+        part[j] = cfma(part[j], a, xp);
+      }
+    }
+    for (int o = ne2; o < 32; o <<= 1)
+#pragma unroll
+      for (int j = 0; j < CB; ++j) {
+        part[j].x += __shfl_xor_sync(0xffffffffu, part[j].x, o);
+        part[j].y += __shfl_xor_sync(0xffffffffu, part[j].y, o);
+      }
+    // Lane r (slice 0) holds row r's sum: bring it to the lane that owns row r's output.
 #pragma unroll
     for (int j = 0; j < CB; ++j) {
-      const float2 xp = lane_value<RPL, CB>(xb, p, j);
+      const float2 sum = make_float2(__shfl_sync(0xffffffffu, part[j].x, lane & (ne2 - 1)),
+                                     __shfl_sync(0xffffffffu, part[j].y, lane & (ne2 - 1)));
+      if (lane < ne) { acc[0][j].x -= sum.x; acc[0][j].y -= sum.y; }
+    }
+  } else {
+    const float2* F = R.arena + f.arena_off + lane + (int64_t)ne * n;  // rows lane + 32 u of X
+#pragma unroll 4
+    for (int p = 0; p < nb; ++p) {
+      float2 a[RPL];
 #pragma unroll
-      for (int u = 0; u < RPL; ++u) acc[u][j] = cfms(acc[u][j], a[u], xp);
+      for (int u = 0; u < RPL; ++u) a[u] = lane + 32 * u < ne ? F[32 * u + (int64_t)p * n] : make_float2(0.f, 0.f);
+#pragma unroll
+      for (int j = 0; j < CB; ++j) {
+        const float2 xp = lane_value<RPL, CB>(xb, p, j);
+#pragma unroll
+        for (int u = 0; u < RPL; ++u) acc[u][j] = cfms(acc[u][j], a[u], xp);
+      }
     }
   }
 #pragma unroll
