@@ -418,14 +418,19 @@ __global__ void __launch_bounds__(256) gm_update_kernel(RefineDesc* __restrict__
   if (R.done) return;
   const int q = blockIdx.y * 256 + threadIdx.x;
   if (q >= R.nblk) return;
+  const int steps = R.inner;  // Arnoldi vectors of this outer step (coefficients past them are 0)
   for (int j = 0; j < R.c; ++j) {
+    // The coefficients first, then every preconditioned vector's element at once.
+    double2 yv[GM_M];
+    float2 zv[GM_M];
+#pragma unroll
+    for (int t = 0; t < GM_M; ++t) yv[t] = t < steps ? R.y[(int64_t)j * GM_M + t] : make_double2(0.0, 0.0);
+#pragma unroll
+    for (int t = 0; t < GM_M; ++t)
+      zv[t] = t < steps ? R.Z[(int64_t)t * R.nblk * R.c + (int64_t)j * R.nblk + q] : make_float2(0.f, 0.f);
     double2 acc = make_double2(0.0, 0.0);
-    for (int t = 0; t < GM_M; ++t) {
-      const double2 yt = R.y[(int64_t)j * GM_M + t];
-      if (yt.x == 0.0 && yt.y == 0.0) continue;
-      const float2 z = R.Z[(int64_t)t * R.nblk * R.c + (int64_t)j * R.nblk + q];
-      acc = cfma(acc, yt, make_double2((double)z.x, (double)z.y));
-    }
+#pragma unroll
+    for (int t = 0; t < GM_M; ++t) acc = cfma(acc, yv[t], make_double2((double)zv[t].x, (double)zv[t].y));
     const int64_t o = q + (int64_t)j * R.nblk;
     R.x[o].x += acc.x;
     R.x[o].y += acc.y;
