@@ -209,6 +209,7 @@ struct TaskLevel {
   size_t inv0 = 0;
   double small_flops = 0, small_bytes = 0, inv_flops = 0, gemm0_flops = 0, gemm1_flops = 0, asm_bytes = 0;
   double tiny_flops = 0, tiny_bytes = 0;
+  int max_tiny_n = 0;
   double upd_flops = 0, upd_bytes = 0;  // the rank-kb updates of the blocked sweep
   double pan_flops = 0;                 // its panel sweeps (kb steps over n rows of kb columns)
 };
@@ -829,6 +830,7 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
             tasks.push_back({(int32_t)j, (int32_t)k, dfr + k});
             const double ne = fr[k].ne, nb = fr[k].n - fr[k].ne;
             lv.tiny_flops += 8.0 / 3 * ne * ne * ne + 8 * ne * ne * nb + 8 * nb * nb * ne;
+            lv.max_tiny_n = std::max(lv.max_tiny_n, fr[k].n);
             lv.tiny_bytes += ((double)fr[k].n * fr[k].n + (mixed ? (double)fr[k].n * fr[k].n : nb * nb)) * vb;
           }
       }
@@ -1005,11 +1007,11 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
         const unsigned blocks = (unsigned)((lv.tiny_n + TINY_WARPS - 1) / TINY_WARPS);
         launch(K_SMALL, lv.tiny_flops, lv.tiny_bytes, [&] {
           if (mixed)
-            tiny_front_kernel<T, true><<<blocks, 256, tiny_smem<T>(), s>>>(djobs, dtasks + lv.tiny0, (int)lv.tiny_n,
-                                                                           Prec<T>::tol, perturb, pert);
+            tiny_front_kernel<T, true><<<blocks, 256, tiny_smem<T>(lv.max_tiny_n), s>>>(
+                djobs, dtasks + lv.tiny0, (int)lv.tiny_n, Prec<T>::tol, perturb, pert, lv.max_tiny_n);
           else
-            tiny_front_kernel<T, false><<<blocks, 256, tiny_smem<T>(), s>>>(djobs, dtasks + lv.tiny0, (int)lv.tiny_n,
-                                                                            Prec<T>::tol, perturb, pert);
+            tiny_front_kernel<T, false><<<blocks, 256, tiny_smem<T>(lv.max_tiny_n), s>>>(
+                djobs, dtasks + lv.tiny0, (int)lv.tiny_n, Prec<T>::tol, perturb, pert, lv.max_tiny_n);
         });
       }
       for (int b = 0; b < 3; ++b) {

@@ -14,17 +14,20 @@ namespace caroli {
 constexpr int TINY_MAX = 32;
 constexpr int TINY_WARPS = 8;
 
-// Dynamic shared memory of tiny_front_kernel.
-template <typename T> constexpr size_t tiny_smem() {
-  return (size_t)TINY_WARPS * (TINY_MAX * (TINY_MAX + 1) + TINY_MAX) * sizeof(typename Cx<T>::V);
+// Dynamic shared memory of tiny_front_kernel for fronts of at most `nmax` variables: per warp the
+// front (nmax x (nmax | 1)) and the pivot row.
+template <typename T> size_t tiny_smem(int nmax) {
+  return (size_t)TINY_WARPS * ((size_t)nmax * (nmax | 1) + nmax) * sizeof(typename Cx<T>::V);
 }
 
+// nmax: the launch's largest front (sizes each warp's shared-memory block, leading dimension nmax | 1).
 template <typename T, bool KEEP>
 __global__ void __launch_bounds__(256) tiny_front_kernel(const JobDesc* __restrict__ jobs, const Task* __restrict__ tasks,
-                                                         int ntasks, double tol, int perturb, int* __restrict__ perturbed) {
+                                                         int ntasks, double tol, int perturb, int* __restrict__ perturbed,
+                                                         int nmax) {
   using V = typename Cx<T>::V;
-  constexpr int LD = TINY_MAX + 1;
-  extern __shared__ __align__(16) unsigned char smem_raw[];  // per warp: front (32 x 33) and pivot row
+  const int LD = nmax | 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];  // per warp: front (nmax x LD) and pivot row
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ti = blockIdx.x * TINY_WARPS + w;
   if (ti >= ntasks) return;
@@ -32,8 +35,8 @@ __global__ void __launch_bounds__(256) tiny_front_kernel(const JobDesc* __restri
   const JobDesc& J = jobs[t.job];
   const FrontDesc& f = *t.fd;
   const int n = f.n, ne = f.ne;
-  V* F = reinterpret_cast<V*>(smem_raw) + (size_t)w * (TINY_MAX * LD + TINY_MAX);
-  V* prow = F + TINY_MAX * LD;
+  V* F = reinterpret_cast<V*>(smem_raw) + (size_t)w * ((size_t)nmax * LD + nmax);
+  V* prow = F + (size_t)nmax * LD;
   // Assembly: lane i builds row i.
   {
     const ChildBlocks<T> kids(J, f);
