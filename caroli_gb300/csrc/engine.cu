@@ -304,7 +304,7 @@ template <typename F> void in_pieces_of(size_t count, size_t piece, F fn) {
 
 struct LevelRange {
   size_t tiny0, tiny_n;  // fronts of at most TINY_MAX variables (one warp each)
-  size_t mid0, mid_n;    // fronts of at most 64 variables (one warp each, two rows per lane)
+  size_t mid0, mid_n;    // fronts of at most 96 variables (one warp each, three rows per lane)
   size_t first, count;   // the others
   int max_n;
   int max_ne;            // bound on the eliminated variables of the others
@@ -463,7 +463,7 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
     for (int L = 0; L < nlev; ++L) {
       const int nt = hcount[3 * L], nm = hcount[3 * L + 1], nr = hcount[3 * L + 2];
       if (nt) warp_fwd(std::integral_constant<int, 1>{}, lr[L].tiny0, nt);
-      if (nm) warp_fwd(std::integral_constant<int, 2>{}, lr[L].mid0, nm);
+      if (nm) warp_fwd(std::integral_constant<int, 3>{}, lr[L].mid0, nm);
       if (!nr) continue;
       const size_t sm = (size_t)std::max(1, lr[L].max_ne) * CB * sizeof(float2);
       const unsigned tiles = (unsigned)((lr[L].max_n + SW_ROWS - 1) / SW_ROWS);
@@ -484,7 +484,7 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
     for (int L = nlev - 1; L >= 0; --L) {
       const int nt = hcount[3 * L], nm = hcount[3 * L + 1], nr = hcount[3 * L + 2];
       if (nt) warp_bwd(std::integral_constant<int, 1>{}, lr[L].tiny0, nt);
-      if (nm) warp_bwd(std::integral_constant<int, 2>{}, lr[L].mid0, nm);
+      if (nm) warp_bwd(std::integral_constant<int, 3>{}, lr[L].mid0, nm);
       if (!nr) continue;
       const size_t sm = (size_t)std::max(1, lr[L].max_n) * CB * sizeof(float2);
       const unsigned tiles = (unsigned)((std::max(1, lr[L].max_ne) + SW_ROWS - 1) / SW_ROWS);
@@ -1072,8 +1072,8 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
       if constexpr (std::is_same<T, float>::value && std::is_same<TR, float>::value) {
         std::vector<LevelRange> lr;
         for (const Level& lv : levels) {
-          // The small buckets of at most 64 variables lead the small tasks; the rest follow.
-          const size_t mid = lv.sbn[0] + lv.sbn[1];
+          // Every small bucket (at most 96 variables) sweeps a warp per front; the large fronts follow.
+          const size_t mid = lv.small_n;
           lr.push_back({lv.tiny0, lv.tiny_n, lv.small0, mid, lv.small0 + mid, lv.small_n - mid + lv.large_n, lv.max_n,
                         std::max(lv.max_large_ne, lv.max_small_n)});
         }
