@@ -168,3 +168,35 @@ def test_uneven_ribbons_in_one_batch():
         for (sys_, s, c), tv in zip(items, t):
             ref = oracle_T(sys_, s, config=c)
             assert abs(tv - ref) <= tol * (1 + abs(ref)), (precision, s.energy, tv, ref)
+
+
+def test_cubic_wire_wide_separators():
+    """A cubic wire with a 20 x 20-site cross-section: separators of 400 variables, so the FP64 panel
+    sweep runs in global memory (its candidate rows no longer fit in shared memory); mixed precision
+    takes the FP64 path there (hundreds of lead channels). Both against the oracle."""
+    sys_ = cubic_wire(16, 20, 20)
+    s = sys_.self_energies(-0.3)
+    ref = oracle_T(sys_, s)
+    for precision in (Precision.DOUBLE, Precision.MIXED):
+        t, st, _ = sys_.solve_batch([s], [0], precision)
+        assert st[0] == 0
+        assert abs(t[0] - ref) <= 1e-10 * (1 + abs(ref)), (precision, t[0], ref)
+
+
+def test_invalid_arguments_and_empty_batch():
+    """Bad plan, slot or configuration: an error from the C ABI (no launch); an empty batch: empty
+    results."""
+    from caroli_gb300 import _native
+
+    sys_ = clean_bhz_ribbon(8, 6)
+    s = sys_.self_energies(0.05)
+    sys_.solve_batch([s], [0])
+    plan = sys_.plan()
+    with pytest.raises(_native.NativeError):
+        plan.solve([57], [0])
+    with pytest.raises(_native.NativeError):
+        plan.solve([0], [3])
+    with pytest.raises(_native.NativeError):
+        plan.solve([0], [0], precision=7)
+    t, st, err = plan.solve([], [])
+    assert t.shape == (0,) and st.shape == (0,)
