@@ -45,6 +45,7 @@ SIGNATURES = {
     "caroli_set_refine_options": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_double, ctypes.c_double]),
     "caroli_set_tensor_cores": (ctypes.c_int, [P, ctypes.c_int]),
     "caroli_solve_multi": (ctypes.c_int, [P, ctypes.c_int, P, P, P, ctypes.c_int, P, P, P]),
+    "caroli_scattering_states": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P, P, P, P]),
     "caroli_kernel_class_name": (ctypes.c_char_p, [ctypes.c_int]),
     "caroli_probe_kernel": (ctypes.c_int, [P, ctypes.c_int]),
     "caroli_kernel_stats": (ctypes.c_int, [P, ctypes.c_int, P, P, P, P, ctypes.c_int]),
@@ -262,6 +263,38 @@ class Plan:
         self.ctx.check(self.ctx.lib.caroli_transmission_with_grad(self.ctx.h, self.id, cnt, ptr(slots), ptr(configs),
                                                                   ptr(t), ptr(st), ptr(dv), ptr(dp) if npar else None))
         return t, st, dv, dp[:, :npar]
+
+    def scattering_states(self, slots, configs, w_left, w_right, n):
+        """ψ_L, ψ_R (n x channels, complex128) of each instance: ``w_left[i][b]``, ``w_right[i][b]``
+        are the lead factors of block b (``caroli_scattering_states``). Returns ``(states, status)``
+        with ``states[i] = (ψ_L, ψ_R)``."""
+        slots = np.ascontiguousarray(slots, np.int32)
+        configs = np.ascontiguousarray(configs, np.int32)
+        cnt = len(slots)
+        keep = []
+
+        def table(ws):
+            mats = [np.asfortranarray(w, dtype=np.complex128) for per in ws for w in per]
+            keep.extend(mats)
+            p = np.array([m.ctypes.data if m.size else 0 for m in mats] or [0], dtype=np.uintp)
+            c = np.array([m.shape[1] for m in mats] or [0], dtype=np.int32)
+            return p, c
+
+        pl, cl = table(w_left)
+        pr, cr = table(w_right)
+        nb = self.nblocks
+        outs = []
+        for i in range(cnt):
+            a = np.zeros((n, int(cl[i * nb:(i + 1) * nb].sum())), np.complex128, order="F")
+            b = np.zeros((n, int(cr[i * nb:(i + 1) * nb].sum())), np.complex128, order="F")
+            outs.append((a, b))
+        po_l = np.array([a.ctypes.data if a.size else 0 for a, _ in outs] or [0], dtype=np.uintp)
+        po_r = np.array([b.ctypes.data if b.size else 0 for _, b in outs] or [0], dtype=np.uintp)
+        st = np.zeros(max(cnt, 1), np.int32)
+        self.ctx.check(self.ctx.lib.caroli_scattering_states(self.ctx.h, self.id, cnt, ptr(slots), ptr(configs),
+                                                             ptr(pl), ptr(cl), ptr(pr), ptr(cr), ptr(po_l), ptr(po_r),
+                                                             ptr(st)))
+        return outs, st[:cnt]
 
     def last_job_info(self):
         cnt = ctypes.c_int64()

@@ -198,6 +198,14 @@ struct GradRequest {
   int64_t nnz = 0;
 };
 
+// A scattering-states request: per job, the lead factors W_L (nl x cl) and W_R (nr x cr) on the
+// device (column-major), and the host buffers of ψ (nblk x (cl + cr), block order).
+struct StatesRequest {
+  std::vector<const double2*> wl, wr;
+  std::vector<int> cl, cr;
+  std::vector<std::vector<double2>>* psi = nullptr;
+};
+
 // One tree level of a batch: its fronts split by size class, and their algorithmic work.
 struct TaskLevel {
   size_t tiny0 = 0, tiny_n = 0;
@@ -251,6 +259,7 @@ struct caroli_ctx {
   Buf inv, ipiv, iy, ibt, iscale, ibad;
   TaskCache tcache;
   Buf grhs, gptr, gdv, gdp;
+  Buf states_w;  // lead factors W_L, W_R of a scattering-states call
   double inner_tol = 1e-10;
   bool tensor_cores = true;  // f32 rank-kb updates on tcgen05 (3xTF32); else on the CUDA cores
   int max_iters = 6;
@@ -317,7 +326,7 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
                    const float2* arena, const std::vector<size_t>& arena_off, const float2* rarena,
                    const std::vector<size_t>& root_off, LaunchT& launch, std::vector<double>& th,
                    std::vector<double>& eh, std::vector<int32_t>& sh, std::vector<int32_t>& ih, RefineBufs& rb,
-                   int adjoint, const std::vector<const double2*>& rhs) {
+                   int adjoint, const std::vector<const double2*>& rhs, const StatesRequest* states = nullptr) {
   cudaStream_t s = ctx->stream;
   std::vector<RefineDesc> rdh(cj);
   size_t xo = 0, to = 0, ho = 0;
@@ -329,7 +338,7 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
     const JobSpec& sp = specs[begin + j];
     const FrontPlan& P = sp.plan->host;
     const DevBlock& B = sp.sys->blocks[sp.block];
-    const int c = sp.sys->slots[sp.slot].channels[sp.block];
+    const int c = states ? states->cl[begin + j] + states->cr[begin + j] : sp.sys->slots[sp.slot].channels[sp.block];
     cmax = std::max(cmax, c);
     max_blk = std::max(max_blk, B.nblk);
     xoffs[j] = xo; xo += (size_t)B.nblk * c;
@@ -392,9 +401,17 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
     R.y = gy + coffs[j] * M;
     R.beta = gbeta + coffs[j];
     R.col_done = gcol + coffs[j];
-    R.done = R.c == 0 ? 1 : 0;  // no channel: T = 0
     R.adjoint = adjoint;
+    R.whole = adjoint;
     R.rhs = adjoint ? rhs[j] : nullptr;
+    if (states) {
+      R.w_l = states->wl[begin + j];
+      R.w_r = states->wr[begin + j];
+      R.cl = states->cl[begin + j];
+      R.c = R.cl + states->cr[begin + j];
+      R.whole = 1;
+    }
+    R.done = R.c == 0 ? 1 : 0;  // no channel: T = 0
   }
   RefineDesc* drd = static_cast<RefineDesc*>(rb.rdesc.get(cj * sizeof(RefineDesc)));
   CK(cudaMemcpyAsync(drd, rdh.data(), cj * sizeof(RefineDesc), cudaMemcpyHostToDevice, s));
@@ -537,7 +554,7 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
       if (all) break;
     }
     launch(K_REF_GMRES, 0.0, 0.0, [&] {
-      gm_solve_kernel<<<(unsigned)cj, std::max(32, ((cmax + 31) / 32) * 32), 0, s>>>(drd, (int)cj);
+      gm_solve_kernel<<<(unsigned)cj, std::min(1024, std::max(32, ((cmax + 31) / 32) * 32)), 0, s>>>(drd, (int)cj);
     });
     in_pieces(cj, [&](size_t f0, size_t c) {
       launch(K_REF_GMRES, 0.0, 0.0, [&] { gm_update_kernel<<<dim3((unsigned)c, rows), 256, 0, s>>>(drd + f0); });
@@ -560,19 +577,26 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
     if (all) break;
   }
   CK(cudaEventRecord(ctx->ev1, s));
-  if (!adjoint) {
+  if (!adjoint && !states) {
     CK(cudaMemcpyAsync(th.data(), rt_out, cj * sizeof(double), cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(eh.data(), rerr, cj * sizeof(double), cudaMemcpyDeviceToHost, s));
   }
+  if (states)
+    for (size_t j = 0; j < cj; ++j) {
+      std::vector<double2>& psi = (*states->psi)[begin + j];
+      psi.resize((size_t)rdh[j].nblk * rdh[j].c);
+      if (!psi.empty())
+        CK(cudaMemcpyAsync(psi.data(), rx + xoffs[j], psi.size() * sizeof(double2), cudaMemcpyDeviceToHost, s));
+    }
   std::vector<RefineDesc> fin(cj);
   CK(cudaMemcpyAsync(fin.data(), drd, cj * sizeof(RefineDesc), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   for (size_t j = 0; j < cj; ++j) {
     ih[j] = std::max(ih[j], fin[j].iters);
     ctx->refine_job_steps += fin[j].steps;
-    if (rdh[j].c == 0) {
+    if (rdh[j].c == 0 || states) {
       if (!adjoint) { th[j] = 0.0; eh[j] = 0.0; }
-      continue;
+      if (rdh[j].c == 0) continue;
     }
     if (!fin[j].done || fin[j].stalled) sh[j] = ST_REFINE_STALLED;
   }
@@ -718,7 +742,7 @@ void gradient(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, s
 // (SINGLE), or complex f32 factors refined in FP64 (MIXED). T: front precision, TR: root precision.
 template <typename T, typename TR>
 void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, Mode mode, std::vector<JobOut>& out,
-              const GradRequest* grad = nullptr) {
+              const GradRequest* grad = nullptr, const StatesRequest* states = nullptr) {
   using V = typename Cx<T>::V;
   using VR = typename Cx<TR>::V;
   cudaStream_t s = ctx->stream;
@@ -1078,7 +1102,7 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
                         std::max(lv.max_large_ne, lv.max_small_n)});
         }
         RefineDesc* fwd = refine(ctx, sys, specs, begin, cj, lr, max_root, dtasks, jd, arena, arena_off, rarena,
-                                 root_off, launch, th, eh, sh, ih, ctx->rb[0], 0, {});
+                                 root_off, launch, th, eh, sh, ih, ctx->rb[0], 0, {}, states);
         if (grad) gradient(ctx, sys, specs, begin, cj, lr, max_root, dtasks, jd, arena, arena_off, rarena, root_off,
                            launch, th, eh, sh, ih, fwd, *grad, out);
       }
@@ -1551,6 +1575,114 @@ int caroli_transmission_with_grad(caroli_ctx* ctx, int plan_id, int count, const
           for (int k = 0; k < g.nparams && k < (int)o.dp.size(); ++k) dt_dp[(size_t)i * g.nparams + k] += o.dp[k];
       }
       t[i] = sum;
+      status[i] = st;
+    }
+    return CAROLI_OK;
+  } catch (const CudaError& e) {
+    return fail_with(ctx, e.e == cudaErrorMemoryAllocation ? CAROLI_ENOMEM : CAROLI_ECUDA,
+                     std::string(e.what) + ": " + cudaGetErrorString(e.e));
+  }
+}
+
+int caroli_scattering_states(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots, const int32_t* configs,
+                             const double* const* w_left, const int32_t* left_channels, const double* const* w_right,
+                             const int32_t* right_channels, double* const* psi_left, double* const* psi_right,
+                             int32_t* status) {
+  System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
+  if (!sys || count < 0 ||
+      (count > 0 && (!slots || !configs || !w_left || !left_channels || !w_right || !right_channels || !psi_left ||
+                     !psi_right || !status)))
+    return fail_with(ctx, CAROLI_EINVAL, "caroli_scattering_states: bad arguments");
+  if (!sys->vals) return fail_with(ctx, CAROLI_EINVAL, "no H values uploaded");
+  const int nb = (int)sys->plans.size();
+  for (int i = 0; i < count; ++i) {
+    if (slots[i] < 0 || slots[i] >= (int)sys->slots.size() || !sys->slots[slots[i]].set)
+      return fail_with(ctx, CAROLI_EINVAL, "energy slot without self-energies");
+    if (configs[i] < 0 || configs[i] >= sys->nconfigs) return fail_with(ctx, CAROLI_EINVAL, "configuration out of range");
+    int64_t cl = 0, cr = 0;
+    for (int b = 0; b < nb; ++b) {
+      const size_t q = (size_t)i * nb + b;
+      const int l = left_channels[q], r = right_channels[q];
+      if (l < 0 || l > sys->plans[b]->host.nl || r < 0 || r > sys->plans[b]->host.nr || (l && !w_left[q]) ||
+          (r && !w_right[q]))
+        return fail_with(ctx, CAROLI_EINVAL, "caroli_scattering_states: bad lead factor");
+      cl += l;
+      cr += r;
+    }
+    if ((cl && !psi_left[i]) || (cr && !psi_right[i]))
+      return fail_with(ctx, CAROLI_EINVAL, "caroli_scattering_states: missing output");
+  }
+  try {
+    CK(cudaSetDevice(ctx->device));
+    ctx->last_ms = 0.0;
+    ctx->last_launches = 0;
+    ctx->factor_ms = ctx->root_ms = ctx->tail_ms = 0.0;
+    ctx->refine_iters = 0;
+    ctx->fallbacks = 0;
+    ctx->refine_job_steps = ctx->refine_batch_steps = 0;
+    std::vector<JobSpec> specs;
+    StatesRequest rq;
+    size_t welems = 0;
+    std::vector<size_t> woff;
+    for (int i = 0; i < count; ++i)
+      for (int b = 0; b < nb; ++b) {
+        const size_t q = (size_t)i * nb + b;
+        specs.push_back({b, slots[i], configs[i], sys->plans[b].get(), sys});
+        rq.cl.push_back(left_channels[q]);
+        rq.cr.push_back(right_channels[q]);
+        woff.push_back(welems);
+        welems += (size_t)sys->plans[b]->host.nl * left_channels[q] + (size_t)sys->plans[b]->host.nr * right_channels[q];
+      }
+    double2* w = static_cast<double2*>(ctx->states_w.get(std::max<size_t>(welems, 1) * sizeof(double2)));
+    for (size_t q = 0; q < specs.size(); ++q) {
+      const FrontPlan& P = specs[q].plan->host;
+      const size_t nl = (size_t)P.nl * rq.cl[q], nr = (size_t)P.nr * rq.cr[q];
+      rq.wl.push_back(w + woff[q]);
+      rq.wr.push_back(w + woff[q] + nl);
+      if (nl) CK(cudaMemcpyAsync(w + woff[q], w_left[q], nl * sizeof(double2), cudaMemcpyHostToDevice, ctx->stream));
+      if (nr) CK(cudaMemcpyAsync(w + woff[q] + nl, w_right[q], nr * sizeof(double2), cudaMemcpyHostToDevice, ctx->stream));
+    }
+    std::vector<std::vector<double2>> psi(specs.size());
+    rq.psi = &psi;
+    std::vector<JobOut> jo;
+    run_jobs<float, float>(ctx, sys, specs, MODE_MIXED, jo, nullptr, &rq);
+    // Block-local columns to the caller's layout: ψ_L of instance i is n x Σ_b cl_b, block b's
+    // columns after those of the blocks before it, zero outside the block's orbitals.
+    const int64_t n = sys->desc.n;
+    for (int i = 0; i < count; ++i) {
+      int64_t cl = 0, cr = 0;
+      for (int b = 0; b < nb; ++b) {
+        cl += left_channels[(size_t)i * nb + b];
+        cr += right_channels[(size_t)i * nb + b];
+      }
+      if (cl) std::fill(psi_left[i], psi_left[i] + 2 * (size_t)n * cl, 0.0);
+      if (cr) std::fill(psi_right[i], psi_right[i] + 2 * (size_t)n * cr, 0.0);
+      int32_t st = ST_OK;
+      int64_t c0l = 0, c0r = 0;
+      for (int b = 0; b < nb; ++b) {
+        const size_t q = (size_t)i * nb + b;
+        const JobOut& o = jo[q];
+        if (st == ST_OK) st = o.status;
+        const auto& orbs = sys->trees[b].orbitals;
+        const size_t nblk = orbs.size();
+        const int l = rq.cl[q], r = rq.cr[q];
+        const std::vector<double2>& x = psi[q];
+        if (x.size() < nblk * (size_t)(l + r)) {
+          if (st == ST_OK) st = ST_NONFINITE;
+          continue;
+        }
+        for (int c = 0; c < l + r; ++c) {
+          double* dst = c < l ? psi_left[i] + 2 * (size_t)n * (c0l + c) : psi_right[i] + 2 * (size_t)n * (c0r + c - l);
+          for (size_t a = 0; a < nblk; ++a) {
+            const double2 v = x[a + c * nblk];
+            if (st == ST_OK && !(std::isfinite(v.x) && std::isfinite(v.y))) st = ST_NONFINITE;
+            dst[2 * orbs[a]] = v.x;
+            dst[2 * orbs[a] + 1] = v.y;
+          }
+        }
+        c0l += l;
+        c0r += r;
+      }
       status[i] = st;
     }
     return CAROLI_OK;

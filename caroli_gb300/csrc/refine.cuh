@@ -63,12 +63,30 @@ struct RefineDesc {
   // The adjoint solve A^† z = b (gradient): Σ -> Σ^†, the root inverse conjugate-transposed, an
   // explicit right-hand side `rhs` (nblk x c), and convergence on the whole vector.
   const double2* rhs;
-  int32_t adjoint, pad2;
+  int32_t adjoint;
+  // Convergence on the whole vector instead of T (adjoint solves, scattering states).
+  int32_t whole;
+  // Scattering states: the first `cl` columns are sourced by W_L (nl x cl, column-major) on the
+  // left slice, the others by W_R on the right slice; cl = 0 for a transmission.
+  const double2* w_l;
+  int32_t cl, pad2;
 };
 
 constexpr int GM_M = 12;  // Arnoldi steps per outer step
 
 __device__ __forceinline__ float2 f2(double2 v) { return make_float2((float)v.x, (float)v.y); }
+
+// Right-hand side B[i, j]: the explicit one, else W_L on the left slice (columns below cl) and
+// W_R on the right slice.
+__device__ __forceinline__ double2 rhs_at(const RefineDesc& R, int i, int j) {
+  if (R.rhs) return R.rhs[i + (int64_t)j * R.nblk];
+  if (j < R.cl) {
+    const int li = R.slice_l[i];
+    return li >= 0 ? R.w_l[li + (int64_t)j * R.nl] : make_double2(0.0, 0.0);
+  }
+  const int ri = R.slice_r[i];
+  return ri >= 0 ? R.w_r[ri + (int64_t)(j - R.cl) * R.nr] : make_double2(0.0, 0.0);
+}
 
 // Σ[i, a] of an m x m column-major block, or (Σ^†)[i, a] = conj(Σ[a, i]) for the adjoint.
 __device__ __forceinline__ double2 sigma_at(const double2* sg, int i, int a, int m, int adjoint) {
@@ -109,8 +127,7 @@ __global__ void __launch_bounds__(256) refine_residual_kernel(RefineDesc* __rest
   const int li = R.slice_l[i], ri = R.slice_r[i];
   for (int j = 0; j < R.c; ++j) {
     const double2* xj = R.x + (int64_t)j * R.nblk;
-    double2 acc = R.rhs ? R.rhs[i + (int64_t)j * R.nblk]
-                        : (ri >= 0 ? R.w_r[ri + (int64_t)j * R.nr] : make_double2(0.0, 0.0));
+    double2 acc = rhs_at(R, i, j);
     acc.x -= R.energy * xj[i].x;
     acc.y -= R.energy * xj[i].y;
     for (int q = R.csr_ptr[i]; q < R.csr_ptr[i + 1]; ++q) acc = cfma(acc, R.vals[R.csr_q[q]], xj[R.csr_col[q]]);
@@ -137,14 +154,14 @@ __global__ void __launch_bounds__(256) refine_check_kernel(RefineDesc* __restric
     return;
   }
   double tl = 0.0, dn = 0.0, xn = 0.0;
-  if (R.adjoint)  // every orbital's value matters (dT/dV_a): the correction of the whole vector
+  if (R.whole)  // every orbital's value matters (dT/dV_a, ψ): the correction of the whole vector
     for (int64_t q = threadIdx.x; q < (int64_t)R.nblk * R.c; q += blockDim.x) {
       const float2 dv = R.d[q];
       const double2 xv = R.x[q];
       dn += (double)dv.x * dv.x + (double)dv.y * dv.y;
       xn += xv.x * xv.x + xv.y * xv.y;
     }
-  for (int idx = threadIdx.x; idx < (R.adjoint ? 0 : R.nl * R.c); idx += blockDim.x) {
+  for (int idx = threadIdx.x; idx < (R.whole ? 0 : R.nl * R.c); idx += blockDim.x) {
     const int a = idx % R.nl, j = idx / R.nl;
     const double2* xj = R.x + (int64_t)j * R.nblk;
     const int row = R.left_local[a];
@@ -197,9 +214,8 @@ __global__ void refine_init_kernel(RefineDesc* __restrict__ rd, int njobs) {
   const int64_t total = (int64_t)R.nblk * R.c;
   for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
     const int i = (int)(q % R.nblk), j = (int)(q / R.nblk);
-    const int ri = R.slice_r[i];
     R.x[q] = make_double2(0.0, 0.0);
-    R.r[q] = R.rhs ? R.rhs[q] : (ri >= 0 ? R.w_r[ri + (int64_t)j * R.nr] : make_double2(0.0, 0.0));
+    R.r[q] = rhs_at(R, i, j);
   }
 }
 
@@ -389,15 +405,8 @@ __global__ void gm_inner_check_kernel(RefineDesc* __restrict__ rd, int njobs, in
   flags[job] = R.inner_done;
 }
 
-// y = H^-1 g on each column's steps, d = Z y, x += d, R.d = d; the largest relative inner
-// residual of the job goes to R.err (reused by the outer check). grid (jobs, row chunks).
-__global__ void gm_solve_kernel(RefineDesc* __restrict__ rd, int njobs) {
-  const int job = blockIdx.x;
-  if (job >= njobs) return;
-  RefineDesc& R = rd[job];
-  if (R.done) return;
-  const int j = threadIdx.x;
-  if (j >= R.c) return;
+// y = H^-1 g on each column's steps (back substitution on the rotated Hessenberg matrix).
+__device__ __forceinline__ void gm_solve_column(RefineDesc& R, int j) {
   const int kc = R.col_done[j] > 0 ? R.col_done[j] : (R.col_done[j] < 0 ? 0 : R.inner);
   const double2* H = R.H + (int64_t)j * (GM_M + 1) * GM_M;
   const double2* g = R.g + (int64_t)j * (GM_M + 1);
@@ -411,6 +420,15 @@ __global__ void gm_solve_kernel(RefineDesc* __restrict__ rd, int njobs) {
                     : make_double2(0.0, 0.0);
   }
   for (int t = kc; t < GM_M; ++t) y[t] = make_double2(0.0, 0.0);
+}
+
+// The coefficients of every column of every job: grid (jobs), a thread per column.
+__global__ void gm_solve_kernel(RefineDesc* __restrict__ rd, int njobs) {
+  const int job = blockIdx.x;
+  if (job >= njobs) return;
+  RefineDesc& R = rd[job];
+  if (R.done) return;
+  for (int j = threadIdx.x; j < R.c; j += blockDim.x) gm_solve_column(R, j);
 }
 
 __global__ void __launch_bounds__(256) gm_update_kernel(RefineDesc* __restrict__ rd) {

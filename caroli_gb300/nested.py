@@ -15,6 +15,9 @@ reference                      here
 ``transmission_with`` :682     ``transmission_with``
 ``transmission_with_precision``  ``transmission_with_precision``
   :688
+``scattering_states`` :851     ``scattering_states`` (and ``scattering_states_batch``)
+``bond_currents`` :903         ``bond_currents``, ``operator_currents``
+``site_densities`` :916        ``site_densities``
 =============================  ==========================================================
 
 The elimination and the trace run on the GPU through ``libcaroli_gb300.so``; the lead
@@ -29,6 +32,8 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _native
+from . import states as _states
+from .states import ScatteringStates
 from .leads import GreenError, LeadSolver, gamma_root
 from .precision import Precision, PrecisionOptions, checked
 from .system import System, build_system
@@ -49,6 +54,12 @@ class LeadSelfEnergies:
         if not hasattr(self, "_w_right"):
             self._w_right = [gamma_root(sr) for _, sr in self.blocks]
         return self._w_right
+
+    def w_left(self):
+        """Per block, W_L with W_L W_L^† = Γ_L (the sources of the left lead's scattering states)."""
+        if not hasattr(self, "_w_left"):
+            self._w_left = [gamma_root(sl) for sl, _ in self.blocks]
+        return self._w_left
 
 
 _CONTEXTS = {}
@@ -72,16 +83,21 @@ class NestedTwoTerminal:
             self._solvers.append((left, right))
         self._plan = None
         self._slot_of = {}
+        self.sites = None  # the region's sites, when built from a region (names of bond ends)
 
     # -- construction -------------------------------------------------------------------------
     @staticmethod
     def from_model(device_model, lead, region, axis, device=0):
-        return NestedTwoTerminal(build_system([device_model], lead, region, axis), device)
+        out = NestedTwoTerminal(build_system([device_model], lead, region, axis), device)
+        out.sites = list(region.sites)
+        return out
 
     @staticmethod
     def from_models(device_models, lead, region, axis, device=0):
         """One system per disorder configuration of the same geometry and leads."""
-        return NestedTwoTerminal(build_system(list(device_models), lead, region, axis), device)
+        out = NestedTwoTerminal(build_system(list(device_models), lead, region, axis), device)
+        out.sites = list(region.sites)
+        return out
 
     def block_count(self):
         return len(self.system.blocks)
@@ -171,6 +187,46 @@ class NestedTwoTerminal:
         t, st, dv, dp = self.transmissions_with_grad([sigma], [config])
         _result(t[0], st[0], sigma.energy)
         return float(t[0]), dv[0], dp[0]
+
+    # -- scattering states (nested.rs:851-1020) ----------------------------------------------
+    def scattering_states_batch(self, sigmas, configs=None):
+        """Scattering states of each ``(sigma, config)`` pair in one GPU batch; a failed point is a
+        ``GreenError`` in its place."""
+        if configs is None:
+            configs = [0] * len(sigmas)
+        slots = [self._slot(s) for s in sigmas]
+        outs, st = self.plan().scattering_states(slots, configs, [s.w_left() for s in sigmas],
+                                                 [s.w_right() for s in sigmas], self.system.n)
+        res = []
+        for (pl, pr), code, s, c in zip(outs, st, sigmas, configs):
+            try:
+                _result(0.0, code, s.energy)
+                res.append(ScatteringStates(s.energy, [pl, pr], int(c)))
+            except GreenError as e:
+                res.append(e)
+        return res
+
+    def scattering_states_with(self, sigma, config=0):
+        out = self.scattering_states_batch([sigma], [config])[0]
+        if isinstance(out, GreenError):
+            raise out
+        return out
+
+    def scattering_states(self, energy, config=0):
+        """``ψ_p = G W_p`` on every orbital for both leads at ``energy`` (nested.rs:851-899)."""
+        return self.scattering_states_with(self.self_energies(energy), config)
+
+    def bond_currents(self, states, f):
+        """``2 Re Tr[H_ij G^<_ji]`` of every bond (nested.rs:903-906)."""
+        return _states.bond_currents(self.system, states, f, None, self.sites)
+
+    def operator_currents(self, states, f, op):
+        """``Re Tr[(O H_ij + H_ij O) G^<_ji]`` of every bond (nested.rs:910-912)."""
+        return _states.bond_currents(self.system, states, f, op, self.sites)
+
+    def site_densities(self, states, f, op=None):
+        """``Σ_p f_p ψ_p† O ψ_p / 2π`` of every site (nested.rs:916-918)."""
+        return _states.site_densities(self.system, states, f, op)
 
     def transmissions_checked(self, energies, options: PrecisionOptions, config=0):
         sigmas = {float(e): self.self_energies(e) for e in energies}

@@ -14,6 +14,7 @@
  *   caroli_sigma_upload                      LeadSelfEnergies from self_energies  nested.rs:439-459, :652-676
  *   caroli_solve_batch                       transmission_with / transmission_with_precision /
  *                                            transmissions                        nested.rs:618-713
+ *   caroli_scattering_states                 NestedTwoTerminal::scattering_states nested.rs:851-899
  *   caroli_transmission_with_grad            no counterpart: the reference has no derivative code;
  *   caroli_derivs_upload                     the adjoint of transmission_with (dT/dV, dT/dJ)
  *   caroli_last_error                        GreenError / GpuError text           caroli-green/src/lib.rs:34-47
@@ -151,6 +152,24 @@ int caroli_derivs_upload(caroli_ctx* ctx, int plan_id, int nparams, const double
  * dT/dp = 2 Re Σ_j Z_j^† (dH/dp) X_j. */
 int caroli_transmission_with_grad(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots, const int32_t* configs,
                                   double* t, int32_t* status, double* dt_dv, double* dt_dp);
+
+/* Scattering states ψ_p = G W_p on every device orbital (NestedTwoTerminal::scattering_states,
+ * nested.rs:851-899) for `count` instances (energy slot, configuration). The caller supplies the
+ * lead factors, as the reference computes them with gamma_root (nested.rs:1036-1047) before its
+ * solve: for instance i and block b (q = i * nblocks + b), w_left[q] is nl_b x left_channels[q] and
+ * w_right[q] is nr_b x right_channels[q], column-major complex128, with W W^† = Γ = i(Σ - Σ^†) of
+ * that block's lead at the slot's energy. Outputs, column-major complex128 with n rows (every
+ * orbital of the system, region order): psi_left[i] has Σ_b left_channels[i * nblocks + b]
+ * columns, block b's after those of the blocks before it and zero outside the block's orbitals
+ * (the reference's concatenation, nested.rs:887-897); psi_right[i] likewise. status[i] per
+ * instance (CAROLI_OK, CAROLI_REFINE_STALLED, CAROLI_NONFINITE ...).
+ * Runs the mixed path: complex-f32 factors precondition an FP64 GMRES solve of A X = B with
+ * B = [e_L W_L, e_R W_R], refined until the correction of the whole of X is below 1e-10 of X
+ * (caroli_set_refine_options). */
+int caroli_scattering_states(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots, const int32_t* configs,
+                             const double* const* w_left, const int32_t* left_channels, const double* const* w_right,
+                             const int32_t* right_channels, double* const* psi_left, double* const* psi_right,
+                             int32_t* status);
 
 /* caroli_solve_batch over instances of several systems (plans) at once: instance i is
  * (plan_ids[i], slots[i], configs[i]), slots and configurations of that plan. Systems of different
