@@ -10,11 +10,13 @@ from .model import BhzParams, Model, OnSiteMap, SparseMatrix, bhz, bhz_exchange,
 from .nested import LeadSelfEnergies, NestedTwoTerminal, solve_systems
 from .precision import Precision, PrecisionOptions, PrecisionReport, checked
 from .states import BondCurrent, ScatteringStates
+from .multi import AttachedLead, Interface, NestedMultiTerminal, attach_leads, lead_voltages
 from .system import System, build_system
 
 __all__ = [
     "Lattice", "Region", "Site", "GreenError", "LeadSolver", "broadening", "gamma_root", "BhzParams", "Model",
     "OnSiteMap", "SparseMatrix", "bhz", "bhz_exchange", "bhz_spin", "cubic", "graphene", "square",
     "LeadSelfEnergies", "NestedTwoTerminal", "solve_systems", "Precision", "PrecisionOptions", "PrecisionReport", "checked",
-    "System", "build_system", "BondCurrent", "ScatteringStates",
+    "System", "build_system", "BondCurrent", "ScatteringStates", "AttachedLead", "Interface",
+    "NestedMultiTerminal", "attach_leads", "lead_voltages",
 ]

@@ -46,6 +46,9 @@ SIGNATURES = {
     "caroli_set_tensor_cores": (ctypes.c_int, [P, ctypes.c_int]),
     "caroli_solve_multi": (ctypes.c_int, [P, ctypes.c_int, P, P, P, ctypes.c_int, P, P, P]),
     "caroli_scattering_states": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P, P, P, P]),
+    "caroli_multi_leads": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P]),
+    "caroli_multi_sigma_upload": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, ctypes.c_double, P]),
+    "caroli_multi_transmissions": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, ctypes.c_int, P, P]),
     "caroli_kernel_class_name": (ctypes.c_char_p, [ctypes.c_int]),
     "caroli_probe_kernel": (ctypes.c_int, [P, ctypes.c_int]),
     "caroli_kernel_stats": (ctypes.c_int, [P, ctypes.c_int, P, P, P, P, ctypes.c_int]),
@@ -295,6 +298,29 @@ class Plan:
                                                              ptr(pl), ptr(cl), ptr(pr), ptr(cr), ptr(po_l), ptr(po_r),
                                                              ptr(st)))
         return outs, st[:cnt]
+
+    def multi_leads(self, nleads, lead_ptr, lead_orbitals):
+        """Leads of a multi-terminal plan (``caroli_multi_leads``)."""
+        lp = np.ascontiguousarray(lead_ptr, np.int64)
+        lo = np.ascontiguousarray(lead_orbitals if len(lead_orbitals) else [0], np.int64)
+        self.ctx.check(self.ctx.lib.caroli_multi_leads(self.ctx.h, self.id, nleads, ptr(lp), ptr(lo)))
+        self.nleads = nleads
+
+    def upload_multi_sigma(self, slot, energy, sigmas):
+        """``sigmas[b][p]``: Σ_p of block b on the lead's orbitals, or None."""
+        mats = [None if m is None else np.asfortranarray(m, dtype=np.complex128) for row in sigmas for m in row]
+        pt = np.array([0 if m is None or m.size == 0 else m.ctypes.data for m in mats] or [0], dtype=np.uintp)
+        self.ctx.check(self.ctx.lib.caroli_multi_sigma_upload(self.ctx.h, self.id, slot, energy, ptr(pt)))
+
+    def multi_solve(self, slots, configs, precision, nleads):
+        slots = np.ascontiguousarray(slots, np.int32)
+        configs = np.ascontiguousarray(configs, np.int32)
+        cnt = len(slots)
+        t = np.zeros((max(cnt, 1), nleads, nleads))
+        st = np.zeros(max(cnt, 1), np.int32)
+        self.ctx.check(self.ctx.lib.caroli_multi_transmissions(self.ctx.h, self.id, cnt, ptr(slots), ptr(configs),
+                                                               precision, ptr(t), ptr(st)))
+        return t[:cnt], st[:cnt]
 
     def last_job_info(self):
         cnt = ctypes.c_int64()

@@ -99,6 +99,10 @@ struct SigmaSlot {
   bool set = false;
   std::vector<double2*> sl, sr, gl, gr, wr;  // per block, device
   std::vector<int> channels;                // columns of W_R per block
+  // Multi-terminal systems: Γ_p of every (block, lead), and per block a device table of the P
+  // pointers.
+  std::vector<double2*> mgam;
+  std::vector<double2**> mtab;
 };
 
 // Block data the refinement needs (block-local CSR of H, slice positions).
@@ -135,14 +139,23 @@ struct System {
   double2* dvals = nullptr;  // dH/dp of every configuration: [config][param][nnz]
   int nparams = 0;
   std::vector<SigmaSlot> slots;
+  // Multi-terminal systems (nleads > 0): the kept orbitals of each block are its "left" list;
+  // lead p of block b occupies the kept positions mpos[b][mptr[b][p] .. mptr[b][p + 1]).
+  int nleads = 0;
+  std::vector<std::vector<int32_t>> mptr, mpos;
+  std::vector<int32_t*> dmptr, dmpos;
   ~System() {
     for (auto& p : plans) p->release();
     for (auto& b : blocks) b.release();
     cudaFree(vals);
     cudaFree(dvals);
-    for (auto& s : slots)
-      for (auto* v : {&s.sl, &s.sr, &s.gl, &s.gr, &s.wr})
+    for (auto& s : slots) {
+      for (auto* v : {&s.sl, &s.sr, &s.gl, &s.gr, &s.wr, &s.mgam})
         for (auto* p : *v) cudaFree(p);
+      for (auto* p : s.mtab) cudaFree(p);
+    }
+    for (auto* p : dmptr) cudaFree(p);
+    for (auto* p : dmpos) cudaFree(p);
   }
 };
 
@@ -260,6 +273,7 @@ struct caroli_ctx {
   TaskCache tcache;
   Buf grhs, gptr, gdv, gdp;
   Buf states_w;  // lead factors W_L, W_R of a scattering-states call
+  Buf mjobs, mscratch, mout;  // multi-terminal traces
   double inner_tol = 1e-10;
   bool tensor_cores = true;  // f32 rank-kb updates on tcgen05 (3xTF32); else on the CUDA cores
   int max_iters = 6;
@@ -611,6 +625,7 @@ struct JobOut {
   int32_t iters = 0;
   int32_t perturbed = 0;
   std::vector<double> dv, dp;  // gradient: dT/dV of the block's orbitals (block order), dT/dp
+  std::vector<double> tm;      // multi-terminal: T[p * P + q] of the block
   std::vector<uint8_t> fail;
 };
 
@@ -1090,8 +1105,64 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
       launch(K_TRACE, 0.0, 0.0, [&] {
         trace_finish_kernel<<<(unsigned)((cj + 127) / 128), 128, 0, s>>>(part, (int)parts_per_job, (int)cj, tdev, status);
       });
+      // Multi-terminal blocks: every T_pq from the root inverse.
+      std::vector<MultiJob> mj;
+      std::vector<size_t> midx;
+      int64_t smax = 1;
+      int pmax = 0;
+      for (size_t j = 0; j < cj; ++j) {
+        const JobSpec& sp = specs[begin + j];
+        if (sp.sys->nleads <= 0) continue;
+        const std::vector<int32_t>& lp = sp.sys->mptr[sp.block];
+        for (int a = 0; a < sp.sys->nleads; ++a)
+          for (int b = 0; b < sp.sys->nleads; ++b)
+            smax = std::max<int64_t>(smax, (int64_t)(lp[a + 1] - lp[a]) * (lp[b + 1] - lp[b]));
+        pmax = std::max(pmax, sp.sys->nleads);
+        MultiJob m{};
+        m.g = rarena + root_off[j];
+        m.lpos = sp.sys->dmpos[sp.block];
+        m.lptr = sp.sys->dmptr[sp.block];
+        m.gamma = sp.sys->slots[sp.slot].mtab[sp.block];
+        m.m = sp.plan->host.fronts[sp.plan->host.root].n;
+        m.nd = sp.plan->host.nd;
+        m.P = sp.sys->nleads;
+        mj.push_back(m);
+        midx.push_back(j);
+      }
+      std::vector<double> mh;
+      if (!mj.empty()) {
+        const size_t pairs = (size_t)pmax * pmax;
+        double2* scratch = static_cast<double2*>(ctx->mscratch.get(mj.size() * pairs * smax * sizeof(double2)));
+        double* mout = static_cast<double*>(ctx->mout.get(mj.size() * pairs * sizeof(double)));
+        for (size_t k = 0; k < mj.size(); ++k) {
+          mj[k].scratch = scratch + k * pairs * smax;
+          mj[k].out = mout + k * pairs;
+        }
+        MultiJob* dmj = static_cast<MultiJob*>(ctx->mjobs.get(mj.size() * sizeof(MultiJob)));
+        CK(cudaMemcpyAsync(dmj, mj.data(), mj.size() * sizeof(MultiJob), cudaMemcpyHostToDevice, s));
+        in_pieces(mj.size(), [&](size_t f0, size_t c) {
+          launch(K_TRACE, 0.0, 0.0, [&] {
+            multi_trace_kernel<TR><<<dim3((unsigned)pairs, (unsigned)c), 256, 0, s>>>(dmj + f0, smax);
+          });
+        });
+        mh.resize(mj.size() * pairs);
+        CK(cudaMemcpyAsync(mh.data(), mout, mh.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+        for (size_t k = 0; k < mj.size(); ++k) {
+          JobOut& o = out[begin + midx[k]];
+          o.tm.clear();
+          o.tm.resize((size_t)mj[k].P * mj[k].P);  // filled after the synchronisation below
+        }
+      }
       CK(cudaEventRecord(ctx->ev1, s));
       CK(cudaMemcpyAsync(th.data(), tdev, cj * sizeof(double), cudaMemcpyDeviceToHost, s));
+      if (!mj.empty()) {
+        CK(cudaStreamSynchronize(s));
+        const size_t pairs = (size_t)pmax * pmax;
+        for (size_t k = 0; k < mj.size(); ++k) {
+          JobOut& o = out[begin + midx[k]];
+          for (size_t q = 0; q < o.tm.size(); ++q) o.tm[q] = mh[k * pairs + q];
+        }
+      }
     } else {
       if constexpr (std::is_same<T, float>::value && std::is_same<TR, float>::value) {
         std::vector<LevelRange> lr;
@@ -1131,6 +1202,8 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
       o.iters = ih[j];
       int32_t st = sdev[j] != ST_OK ? sdev[j] : sh[j];
       if (st == ST_OK && !std::isfinite(o.t)) st = ST_NONFINITE;
+      for (double v : o.tm)
+        if (st == ST_OK && !std::isfinite(v)) st = ST_NONFINITE;
       const size_t nf = specs[begin + j].plan->host.fronts.size();
       bool delayed = false;
       for (size_t k = 0; k < nf; ++k) delayed |= fh[fail_off[j] + k] != 0;
@@ -1534,6 +1607,7 @@ int caroli_transmission_with_grad(caroli_ctx* ctx, int plan_id, int count, const
   System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
   if (!sys || count < 0 || (count > 0 && (!slots || !configs || !t || !status || !dt_dv)))
     return fail_with(ctx, CAROLI_EINVAL, "caroli_transmission_with_grad: bad arguments");
+  if (sys->nleads > 0) return fail_with(ctx, CAROLI_EINVAL, "caroli_transmission_with_grad: a multi-terminal plan");
   if (!sys->vals) return fail_with(ctx, CAROLI_EINVAL, "no H values uploaded");
   for (int i = 0; i < count; ++i) {
     if (slots[i] < 0 || slots[i] >= (int)sys->slots.size() || !sys->slots[slots[i]].set)
@@ -1593,6 +1667,7 @@ int caroli_scattering_states(caroli_ctx* ctx, int plan_id, int count, const int3
       (count > 0 && (!slots || !configs || !w_left || !left_channels || !w_right || !right_channels || !psi_left ||
                      !psi_right || !status)))
     return fail_with(ctx, CAROLI_EINVAL, "caroli_scattering_states: bad arguments");
+  if (sys->nleads > 0) return fail_with(ctx, CAROLI_EINVAL, "caroli_scattering_states: a multi-terminal plan");
   if (!sys->vals) return fail_with(ctx, CAROLI_EINVAL, "no H values uploaded");
   const int nb = (int)sys->plans.size();
   for (int i = 0; i < count; ++i) {
@@ -1682,6 +1757,179 @@ int caroli_scattering_states(caroli_ctx* ctx, int plan_id, int count, const int3
         }
         c0l += l;
         c0r += r;
+      }
+      status[i] = st;
+    }
+    return CAROLI_OK;
+  } catch (const CudaError& e) {
+    return fail_with(ctx, e.e == cudaErrorMemoryAllocation ? CAROLI_ENOMEM : CAROLI_ECUDA,
+                     std::string(e.what) + ": " + cudaGetErrorString(e.e));
+  }
+}
+
+int caroli_multi_leads(caroli_ctx* ctx, int plan_id, int nleads, const int64_t* lead_ptr, const int64_t* lead_orbitals) {
+  System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
+  if (!sys || nleads <= 0 || !lead_ptr || !lead_orbitals)
+    return fail_with(ctx, CAROLI_EINVAL, "caroli_multi_leads: bad arguments");
+  const int nb = (int)sys->plans.size();
+  for (int b = 0; b < nb; ++b)
+    if (sys->plans[b]->host.nr != 0)
+      return fail_with(ctx, CAROLI_EINVAL, "caroli_multi_leads: a multi-terminal plan has no right slice");
+  if (lead_ptr[0] != 0) return fail_with(ctx, CAROLI_EINVAL, "caroli_multi_leads: lead_ptr[0] must be 0");
+  std::vector<std::vector<int32_t>> mptr(nb), mpos(nb);
+  for (int b = 0; b < nb; ++b) {
+    // Kept orbitals of the block (its left list) and their positions.
+    std::vector<std::pair<int64_t, int32_t>> kept;
+    for (int64_t q = sys->left_ptr[b]; q < sys->left_ptr[b + 1]; ++q)
+      kept.push_back({sys->left[q], (int32_t)(q - sys->left_ptr[b])});
+    std::sort(kept.begin(), kept.end());
+    mptr[b].push_back(0);
+    for (int p = 0; p < nleads; ++p) {
+      const int64_t lo = lead_ptr[(size_t)b * nleads + p], hi = lead_ptr[(size_t)b * nleads + p + 1];
+      if (hi < lo) return fail_with(ctx, CAROLI_EINVAL, "caroli_multi_leads: lead_ptr not increasing");
+      for (int64_t q = lo; q < hi; ++q) {
+        auto it = std::lower_bound(kept.begin(), kept.end(), std::make_pair(lead_orbitals[q], (int32_t)-1));
+        if (it == kept.end() || it->first != lead_orbitals[q])
+          return fail_with(ctx, CAROLI_EINVAL, "caroli_multi_leads: a lead orbital is not kept in its block");
+        mpos[b].push_back(it->second);
+      }
+      mptr[b].push_back((int32_t)mpos[b].size());
+    }
+  }
+  try {
+    CK(cudaSetDevice(ctx->device));
+    for (auto* p : sys->dmptr) cudaFree(p);
+    for (auto* p : sys->dmpos) cudaFree(p);
+    sys->dmptr.clear();
+    sys->dmpos.clear();
+    for (int b = 0; b < nb; ++b) {
+      sys->dmptr.push_back(upload_vec(mptr[b], ctx->stream));
+      sys->dmpos.push_back(upload_vec(mpos[b], ctx->stream));
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    sys->mptr = std::move(mptr);
+    sys->mpos = std::move(mpos);
+    sys->nleads = nleads;
+    for (auto& sg : sys->slots) sg.set = false;  // self-energies of the old leads
+    return CAROLI_OK;
+  } catch (const CudaError& e) {
+    return fail_with(ctx, e.e == cudaErrorMemoryAllocation ? CAROLI_ENOMEM : CAROLI_ECUDA, cudaGetErrorString(e.e));
+  }
+}
+
+int caroli_multi_sigma_upload(caroli_ctx* ctx, int plan_id, int slot, double energy, const double* const* sigma) {
+  System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
+  if (!sys || slot < 0 || !sigma) return fail_with(ctx, CAROLI_EINVAL, "caroli_multi_sigma_upload: bad arguments");
+  if (sys->nleads <= 0) return fail_with(ctx, CAROLI_EINVAL, "caroli_multi_sigma_upload: no leads (caroli_multi_leads)");
+  const int nb = (int)sys->plans.size(), P = sys->nleads;
+  for (int b = 0; b < nb; ++b)
+    for (int p = 0; p < P; ++p)
+      if (sys->mptr[b][p + 1] > sys->mptr[b][p] && !sigma[(size_t)b * P + p])
+        return fail_with(ctx, CAROLI_EINVAL, "caroli_multi_sigma_upload: missing self-energy");
+  // Σ of the kept orbitals: every lead's Σ_p added at its positions (nested_multi.rs:309-318).
+  std::vector<std::vector<double>> comb(nb), empty(nb);
+  std::vector<const double*> pl(nb), pr(nb);
+  for (int b = 0; b < nb; ++b) {
+    const size_t nl = (size_t)sys->plans[b]->host.nl;
+    comb[b].assign(2 * nl * nl, 0.0);
+    for (int p = 0; p < P; ++p) {
+      const int32_t* pos = sys->mpos[b].data() + sys->mptr[b][p];
+      const int np = sys->mptr[b][p + 1] - sys->mptr[b][p];
+      const double* sp = sigma[(size_t)b * P + p];
+      for (int j = 0; j < np; ++j)
+        for (int i = 0; i < np; ++i) {
+          comb[b][2 * (pos[i] + pos[j] * nl)] += sp[2 * (i + (size_t)j * np)];
+          comb[b][2 * (pos[i] + pos[j] * nl) + 1] += sp[2 * (i + (size_t)j * np) + 1];
+        }
+    }
+    empty[b].assign(2, 0.0);
+    pl[b] = comb[b].data();
+    pr[b] = empty[b].data();
+  }
+  int rc = caroli_sigma_upload(ctx, plan_id, slot, energy, pl.data(), pr.data(), nullptr, nullptr);
+  if (rc != CAROLI_OK) return rc;
+  try {
+    SigmaSlot& sg = sys->slots[slot];
+    sg.set = false;
+    if (sg.mgam.size() != (size_t)nb * P) {
+      for (auto* p : sg.mgam) cudaFree(p);
+      for (auto* p : sg.mtab) cudaFree(p);
+      sg.mgam.clear();
+      sg.mtab.clear();
+      for (int b = 0; b < nb; ++b) {
+        for (int p = 0; p < P; ++p) {
+          const size_t np = (size_t)(sys->mptr[b][p + 1] - sys->mptr[b][p]);
+          sg.mgam.push_back(dalloc<double2>(std::max<size_t>(np * np, 1)));
+        }
+        sg.mtab.push_back(dalloc<double2*>((size_t)P));
+        CK(cudaMemcpyAsync(sg.mtab[b], sg.mgam.data() + (size_t)b * P, P * sizeof(double2*), cudaMemcpyHostToDevice,
+                           ctx->stream));
+      }
+    }
+    std::vector<std::vector<double>> keep;
+    for (int b = 0; b < nb; ++b)
+      for (int p = 0; p < P; ++p) {
+        const size_t np = (size_t)(sys->mptr[b][p + 1] - sys->mptr[b][p]);
+        if (!np) continue;
+        // Γ_p = i (Σ_p - Σ_p^†) (caroli-green/src/lib.rs:67-71).
+        const double* sp = sigma[(size_t)b * P + p];
+        std::vector<double> g(2 * np * np);
+        for (size_t j = 0; j < np; ++j)
+          for (size_t i = 0; i < np; ++i) {
+            const double dr = sp[2 * (i + j * np)] - sp[2 * (j + i * np)];
+            const double di = sp[2 * (i + j * np) + 1] + sp[2 * (j + i * np) + 1];
+            g[2 * (i + j * np)] = -di;
+            g[2 * (i + j * np) + 1] = dr;
+          }
+        CK(cudaMemcpyAsync(sg.mgam[(size_t)b * P + p], g.data(), np * np * sizeof(double2), cudaMemcpyHostToDevice,
+                           ctx->stream));
+        keep.push_back(std::move(g));
+      }
+    CK(cudaStreamSynchronize(ctx->stream));
+    sg.set = true;
+    return CAROLI_OK;
+  } catch (const CudaError& e) {
+    return fail_with(ctx, e.e == cudaErrorMemoryAllocation ? CAROLI_ENOMEM : CAROLI_ECUDA, cudaGetErrorString(e.e));
+  }
+}
+
+int caroli_multi_transmissions(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots, const int32_t* configs,
+                               int precision, double* t, int32_t* status) {
+  System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
+  if (!sys || count < 0 || (count > 0 && (!slots || !configs || !t || !status)))
+    return fail_with(ctx, CAROLI_EINVAL, "caroli_multi_transmissions: bad arguments");
+  if (sys->nleads <= 0) return fail_with(ctx, CAROLI_EINVAL, "caroli_multi_transmissions: no leads (caroli_multi_leads)");
+  if (precision != CAROLI_DOUBLE && precision != CAROLI_SINGLE)
+    return fail_with(ctx, CAROLI_EINVAL, "caroli_multi_transmissions: CAROLI_DOUBLE or CAROLI_SINGLE");
+  if (!sys->vals) return fail_with(ctx, CAROLI_EINVAL, "no H values uploaded");
+  for (int i = 0; i < count; ++i) {
+    if (slots[i] < 0 || slots[i] >= (int)sys->slots.size() || !sys->slots[slots[i]].set ||
+        sys->slots[slots[i]].mtab.empty())
+      return fail_with(ctx, CAROLI_EINVAL, "energy slot without multi-terminal self-energies");
+    if (configs[i] < 0 || configs[i] >= sys->nconfigs) return fail_with(ctx, CAROLI_EINVAL, "configuration out of range");
+  }
+  try {
+    CK(cudaSetDevice(ctx->device));
+    ctx->last_ms = 0.0;
+    ctx->last_launches = 0;
+    ctx->factor_ms = ctx->root_ms = ctx->tail_ms = 0.0;
+    ctx->fallbacks = 0;
+    ctx->refine_iters = 0;
+    ctx->refine_job_steps = ctx->refine_batch_steps = 0;
+    const int nb = (int)sys->plans.size(), P = sys->nleads;
+    std::vector<JobSpec> specs;
+    for (int i = 0; i < count; ++i)
+      for (int b = 0; b < nb; ++b) specs.push_back({b, slots[i], configs[i], sys->plans[b].get(), sys});
+    std::vector<JobOut> jo;
+    solve_jobs(ctx, sys, specs, (Mode)precision, jo);
+    for (int i = 0; i < count; ++i) {
+      double* ti = t + (size_t)i * P * P;
+      std::fill(ti, ti + (size_t)P * P, 0.0);
+      int32_t st = ST_OK;
+      for (int b = 0; b < nb; ++b) {
+        const JobOut& o = jo[(size_t)i * nb + b];
+        if (st == ST_OK) st = o.status;
+        for (size_t q = 0; q < o.tm.size() && q < (size_t)P * P; ++q) ti[q] += o.tm[q];
       }
       status[i] = st;
     }
@@ -1783,6 +2031,8 @@ int solve_instances(caroli_ctx* ctx, const std::vector<System*>& isys, int count
   for (int i = 0; i < count; ++i) {
     System* sys = isys[i];
     if (!sys) return fail_with(ctx, CAROLI_EINVAL, std::string(who) + ": unknown plan");
+    if (sys->nleads > 0)
+      return fail_with(ctx, CAROLI_EINVAL, std::string(who) + ": a multi-terminal plan (caroli_multi_transmissions)");
     if (!sys->vals) return fail_with(ctx, CAROLI_EINVAL, "no H values uploaded");
     if (slots[i] < 0 || slots[i] >= (int)sys->slots.size() || !sys->slots[slots[i]].set)
       return fail_with(ctx, CAROLI_EINVAL, "energy slot without self-energies");
@@ -2005,6 +2255,7 @@ extern "C" int caroli_solve_batch_noalloc(caroli_ctx* ctx, int plan_id, int coun
   System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
   if (!sys || count < 0 || (count > 0 && (!slots || !configs || !t || !status)))
     return fail_with(ctx, CAROLI_EINVAL, "caroli_solve_batch_noalloc: bad arguments");
+  if (sys->nleads > 0) return fail_with(ctx, CAROLI_EINVAL, "caroli_solve_batch_noalloc: a multi-terminal plan");
   if (!sys->vals) return fail_with(ctx, CAROLI_EINVAL, "no H values uploaded");
   for (int i = 0; i < count; ++i) {
     if (slots[i] < 0 || slots[i] >= (int)sys->slots.size() || !sys->slots[slots[i]].set)

@@ -575,6 +575,65 @@ __global__ void __launch_bounds__(256) trace_kernel(const JobDesc* __restrict__ 
   }
 }
 
+// ---- multi-terminal trace: T_pq = Tr[Γ_p G_pq Γ_q G_pq^†] for every pair of leads ------------
+// (NestedMultiTerminal::block_transmissions, nested_multi.rs:337-364). The root inverse holds G on
+// the kept orbitals (the union of the leads' orbitals); lead p occupies the kept positions
+// lpos[lptr[p] .. lptr[p + 1]), in the order of its Γ_p (np x np, column-major).
+struct MultiJob {
+  const void* g;                // root inverse (m x m), in the precision of the root
+  const int32_t* lpos;          // kept positions of every lead, concatenated
+  const int32_t* lptr;          // P + 1 offsets into lpos
+  const double2* const* gamma;  // Γ_p per lead (device pointers)
+  double2* scratch;             // P * P blocks of `smax` elements: X = G_pq Γ_q
+  double* out;                  // P * P transmissions, T[p * P + q]
+  int32_t m, nd, P, pad;
+};
+
+// grid (P * P, jobs): one CTA per pair; X = G_pq Γ_q, then Σ_{a,d} (Γ_p X)[a,d] conj(G_pq[a,d]).
+template <typename TR>
+__global__ void __launch_bounds__(256) multi_trace_kernel(const MultiJob* __restrict__ jobs, int64_t smax) {
+  using V = typename Cx<TR>::V;
+  __shared__ double red[32];
+  const MultiJob& J = jobs[blockIdx.y];
+  if ((int)blockIdx.x >= J.P * J.P) return;
+  const int p = blockIdx.x / J.P, q = blockIdx.x % J.P;
+  const int np = J.lptr[p + 1] - J.lptr[p], nq = J.lptr[q + 1] - J.lptr[q];
+  const int32_t* ip = J.lpos + J.lptr[p];
+  const int32_t* iq = J.lpos + J.lptr[q];
+  const double2* gp = J.gamma[p];
+  const double2* gq = J.gamma[q];
+  const V* Gfull = static_cast<const V*>(J.g);
+  auto G = [&](int i, int j) -> double2 {
+    const V v = Gfull[(J.nd + i) + (int64_t)(J.nd + j) * J.m];
+    return make_double2((double)v.x, (double)v.y);
+  };
+  double2* X = J.scratch + (int64_t)blockIdx.x * smax;
+  for (int64_t idx = threadIdx.x; idx < (int64_t)np * nq; idx += blockDim.x) {
+    const int b = (int)(idx % np), d = (int)(idx / np);
+    double2 acc = make_double2(0.0, 0.0);
+    for (int c = 0; c < nq; ++c) acc = cfma(acc, G(ip[b], iq[c]), gq[c + (int64_t)d * nq]);
+    X[idx] = acc;
+  }
+  __syncthreads();
+  double local = 0.0;
+  for (int64_t idx = threadIdx.x; idx < (int64_t)np * nq; idx += blockDim.x) {
+    const int a = (int)(idx % np), d = (int)(idx / np);
+    double2 y = make_double2(0.0, 0.0);
+    for (int b = 0; b < np; ++b) y = cfma(y, gp[a + (int64_t)b * np], X[b + (int64_t)d * np]);
+    const double2 g = G(ip[a], iq[d]);
+    local += y.x * g.x + y.y * g.y;
+  }
+  for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) red[w] = local;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sum = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) sum += red[k];
+    J.out[blockIdx.x] = sum;
+  }
+}
+
 __global__ void trace_finish_kernel(const double* __restrict__ part, int parts_per_job, int njobs,
                                     double* __restrict__ t_out, int32_t* __restrict__ status) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;

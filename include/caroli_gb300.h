@@ -15,6 +15,9 @@
  *   caroli_solve_batch                       transmission_with / transmission_with_precision /
  *                                            transmissions                        nested.rs:618-713
  *   caroli_scattering_states                 NestedTwoTerminal::scattering_states nested.rs:851-899
+ *   caroli_multi_leads                       NestedMultiTerminal::from_model      nested_multi.rs:61-153
+ *   caroli_multi_sigma_upload                its self_energies                    nested_multi.rs:188-199
+ *   caroli_multi_transmissions               transmissions_with_precision         nested_multi.rs:171-186
  *   caroli_transmission_with_grad            no counterpart: the reference has no derivative code;
  *   caroli_derivs_upload                     the adjoint of transmission_with (dT/dV, dT/dJ)
  *   caroli_last_error                        GreenError / GpuError text           caroli-green/src/lib.rs:34-47
@@ -170,6 +173,26 @@ int caroli_scattering_states(caroli_ctx* ctx, int plan_id, int count, const int3
                              const double* const* w_left, const int32_t* left_channels, const double* const* w_right,
                              const int32_t* right_channels, double* const* psi_left, double* const* psi_right,
                              int32_t* status);
+
+/* Multi-terminal devices (NestedMultiTerminal, crates/caroli-green/src/nested_multi.rs): any number
+ * of leads attached to the device, T_pq between every pair.
+ * 1. caroli_plan_upload with, per block, the kept orbitals (every device orbital some lead couples
+ *    to, the sites holding them excluded from `interior`) as its left list and an empty right list:
+ *    the tree's root keeps them (nested_multi.rs:64-77, :297-303).
+ * 2. caroli_multi_leads: `nleads` leads; the device orbitals of lead p in block b are
+ *    lead_orbitals[lead_ptr[b * nleads + p] .. lead_ptr[b * nleads + p + 1]) (lead_ptr[0] = 0; an
+ *    empty range for a lead the block does not reach), each one of the block's kept orbitals.
+ * 3. caroli_multi_sigma_upload: Σ_p = V_p g_p V_p^† of every (block, lead) at one energy,
+ *    sigma[b * nleads + p] column-major complex128 in the order of that lead's orbitals (NULL for an
+ *    empty lead). The root subtracts their sum (nested_multi.rs:304-318).
+ * 4. caroli_multi_transmissions: t[(i * nleads + p) * nleads + q] = T_pq = Tr[Γ_p G_pq Γ_q G_pq^†]
+ *    from lead q into lead p, summed over the blocks (nested_multi.rs:337-364), for `count`
+ *    instances (energy slot, configuration); CAROLI_DOUBLE or CAROLI_SINGLE, as the reference's
+ *    Precision. The two-terminal entry points refuse a plan with leads. */
+int caroli_multi_leads(caroli_ctx* ctx, int plan_id, int nleads, const int64_t* lead_ptr, const int64_t* lead_orbitals);
+int caroli_multi_sigma_upload(caroli_ctx* ctx, int plan_id, int slot, double energy, const double* const* sigma);
+int caroli_multi_transmissions(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots, const int32_t* configs,
+                               int precision, double* t, int32_t* status);
 
 /* caroli_solve_batch over instances of several systems (plans) at once: instance i is
  * (plan_ids[i], slots[i], configs[i]), slots and configurations of that plan. Systems of different

@@ -1,0 +1,50 @@
+"""ORACLE — test infrastructure only (tests). Multi-terminal transmissions by a dense inverse of
+the whole device, as ``MultiTerminal::solve`` and ``MultiSolution::transmission``
+(``crates/caroli-green/src/multi.rs:88-111``, ``:178-189``): A = E - H - Σ_p Σ_p (each lead's
+self-energy on the orbitals it couples to), G = A^-1, T_pq = Tr[Γ_p G_pq Γ_q G_pq^†]. It uses the
+full lead cells (no block decomposition), so it also checks the GPU path's split into independent
+blocks and its restricted leads. The reference checks NestedMultiTerminal against MultiTerminal
+the same way.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def dense_h(system, config=0):
+    n = system.n
+    h = np.zeros((n, n), np.complex128)
+    rows = np.repeat(np.arange(n), np.diff(system.row_ptr))
+    np.add.at(h, (rows, np.asarray(system.cols, np.int64)), np.asarray(system.values[config]))
+    return h
+
+
+def surface_self_energy(lead, energy):
+    """Σ = V g V^† of an attached lead, g = (E - h00 - Σ_rest)^-1 (multi.rs:43-55), with Σ_rest
+    the right self-energy of the lead cell from the mode solver."""
+    from caroli_gb300.leads import LeadSolver
+
+    rest = LeadSolver(lead.h00, lead.h01).self_energies(energy)[1]
+    m = lead.h00.shape[0]
+    g = np.linalg.inv(energy * np.eye(m) - lead.h00 - rest)
+    return lead.coupling @ g @ lead.coupling.conj().T
+
+
+def transmissions(system, leads, energy, config=0):
+    """T[p][q] of the device `system` (its H values of `config`) with the full attached leads."""
+    a = energy * np.eye(system.n) - dense_h(system, config)
+    sig = []
+    for l in leads:
+        s = surface_self_energy(l, energy)
+        a[np.ix_(l.orbitals, l.orbitals)] -= s
+        sig.append(s)
+    g = np.linalg.inv(a)
+    nl = len(leads)
+    t = np.zeros((nl, nl))
+    for p in range(nl):
+        gp = 1j * (sig[p] - sig[p].conj().T)
+        for q in range(nl):
+            gq = 1j * (sig[q] - sig[q].conj().T)
+            gpq = g[np.ix_(leads[p].orbitals, leads[q].orbitals)]
+            t[p, q] = float(np.real(np.trace(gp @ gpq @ gq @ gpq.conj().T)))
+    return t

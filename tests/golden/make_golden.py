@@ -4,7 +4,8 @@ Run in a checkout that has the caroli sources at REFERENCE (read-only input):
     python tests/golden/make_golden.py /path/to/caroli
 It reads
 - benchmarks/results/Mac-mini-de-Arnaud.jsonl: the nested-dissection (code "caroli") and RGF
-  ("caroli-rgf") transmissions of the benchmark problems of benchmarks/transport.toml;
+  ("caroli-rgf") transmissions of the benchmark problems of benchmarks/transport.toml (for the
+  four-terminal square-cross, the twelve T_pq with p != q of each energy, p-major);
 - reference/baseline/golden/ti-cond2t-clean/{axes,cond}_00.dat: the thesis conductance of the
   clean BHZ 16 x 10 ribbon (Fortran unformatted records, int32-framed float64);
 - crates/caroli-disorder/src/rng.rs: nothing (the RNG known answers are in the test itself).
@@ -35,7 +36,8 @@ def main(ref):
     for r in rows:
         if r.get("mode", "single") != "single" or r.get("code") not in ("caroli", "caroli-rgf"):
             continue
-        if r["problem"] not in ("bhz-anderson", "graphene-anderson", "square-anderson", "square-clean"):
+        if r["problem"] not in ("bhz-anderson", "graphene-anderson", "square-anderson", "square-clean",
+                                "square-cross"):
             continue
         if r["width"] not in (32, 64):
             continue
@@ -46,7 +48,9 @@ def main(ref):
                    "problems": {"square-clean": {"seed": None, "anderson": None},
                                 "square-anderson": {"seed": 1, "anderson": 2.0},
                                 "bhz-anderson": {"seed": 2, "anderson": 0.5},
-                                "graphene-anderson": {"seed": 4, "anderson": 1.0}},
+                                "graphene-anderson": {"seed": 4, "anderson": 1.0},
+                                "square-cross": {"seed": 5, "anderson": 1.0, "geometry": "cross",
+                                                 "order": "T_pq for p != q, p-major"}},
                    "results": bench}, f, indent=1)
     g = os.path.join(ref, "reference/baseline/golden/ti-cond2t-clean")
     axes = records(os.path.join(g, "axes_00.dat"))[0]

@@ -132,3 +132,47 @@ def graphene_ribbons(count, seed=1, widths=(8, 24), lengths=(12, 40), w=1.0):
         device = clean.with_onsite_term(ScalarPotential(pot, width, subs, 1))
         out.append(NestedTwoTerminal.from_model(device, clean, region, 0))
     return out
+
+
+def cross_geometry(lattice, w):
+    """A w x w square with arms of length w / 4 on its four edges and the interfaces of their
+    leads (left, right, bottom, top): the benchmark's "cross" (caroli-bench/src/main.rs:128-153)."""
+    from caroli_gb300 import Interface, Region
+    from caroli_gb300.lattice import Site
+
+    arm = w // 4
+    subs = len(lattice.sublattices)
+
+    def sites(cells):
+        return [Site((x, y, 0), s) for (x, y) in cells for s in range(subs)]
+
+    cells = [(x, y) for x in range(-arm, w + arm) for y in range(-arm, w + arm) if 0 <= x < w or 0 <= y < w]
+    column = lambda x: Region.from_sites(lattice, sites([(x, y) for y in range(w)]))
+    row = lambda y: Region.from_sites(lattice, sites([(x, y) for x in range(w)]))
+    interfaces = [Interface(column(-arm), (-1, 0, 0)), Interface(column(w + arm - 1), (1, 0, 0)),
+                  Interface(row(-arm), (0, -1, 0)), Interface(row(w + arm - 1), (0, 1, 0))]
+    return Region.from_sites(lattice, sites(cells)), interfaces
+
+
+def cross_problem(width, model="square", seed=5, anderson=1.0):
+    """The square-cross benchmark problem (benchmarks/transport.toml:54-62): Anderson disorder
+    w (u - 0.5) per site of the bounding box from xoshiro seed_from_u64(seed * 1 000 003 + W),
+    index (x ny + y) subs + sub from the box's corner (caroli-bench/src/main.rs:108-125)."""
+    from caroli_gb300 import NestedMultiTerminal
+
+    clean = CLEAN[model]() if model in CLEAN else model
+    region, interfaces = cross_geometry(clean.lattice, width)
+    arm = width // 4
+    nx = ny = width + 2 * arm
+    subs = len(clean.lattice.sublattices)
+    orb = clean.lattice.sublattices[0].orbitals
+    pot = bench_disorder(seed, width, nx, ny, subs, anderson)
+    dev = clean.with_onsite_term(ScalarPotential(pot, ny, subs, orb, origin=(-arm, -arm)))
+    return dev, clean, region, interfaces
+
+
+def cross_system(width, model="square", seed=5, anderson=1.0):
+    from caroli_gb300 import NestedMultiTerminal
+
+    dev, clean, region, interfaces = cross_problem(width, model, seed, anderson)
+    return NestedMultiTerminal.from_model(dev, clean, region, interfaces)
