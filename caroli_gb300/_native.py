@@ -47,6 +47,8 @@ SIGNATURES = {
     "caroli_solve_multi": (ctypes.c_int, [P, ctypes.c_int, P, P, P, ctypes.c_int, P, P, P]),
     "caroli_scattering_states": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P, P, P, P]),
     "caroli_multi_leads": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P]),
+    "caroli_values_generate": (ctypes.c_int, [P, ctypes.c_int, P, ctypes.c_int, P, ctypes.c_int, ctypes.c_int]),
+    "caroli_values_download": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P]),
     "caroli_multi_sigma_upload": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, ctypes.c_double, P]),
     "caroli_multi_transmissions": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, ctypes.c_int, P, P]),
     "caroli_kernel_class_name": (ctypes.c_char_p, [ctypes.c_int]),
@@ -55,6 +57,19 @@ SIGNATURES = {
 }
 
 _lib = None
+
+
+ANDERSON, MAGNETIC = 0, 1
+MOMENTS_ISOTROPIC, MOMENTS_POLARIZED, MOMENTS_CONE = 0, 1, 2
+
+
+class Disorder(ctypes.Structure):
+    """``caroli_disorder`` of the C ABI."""
+
+    _fields_ = [("kind", ctypes.c_int32), ("moments", ctypes.c_int32), ("seed", ctypes.c_uint64),
+                ("strength", ctypes.c_double), ("concentration", ctypes.c_double), ("exchange", ctypes.c_double),
+                ("moment_param", ctypes.c_double), ("orbitals", ctypes.c_int32), ("pad", ctypes.c_int32),
+                ("spin", ctypes.c_void_p)]
 
 
 class NativeError(RuntimeError):
@@ -298,6 +313,20 @@ class Plan:
                                                              ptr(pl), ptr(cl), ptr(pr), ptr(cr), ptr(po_l), ptr(po_r),
                                                              ptr(st)))
         return outs, st[:cnt]
+
+    def generate_values(self, clean_values, entries, nconfigs, first_config=0):
+        """H values of ``nconfigs`` configurations generated on the device
+        (``caroli_values_generate``): ``entries`` is a list of ``Disorder`` with the spin matrices
+        kept alive by the caller."""
+        clean = np.ascontiguousarray(clean_values, np.complex128)
+        arr = (Disorder * max(len(entries), 1))(*entries)
+        self.ctx.check(self.ctx.lib.caroli_values_generate(self.ctx.h, self.id, ptr(clean), len(entries),
+                                                           ctypes.cast(arr, ctypes.c_void_p), nconfigs, first_config))
+
+    def download_values(self, config, nnz):
+        out = np.zeros(nnz, np.complex128)
+        self.ctx.check(self.ctx.lib.caroli_values_download(self.ctx.h, self.id, config, ptr(out)))
+        return out
 
     def multi_leads(self, nleads, lead_ptr, lead_orbitals):
         """Leads of a multi-terminal plan (``caroli_multi_leads``)."""

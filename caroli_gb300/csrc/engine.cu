@@ -25,6 +25,7 @@
 #include "dense.cuh"
 #include "tiny.cuh"
 #include "sweep.cuh"
+#include "disorder.cuh"
 
 using namespace caroli;
 
@@ -144,6 +145,10 @@ struct System {
   int nleads = 0;
   std::vector<std::vector<int32_t>> mptr, mpos;
   std::vector<int32_t*> dmptr, dmpos;
+  // On-device disorder: the site of every stored entry inside an on-site block (-1 otherwise) and
+  // its (row, column) within the block.
+  int32_t* os_site = nullptr;
+  int16_t* os_ab = nullptr;
   ~System() {
     for (auto& p : plans) p->release();
     for (auto& b : blocks) b.release();
@@ -156,6 +161,8 @@ struct System {
     }
     for (auto* p : dmptr) cudaFree(p);
     for (auto* p : dmpos) cudaFree(p);
+    cudaFree(os_site);
+    cudaFree(os_ab);
   }
 };
 
@@ -274,6 +281,7 @@ struct caroli_ctx {
   Buf grhs, gptr, gdv, gdp;
   Buf states_w;  // lead factors W_L, W_R of a scattering-states call
   Buf mjobs, mscratch, mout;  // multi-terminal traces
+  Buf dent, dspin, dscal, dcoef, dflag, dtab, dclean;  // on-device disorder
   double inner_tol = 1e-10;
   bool tensor_cores = true;  // f32 rank-kb updates on tcgen05 (3xTF32); else on the CUDA cores
   int max_iters = 6;
@@ -1581,6 +1589,149 @@ int caroli_values_upload(caroli_ctx* ctx, int plan_id, int nconfigs, const doubl
     return CAROLI_OK;
   } catch (const CudaError& e) {
     return fail_with(ctx, e.e == cudaErrorMemoryAllocation ? CAROLI_ENOMEM : CAROLI_ECUDA, cudaGetErrorString(e.e));
+  }
+}
+
+int caroli_values_generate(caroli_ctx* ctx, int plan_id, const double* clean_values, int nentries,
+                           const caroli_disorder* entries, int nconfigs, int first_config) {
+  System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
+  if (!sys || !clean_values || nentries < 0 || (nentries > 0 && !entries) || nconfigs <= 0 || first_config < 0)
+    return fail_with(ctx, CAROLI_EINVAL, "caroli_values_generate: bad arguments");
+  const SystemDesc& d = sys->desc;
+  const int64_t n = d.n, nnz = d.row_ptr[n], nsites = d.nsites;
+  // Site of every orbital, and the stored entries of each site's on-site block.
+  std::vector<int32_t> site_of(n, -1);
+  for (int64_t i = 0; i < nsites; ++i)
+    for (int64_t o = d.site_offsets[i]; o < d.site_offsets[i] + d.site_orbitals[i]; ++o) site_of[o] = (int32_t)i;
+  std::vector<int32_t> os_site(std::max<int64_t>(nnz, 1), -1);
+  std::vector<int16_t> os_ab(2 * std::max<int64_t>(nnz, 1), 0);
+  std::vector<std::vector<uint8_t>> present(nsites);
+  for (int64_t r = 0; r < n; ++r)
+    for (int64_t q = d.row_ptr[r]; q < d.row_ptr[r + 1]; ++q) {
+      const int64_t c = d.cols[q];
+      const int32_t si = site_of[r];
+      if (si < 0 || site_of[c] != si) continue;
+      const int64_t k = d.site_orbitals[si];
+      const int a = (int)(r - d.site_offsets[si]), b = (int)(c - d.site_offsets[si]);
+      os_site[q] = si;
+      os_ab[2 * q] = (int16_t)a;
+      os_ab[2 * q + 1] = (int16_t)b;
+      if (present[si].empty()) present[si].assign(k * k, 0);
+      present[si][a + b * k] = 1;
+    }
+  // Entries: the pattern must hold every on-site entry a term can make non-zero.
+  std::vector<DisorderDev> ent(nentries);
+  std::vector<double2> spin;
+  std::vector<size_t> spin_off(nentries, 0);
+  for (int e = 0; e < nentries; ++e) {
+    const caroli_disorder& x = entries[e];
+    DisorderDev& y = ent[e];
+    y.kind = x.kind;
+    y.moments = x.moments;
+    y.seed = x.seed;
+    y.strength = x.strength;
+    y.exchange = x.exchange;
+    y.mparam = x.moment_param;
+    y.orb = x.orbitals;
+    if (x.kind == CAROLI_ANDERSON) {
+      for (int64_t i = 0; i < nsites; ++i)
+        for (int64_t a = 0; a < d.site_orbitals[i]; ++a)
+          if (present[i].empty() || !present[i][a + a * d.site_orbitals[i]])
+            return fail_with(ctx, CAROLI_EINVAL, "caroli_values_generate: the pattern lacks an on-site diagonal entry");
+    } else if (x.kind == CAROLI_MAGNETIC) {
+      if (!x.spin || x.orbitals <= 0 || x.orbitals > 32 || x.concentration < 0.0 || x.concentration > 1.0 ||
+          x.moments < CAROLI_MOMENTS_ISOTROPIC || x.moments > CAROLI_MOMENTS_CONE)
+        return fail_with(ctx, CAROLI_EINVAL, "caroli_values_generate: bad magnetic entry");
+      y.n_imp = (int32_t)(x.concentration * (double)nsites);
+      const int64_t k = x.orbitals;
+      spin_off[e] = spin.size();
+      for (int64_t m = 0; m < 3 * k * k; ++m) spin.push_back(make_double2(x.spin[2 * m], x.spin[2 * m + 1]));
+      for (int64_t i = 0; i < nsites; ++i) {
+        if (d.site_orbitals[i] != k)
+          return fail_with(ctx, CAROLI_EINVAL, "caroli_values_generate: spin matrices of another orbital count");
+        // n = z exactly (m_z = 1, or a cone of zero angle): S_x and S_y get exact zeros.
+        const bool only_z = (x.moments == CAROLI_MOMENTS_POLARIZED && x.moment_param == 1.0) ||
+                            (x.moments == CAROLI_MOMENTS_CONE && x.moment_param == 0.0);
+        for (int64_t m = 0; m < k * k; ++m) {
+          bool nz = false;
+          for (int sidx = only_z ? 2 : 0; sidx < 3; ++sidx)
+            nz |= x.spin[2 * (sidx * k * k + m)] != 0.0 || x.spin[2 * (sidx * k * k + m) + 1] != 0.0;
+          if (nz && (present[i].empty() || !present[i][m]))
+            return fail_with(ctx, CAROLI_EINVAL, "caroli_values_generate: the pattern lacks an on-site entry of the spin");
+        }
+      }
+    } else {
+      return fail_with(ctx, CAROLI_EINVAL, "caroli_values_generate: unknown disorder kind");
+    }
+  }
+  try {
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    if (!sys->os_site) {
+      sys->os_site = upload_vec(os_site, s);
+      sys->os_ab = upload_vec(os_ab, s);
+    }
+    double2* dspin = static_cast<double2*>(ctx->dspin.get(std::max<size_t>(spin.size(), 1) * sizeof(double2)));
+    if (!spin.empty()) CK(cudaMemcpyAsync(dspin, spin.data(), spin.size() * sizeof(double2), cudaMemcpyHostToDevice, s));
+    for (int e = 0; e < nentries; ++e) ent[e].spin = dspin + spin_off[e];
+    DisorderDev* dent = static_cast<DisorderDev*>(ctx->dent.get(std::max<size_t>(nentries, 1) * sizeof(DisorderDev)));
+    if (nentries) CK(cudaMemcpyAsync(dent, ent.data(), nentries * sizeof(DisorderDev), cudaMemcpyHostToDevice, s));
+    const size_t per = (size_t)std::max(nentries, 1) * nconfigs * (size_t)std::max<int64_t>(nsites, 1);
+    double* scal = static_cast<double*>(ctx->dscal.get(per * sizeof(double)));
+    double* coef = static_cast<double*>(ctx->dcoef.get(per * 3 * sizeof(double)));
+    uint8_t* flag = static_cast<uint8_t*>(ctx->dflag.get(per));
+    int32_t* tab = static_cast<int32_t*>(ctx->dtab.get(per * sizeof(int32_t)));
+    double2* clean = static_cast<double2*>(ctx->dclean.get(std::max<int64_t>(nnz, 1) * sizeof(double2)));
+    if (nnz) CK(cudaMemcpyAsync(clean, clean_values, nnz * sizeof(double2), cudaMemcpyHostToDevice, s));
+    const size_t count = (size_t)nnz * nconfigs;
+    if (!sys->vals || sys->vals_count != count) {
+      cudaFree(sys->vals);
+      sys->vals = nullptr;
+      sys->vals_count = 0;
+      sys->vals = dalloc<double2>(std::max<size_t>(count, 1));
+      sys->vals_count = count;
+    }
+    int64_t launches = 0;
+    const int threads = nentries * nconfigs;
+    if (threads > 0) {
+      disorder_draw_kernel<<<(threads + 31) / 32, 32, 0, s>>>(dent, nentries, nconfigs, first_config, (int)nsites, scal,
+                                                                coef, flag, tab);
+      CK(cudaGetLastError());
+      ++launches;
+    }
+    if (nnz > 0)
+      in_pieces((size_t)nconfigs, [&](size_t c0, size_t c) {
+        disorder_apply_kernel<<<dim3((unsigned)((nnz + 255) / 256), (unsigned)c), 256, 0, s>>>(
+            dent, nentries, nconfigs, (int)nsites, nnz, clean, sys->os_site, sys->os_ab, scal + c0 * nsites,
+            coef + c0 * nsites * 3, flag + c0 * nsites, sys->vals + c0 * nnz);
+        CK(cudaGetLastError());
+        ++launches;
+      });
+    CK(cudaStreamSynchronize(s));
+    ctx->last_launches = launches;
+    ctx->region_launches += launches;
+    sys->nconfigs = nconfigs;
+    return CAROLI_OK;
+  } catch (const CudaError& e) {
+    return fail_with(ctx, e.e == cudaErrorMemoryAllocation ? CAROLI_ENOMEM : CAROLI_ECUDA,
+                     std::string(e.what) + ": " + cudaGetErrorString(e.e));
+  }
+}
+
+int caroli_values_download(caroli_ctx* ctx, int plan_id, int config, double* values) {
+  System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
+  if (!sys || !values || !sys->vals || config < 0 || config >= sys->nconfigs)
+    return fail_with(ctx, CAROLI_EINVAL, "caroli_values_download: bad arguments");
+  try {
+    CK(cudaSetDevice(ctx->device));
+    const size_t nnz = (size_t)sys->desc.row_ptr[sys->desc.n];
+    if (nnz)
+      CK(cudaMemcpyAsync(values, sys->vals + (size_t)config * nnz, nnz * sizeof(double2), cudaMemcpyDeviceToHost,
+                         ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return CAROLI_OK;
+  } catch (const CudaError& e) {
+    return fail_with(ctx, CAROLI_ECUDA, cudaGetErrorString(e.e));
   }
 }
 

@@ -27,6 +27,7 @@ raises ``GreenError("Singular", …)`` as ``GreenError::Singular`` (nested.rs:79
 """
 from __future__ import annotations
 
+import math
 from dataclasses import dataclass
 
 import numpy as np
@@ -99,10 +100,62 @@ class NestedTwoTerminal:
         out.sites = list(region.sites)
         return out
 
+    @staticmethod
+    def from_disorder(clean_model, lead, region, axis, entries, nconfigs, first_config=0, device=0):
+        """``nconfigs`` disorder configurations of the CLI's ``[[disorder]]`` entries
+        (``caroli-cli/src/build.rs:251-310``; the dicts of ``disorder.disordered``) generated on the
+        GPU (``caroli_values_generate``): configuration c is the CLI's configuration
+        ``first_config + c``. The pattern holds every on-site entry the entries can fill."""
+        from . import disorder as dis
+        from .model import SparseMatrix
+
+        n = region.orbitals
+        offs = region.offsets()
+        norb = region.site_orbital_counts()
+        touched = {}
+        for d in entries:
+            if d["kind"] == "anderson":
+                for k in set(int(x) for x in norb):
+                    touched.setdefault(k, np.zeros((k, k), bool))[np.arange(k), np.arange(k)] = True
+            elif d["kind"] == "magnetic":
+                mom = d.get("moments", dis.Moments.isotropic())
+                spin = [np.asarray(m, np.complex128) for m in d["spin"]]
+                k = spin[0].shape[0]
+                # n = z exactly for m_z = 1 or a zero cone: only S_z can fill entries.
+                only_z = (mom.kind == "polarized" and mom.mz == 1.0) or (mom.kind == "cone" and mom.theta0 == 0.0)
+                used = spin[2:] if only_z else spin
+                mask = touched.setdefault(k, np.zeros((k, k), bool))
+                for m in used:
+                    mask |= m != 0
+            else:
+                raise ValueError(f"unknown disorder {d['kind']}")
+        rows, cols = [], []
+        for i in range(len(region)):
+            mask = touched.get(int(norb[i]))
+            if mask is None:
+                continue
+            a, b = np.nonzero(mask)
+            rows.append(offs[i] + a)
+            cols.append(offs[i] + b)
+        rows = np.concatenate(rows) if rows else np.zeros(0, np.int64)
+        cols = np.concatenate(cols) if cols else np.zeros(0, np.int64)
+        extra = SparseMatrix.from_triplets(n, rows, cols, np.ones(len(rows), np.complex128))
+        system = build_system([clean_model], lead, region, axis, extra=extra)
+        out = NestedTwoTerminal(system, device)
+        out.sites = list(region.sites)
+        out._disorder = (entries, int(nconfigs), int(first_config))
+        return out
+
+    def generated_values(self, config):
+        """H values of configuration ``config`` as the device holds them (on the system's pattern)."""
+        return self.plan().download_values(config, self.system.nnz)
+
     def block_count(self):
         return len(self.system.blocks)
 
     def config_count(self):
+        if getattr(self, "_disorder", None) is not None:
+            return self._disorder[1]
         return self.system.config_count()
 
     # -- self-energies ------------------------------------------------------------------------
@@ -118,8 +171,34 @@ class NestedTwoTerminal:
     def plan(self):
         if self._plan is None:
             self._plan = _native.Plan(context(self.device), self.system)
-            self._plan.upload_values(self.system.values)
+            if getattr(self, "_disorder", None) is not None:
+                self._generate(*self._disorder)
+            else:
+                self._plan.upload_values(self.system.values)
         return self._plan
+
+    def _generate(self, entries, nconfigs, first_config):
+        from . import disorder as dis
+
+        structs, keep = [], []
+        for k, d in enumerate(entries):
+            seed = int(d.get("seed", 1 + 1000 * k))
+            if d["kind"] == "anderson":
+                structs.append(_native.Disorder(kind=_native.ANDERSON, seed=seed, strength=float(d["strength"])))
+                continue
+            mom = d.get("moments", dis.Moments.isotropic())
+            kinds = {"isotropic": _native.MOMENTS_ISOTROPIC, "polarized": _native.MOMENTS_POLARIZED,
+                     "cone": _native.MOMENTS_CONE}
+            param = mom.mz if mom.kind == "polarized" else (-(1.0 - math.cos(mom.theta0)) if mom.kind == "cone" else 0.0)
+            spin = np.ascontiguousarray(np.stack([np.asfortranarray(m, np.complex128).ravel(order="F")
+                                                  for m in d["spin"]]))
+            keep.append(spin)
+            structs.append(_native.Disorder(kind=_native.MAGNETIC, moments=kinds[mom.kind], seed=seed,
+                                            concentration=float(d["concentration"]), exchange=float(d["exchange"]),
+                                            moment_param=float(param), orbitals=int(spin.shape[1] ** 0.5 + 0.5),
+                                            spin=spin.ctypes.data))
+        self._plan.generate_values(self.system.values[0], structs, nconfigs, first_config)
+        del keep
 
     def _slot(self, sigma: LeadSelfEnergies):
         if len(sigma.blocks) != len(self.system.blocks):

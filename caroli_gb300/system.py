@@ -111,15 +111,22 @@ def lead_cell(lead: Model, cell: Region, step, along):
     return h00, h01
 
 
-def build_system(devices, lead: Model, region: Region, axis: int) -> System:
-    """The description of ``devices`` (one model per disorder configuration, same geometry)."""
+def build_system(devices, lead: Model, region: Region, axis: int, extra: SparseMatrix = None) -> System:
+    """The description of ``devices`` (one model per disorder configuration, same geometry).
+    ``extra``: entries added to the pattern (zero in every configuration) and counted as couplings
+    for the blocks, e.g. the on-site entries that disorder generated on the device can fill."""
     if isinstance(devices, Model):
         devices = [devices]
     for hop in lead.hoppings:
         if abs(hop.offset[axis]) > 1:
             raise ValueError(f"a lead hopping skips a cell along axis {axis}")
     mats = [d.sparse_hamiltonian(region) for d in devices]
-    row_ptr, cols, values = merge_patterns(mats)
+    if extra is not None:
+        row_ptr, cols, values = merge_patterns(mats + [extra])
+        structural = values.pop() != 0
+    else:
+        row_ptr, cols, values = merge_patterns(mats)
+        structural = None
     n = region.orbitals
     slices = region.slices(axis)
     first, last = slices[0], slices[-1]
@@ -143,7 +150,7 @@ def build_system(devices, lead: Model, region: Region, axis: int) -> System:
 
     # Components of the nonzero entries of H (any configuration) and of the lead matrices.
     rows = np.repeat(np.arange(n, dtype=np.int64), np.diff(row_ptr))
-    nz = np.zeros(len(cols), bool)
+    nz = np.zeros(len(cols), bool) if structural is None else structural.copy()
     for v in values:
         nz |= v != 0
     ei, ej = [rows[nz]], [cols[nz].astype(np.int64)]

@@ -15,6 +15,8 @@
  *   caroli_solve_batch                       transmission_with / transmission_with_precision /
  *                                            transmissions                        nested.rs:618-713
  *   caroli_scattering_states                 NestedTwoTerminal::scattering_states nested.rs:851-899
+ *   caroli_values_generate                   the CLI's per-configuration disorder  caroli-cli/src/build.rs:251-310
+ *   caroli_values_download                   (reads the generated values back)
  *   caroli_multi_leads                       NestedMultiTerminal::from_model      nested_multi.rs:61-153
  *   caroli_multi_sigma_upload                its self_energies                    nested_multi.rs:188-199
  *   caroli_multi_transmissions               transmissions_with_precision         nested_multi.rs:171-186
@@ -90,6 +92,41 @@ int caroli_plan_fronts(caroli_ctx* ctx, int plan_id, int block, int64_t capacity
 /* H values of `nconfigs` disorder configurations on the plan's pattern: values[c*nnz + q] as
  * interleaved complex128 (re, im). Replaces previously uploaded values. */
 int caroli_values_upload(caroli_ctx* ctx, int plan_id, int nconfigs, const double* values);
+
+/* On-device disorder: the H values of `nconfigs` configurations generated on the GPU (no host
+ * model build, no values upload), bit for bit the CLI's [[disorder]] entries
+ * (caroli-cli/src/build.rs:251-310; caroli-disorder/src/{rng,lib}.rs). Configuration c of the
+ * result is configuration first_config + c of the sequence: entry e draws from xoshiro256**
+ * seed_from_u64(seed_e + first_config + c) (the CLI's seed_e is 1 + 1000 e unless the entry sets
+ * one). Values = clean_values (interleaved complex128 on the plan's pattern) plus, on each site's
+ * on-site block, every entry's term in order:
+ *   CAROLI_ANDERSON  w (u - 1/2) on the diagonal of every site, sites in region order;
+ *   CAROLI_MAGNETIC  floor(concentration * nsites) impurity sites (partial Fisher-Yates), a unit
+ *                    moment each (CAROLI_MOMENTS_ISOTROPIC; _POLARIZED, moment_param = m_z; _CONE,
+ *                    moment_param = -(1 - cos θ0)), and J (n_x S_x + n_y S_y + n_z S_z) on the
+ *                    site, spin = S_x, S_y, S_z (orbitals x orbitals column-major complex128 each).
+ * The pattern must hold every on-site entry a term can make non-zero (CAROLI_EINVAL otherwise).
+ * Products and sums are rounded as the host rounds them: the values equal the host-built ones
+ * exactly, except that the azimuth's cos and sin (isotropic and cone moments) may differ from the
+ * host's libm in the last bit. Replaces the uploaded values. */
+enum { CAROLI_ANDERSON = 0, CAROLI_MAGNETIC = 1 };
+enum { CAROLI_MOMENTS_ISOTROPIC = 0, CAROLI_MOMENTS_POLARIZED = 1, CAROLI_MOMENTS_CONE = 2 };
+typedef struct caroli_disorder {
+  int32_t kind;           /* CAROLI_ANDERSON or CAROLI_MAGNETIC */
+  int32_t moments;        /* CAROLI_MOMENTS_* (magnetic) */
+  uint64_t seed;          /* configuration c draws from seed_from_u64(seed + c) */
+  double strength;        /* Anderson w */
+  double concentration;   /* magnetic: impurities per site */
+  double exchange;        /* magnetic: J */
+  double moment_param;    /* m_z (polarized) or -(1 - cos θ0) (cone) */
+  int32_t orbitals;       /* magnetic: orbitals of every site (size of the spin matrices) */
+  int32_t pad;
+  const double* spin;     /* magnetic: S_x, S_y, S_z */
+} caroli_disorder;
+int caroli_values_generate(caroli_ctx* ctx, int plan_id, const double* clean_values, int nentries,
+                           const caroli_disorder* entries, int nconfigs, int first_config);
+/* The values of configuration `config` (nnz interleaved complex128) as the device holds them. */
+int caroli_values_download(caroli_ctx* ctx, int plan_id, int config, double* values);
 
 /* Lead self-energies of energy slot `slot` (any slot number; re-uploading replaces it):
  * sigma_l[b], sigma_r[b] are column-major complex128 (nl_b x nl_b, nr_b x nr_b) of block b.
