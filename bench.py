@@ -54,12 +54,35 @@ def build_workload(length=200, width=64, configs=8, energies=33):
     region = Region.cuboid(m.lattice, [length, width, 0])
     entry = {"kind": "magnetic", "concentration": 0.2, "exchange": 0.4, "moments": Moments.polarized(1.0),
              "spin": bhz_spin("opposite-g")}
+    t0 = time.perf_counter()
     devices = [disordered(m, region, [entry], c) for c in range(configs)]
     sys_ = NestedTwoTerminal.from_models(devices, m, region, 0)
+    sys_._host_build_s = time.perf_counter() - t0  # the configurations' H values built on the host
+    sys_._workload = (m, region, [entry], configs)
     es = np.linspace(-0.16, 0.16, energies)
     sigmas = [sys_.self_energies(e) for e in es]
     pairs = [(s, c) for s in sigmas for c in range(configs)]
     return sys_, sigmas, pairs
+
+
+def time_generation(sys_, ctx):
+    """The workload's configurations generated on the device (caroli_values_generate) instead of
+    built on the host and uploaded: device time, and whether the values are the host's exactly."""
+    from caroli_gb300 import NestedTwoTerminal
+
+    m, region, entries, configs = sys_._workload
+    gen = NestedTwoTerminal.from_disorder(m, m, region, 0, entries, configs)
+    gen.plan()  # plan upload and a first generation
+    ctx.region_begin()
+    gen._generate(*gen._disorder)
+    ms, launches = ctx.region_end()
+    same_pattern = np.array_equal(gen.system.row_ptr, sys_.system.row_ptr) and np.array_equal(
+        gen.system.cols, sys_.system.cols)
+    identical = same_pattern and all(np.array_equal(gen.generated_values(c), sys_.system.values[c])
+                                     for c in range(configs))
+    return {"configs": configs, "device_ms": ms, "launches": int(launches),
+            "host_build_s": sys_._host_build_s, "values_identical_to_host": bool(identical),
+            "h2d_bytes_saved": int(sum(v.nbytes for v in sys_.system.values))}
 
 
 class Clocks:
@@ -300,6 +323,7 @@ def run_ours(args):
         sys_.solve_batch(S, C, Precision.MIXED)
     e2e_ms, _ = ctx.region_end()
     e2e_wall = time.perf_counter() - e0
+    gen = time_generation(sys_, ctx) if rank == 0 else None
     # Per-kernel probe (untimed pass per class): the dominant kernel and its roofline.
     names = ctx.kernel_classes()
     probe = {}
@@ -373,6 +397,7 @@ def run_ours(args):
         "e2e": {"value": nsolve * args.steps / (e2e_ms * 1e-3), "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "wall_s": e2e_wall},
         "gpu_launches": int(launches),
+        "inputs_on_device": gen,
         "roofline": roof,
         "kernels_ms_per_step": kernels,
         "clocks": clk.summary(),
