@@ -48,6 +48,9 @@ SIGNATURES = {
     "caroli_scattering_states": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P, P, P, P]),
     "caroli_multi_leads": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P]),
     "caroli_values_generate": (ctypes.c_int, [P, ctypes.c_int, P, ctypes.c_int, P, ctypes.c_int, ctypes.c_int]),
+    "caroli_lead_modes": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, P,
+                                         ctypes.c_double]),
+    "caroli_sigma_from_modes": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, ctypes.c_double, P, P, P, P, P]),
     "caroli_values_download": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P]),
     "caroli_multi_sigma_upload": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, ctypes.c_double, P]),
     "caroli_multi_transmissions": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, ctypes.c_int, P, P]),
@@ -313,6 +316,28 @@ class Plan:
                                                              ptr(pl), ptr(cl), ptr(pr), ptr(cr), ptr(po_l), ptr(po_r),
                                                              ptr(st)))
         return outs, st[:cnt]
+
+    def lead_modes(self, block, side, y, sc):
+        """Cell eigenvectors of a block's lead with a scalar coupling (``caroli_lead_modes``)."""
+        y = np.asfortranarray(y, dtype=np.complex128)
+        self.ctx.check(self.ctx.lib.caroli_lead_modes(self.ctx.h, self.id, block, side, y.shape[0], ptr(y), sc))
+
+    def sigma_from_modes(self, slot, energy, blocks):
+        """``blocks[b] = (1/λ_L, λ_R, channel modes, channel weights)`` (``caroli_sigma_from_modes``)."""
+        keep = []
+
+        def arr(x, dt):
+            a = np.ascontiguousarray(x if len(x) else np.zeros(1), dtype=dt)
+            keep.append(a)
+            return a
+
+        dl = np.array([arr(b[0], np.complex128).ctypes.data for b in blocks], dtype=np.uintp)
+        dr = np.array([arr(b[1], np.complex128).ctypes.data for b in blocks], dtype=np.uintp)
+        nc = np.array([len(b[2]) for b in blocks], dtype=np.int32)
+        cm = np.array([arr(b[2], np.int32).ctypes.data for b in blocks], dtype=np.uintp)
+        cw = np.array([arr(b[3], np.float64).ctypes.data for b in blocks], dtype=np.uintp)
+        self.ctx.check(self.ctx.lib.caroli_sigma_from_modes(self.ctx.h, self.id, slot, energy, ptr(dl), ptr(dr),
+                                                            ptr(nc), ptr(cm), ptr(cw)))
 
     def generate_values(self, clean_values, entries, nconfigs, first_config=0):
         """H values of ``nconfigs`` configurations generated on the device

@@ -26,6 +26,7 @@
 #include "tiny.cuh"
 #include "sweep.cuh"
 #include "disorder.cuh"
+#include "leadsig.cuh"
 
 using namespace caroli;
 
@@ -149,6 +150,10 @@ struct System {
   // its (row, column) within the block.
   int32_t* os_site = nullptr;
   int16_t* os_ab = nullptr;
+  // Lead modes for self-energies on the device: per side (left, right) and block, the
+  // eigenvectors Y of the lead cell (slice x slice) and s c.
+  std::vector<double2*> lead_y[2];
+  std::vector<double> lead_sc[2];
   ~System() {
     for (auto& p : plans) p->release();
     for (auto& b : blocks) b.release();
@@ -163,6 +168,8 @@ struct System {
     for (auto* p : dmpos) cudaFree(p);
     cudaFree(os_site);
     cudaFree(os_ab);
+    for (auto& v : lead_y)
+      for (auto* p : v) cudaFree(p);
   }
 };
 
@@ -282,6 +289,7 @@ struct caroli_ctx {
   Buf states_w;  // lead factors W_L, W_R of a scattering-states call
   Buf mjobs, mscratch, mout;  // multi-terminal traces
   Buf dent, dspin, dscal, dcoef, dflag, dtab, dclean;  // on-device disorder
+  Buf lead_d, lead_cols, lead_w;                       // self-energies from lead modes
   double inner_tol = 1e-10;
   bool tensor_cores = true;  // f32 rank-kb updates on tcgen05 (3xTF32); else on the CUDA cores
   int max_iters = 6;
@@ -2091,33 +2099,136 @@ int caroli_multi_transmissions(caroli_ctx* ctx, int plan_id, int count, const in
   }
 }
 
+}  // extern "C"
+
+namespace {
+
+// The device buffers of energy slot `slot` (sized by the blocks' lead slices, W_R for up to nr
+// channels), allocated on first use: uploading the next energy into a slot only copies. The slot
+// is marked unset until its caller has filled it.
+SigmaSlot& slot_buffers(System* sys, int slot) {
+  if ((int)sys->slots.size() <= slot) sys->slots.resize(slot + 1);
+  SigmaSlot& sg = sys->slots[slot];
+  const size_t nblocks = sys->plans.size();
+  if (sg.sl.size() != nblocks) {
+    for (auto* v : {&sg.sl, &sg.sr, &sg.gl, &sg.gr, &sg.wr}) {
+      for (auto* p : *v) cudaFree(p);
+      v->clear();
+    }
+    for (size_t b = 0; b < nblocks; ++b) {
+      const size_t nl = sys->plans[b]->host.nl, nr = sys->plans[b]->host.nr;
+      sg.sl.push_back(dalloc<double2>(std::max<size_t>(nl * nl, 1)));
+      sg.sr.push_back(dalloc<double2>(std::max<size_t>(nr * nr, 1)));
+      sg.gl.push_back(dalloc<double2>(std::max<size_t>(nl * nl, 1)));
+      sg.gr.push_back(dalloc<double2>(std::max<size_t>(nr * nr, 1)));
+      sg.wr.push_back(dalloc<double2>(std::max<size_t>(nr * nr, 1)));
+    }
+  }
+  sg.channels.assign(nblocks, 0);
+  sg.set = false;
+  return sg;
+}
+
+}  // namespace
+
+extern "C" {
+
+int caroli_lead_modes(caroli_ctx* ctx, int plan_id, int block, int side, int n, const double* y, double sc) {
+  System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
+  if (!sys || block < 0 || block >= (int)sys->plans.size() || (side != 0 && side != 1) || !y)
+    return fail_with(ctx, CAROLI_EINVAL, "caroli_lead_modes: bad arguments");
+  const FrontPlan& P = sys->plans[block]->host;
+  if (n != (side == 0 ? P.nl : P.nr)) return fail_with(ctx, CAROLI_EINVAL, "caroli_lead_modes: n is not the slice size");
+  try {
+    CK(cudaSetDevice(ctx->device));
+    const size_t nb = sys->plans.size();
+    if (sys->lead_y[side].size() != nb) {
+      sys->lead_y[side].assign(nb, nullptr);
+      sys->lead_sc[side].assign(nb, 0.0);
+    }
+    cudaFree(sys->lead_y[side][block]);
+    sys->lead_y[side][block] = dalloc<double2>(std::max<size_t>((size_t)n * n, 1));
+    if (n) CK(cudaMemcpyAsync(sys->lead_y[side][block], y, (size_t)n * n * sizeof(double2), cudaMemcpyHostToDevice,
+                              ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    sys->lead_sc[side][block] = sc;
+    return CAROLI_OK;
+  } catch (const CudaError& e) {
+    return fail_with(ctx, e.e == cudaErrorMemoryAllocation ? CAROLI_ENOMEM : CAROLI_ECUDA, cudaGetErrorString(e.e));
+  }
+}
+
+int caroli_sigma_from_modes(caroli_ctx* ctx, int plan_id, int slot, double energy, const double* const* d_left,
+                            const double* const* d_right, const int32_t* channels, const int32_t* const* channel_modes,
+                            const double* const* channel_weights) {
+  System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
+  if (!sys || slot < 0 || !d_left || !d_right || !channels || !channel_modes || !channel_weights)
+    return fail_with(ctx, CAROLI_EINVAL, "caroli_sigma_from_modes: bad arguments");
+  const int nb = (int)sys->plans.size();
+  for (int side = 0; side < 2; ++side)
+    if ((int)sys->lead_y[side].size() != nb) return fail_with(ctx, CAROLI_EINVAL, "caroli_sigma_from_modes: no lead modes");
+  for (int b = 0; b < nb; ++b) {
+    const FrontPlan& P = sys->plans[b]->host;
+    if (!sys->lead_y[0][b] || !sys->lead_y[1][b] || !d_left[b] || !d_right[b])
+      return fail_with(ctx, CAROLI_EINVAL, "caroli_sigma_from_modes: missing lead modes of a block");
+    if (channels[b] < 0 || channels[b] > P.nr || (channels[b] && (!channel_modes[b] || !channel_weights[b])))
+      return fail_with(ctx, CAROLI_EINVAL, "caroli_sigma_from_modes: bad channels");
+    for (int c = 0; c < channels[b]; ++c)
+      if (channel_modes[b][c] < 0 || channel_modes[b][c] >= P.nr)
+        return fail_with(ctx, CAROLI_EINVAL, "caroli_sigma_from_modes: channel mode out of range");
+  }
+  try {
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    SigmaSlot& sg = slot_buffers(sys, slot);
+    int nmax = 1;
+    for (int b = 0; b < nb; ++b) nmax = std::max(nmax, std::max(sys->plans[b]->host.nl, sys->plans[b]->host.nr));
+    double2* dd = static_cast<double2*>(ctx->lead_d.get(2 * (size_t)nmax * sizeof(double2)));
+    int32_t* dcols = static_cast<int32_t*>(ctx->lead_cols.get((size_t)nmax * sizeof(int32_t)));
+    double* dw = static_cast<double*>(ctx->lead_w.get((size_t)nmax * sizeof(double)));
+    for (int b = 0; b < nb; ++b) {
+      const FrontPlan& P = sys->plans[b]->host;
+      for (int side = 0; side < 2; ++side) {
+        const int n = side == 0 ? P.nl : P.nr;
+        if (!n) continue;
+        double2* d = dd + (size_t)side * nmax;
+        CK(cudaMemcpyAsync(d, side == 0 ? d_left[b] : d_right[b], (size_t)n * sizeof(double2), cudaMemcpyHostToDevice, s));
+        double2* S = side == 0 ? sg.sl[b] : sg.sr[b];
+        double2* G = side == 0 ? sg.gl[b] : sg.gr[b];
+        const unsigned t = (unsigned)((n + LS_TILE - 1) / LS_TILE);
+        lead_sigma_kernel<<<dim3(t, t), 256, 0, s>>>(sys->lead_y[side][b], n, d, sys->lead_sc[side][b], S);
+        CK(cudaGetLastError());
+        lead_gamma_kernel<<<(unsigned)(((int64_t)n * n + 255) / 256), 256, 0, s>>>(S, n, G);
+        CK(cudaGetLastError());
+      }
+      const int nc = channels[b];
+      if (nc) {
+        CK(cudaMemcpyAsync(dcols, channel_modes[b], nc * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dw, channel_weights[b], nc * sizeof(double), cudaMemcpyHostToDevice, s));
+        lead_channels_kernel<<<(unsigned)(((int64_t)P.nr * nc + 255) / 256), 256, 0, s>>>(sys->lead_y[1][b], P.nr, dcols,
+                                                                                        dw, nc, sg.wr[b]);
+        CK(cudaGetLastError());
+      }
+      sg.channels[b] = nc;
+      // The host vectors of this block must outlive the copies: synchronise per block.
+      CK(cudaStreamSynchronize(s));
+    }
+    sg.energy = energy;
+    sg.set = true;
+    return CAROLI_OK;
+  } catch (const CudaError& e) {
+    return fail_with(ctx, e.e == cudaErrorMemoryAllocation ? CAROLI_ENOMEM : CAROLI_ECUDA, cudaGetErrorString(e.e));
+  }
+}
+
 int caroli_sigma_upload(caroli_ctx* ctx, int plan_id, int slot, double energy, const double* const* sigma_l,
                         const double* const* sigma_r, const double* const* w_right, const int32_t* channels) {
   System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
   if (!sys || slot < 0 || !sigma_l || !sigma_r) return fail_with(ctx, CAROLI_EINVAL, "caroli_sigma_upload: bad arguments");
   try {
     CK(cudaSetDevice(ctx->device));
-    if ((int)sys->slots.size() <= slot) sys->slots.resize(slot + 1);
-    SigmaSlot& sg = sys->slots[slot];
-    // A slot keeps its device buffers (sized by the blocks' lead slices, W_R for up to nr
-    // channels), so uploading the next energy into it only copies.
+    SigmaSlot& sg = slot_buffers(sys, slot);
     const size_t nblocks = sys->plans.size();
-    if (sg.sl.size() != nblocks) {
-      for (auto* v : {&sg.sl, &sg.sr, &sg.gl, &sg.gr, &sg.wr}) {
-        for (auto* p : *v) cudaFree(p);
-        v->clear();
-      }
-      for (size_t b = 0; b < nblocks; ++b) {
-        const size_t nl = sys->plans[b]->host.nl, nr = sys->plans[b]->host.nr;
-        sg.sl.push_back(dalloc<double2>(std::max<size_t>(nl * nl, 1)));
-        sg.sr.push_back(dalloc<double2>(std::max<size_t>(nr * nr, 1)));
-        sg.gl.push_back(dalloc<double2>(std::max<size_t>(nl * nl, 1)));
-        sg.gr.push_back(dalloc<double2>(std::max<size_t>(nr * nr, 1)));
-        sg.wr.push_back(dalloc<double2>(std::max<size_t>(nr * nr, 1)));
-      }
-    }
-    sg.channels.assign(nblocks, 0);
-    sg.set = false;
     std::vector<std::vector<double>> keep;  // host data of the asynchronous copies
     auto put = [&](double2* d, const double* h, size_t count) {
       if (count) CK(cudaMemcpyAsync(d, h, count * sizeof(double2), cudaMemcpyHostToDevice, ctx->stream));

@@ -89,8 +89,32 @@ class LeadSolver:
                 last = GreenError("Eigen", str(err))
         raise last
 
+    def definite_roots(self, energy):
+        """For a scalar coupling ``h01 = s c 1``: ``(1/λ_L, λ_R, energy used)`` per mode of the cell
+        eigenvectors ``self.cell[3]`` (shifted off band edges as ``self_energies``), so that
+        ``Σ_L = s c Y diag(1/λ_L) Y^†`` and ``Σ_R = s c Y diag(λ_R) Y^†``."""
+        if self.cell is None:
+            raise ValueError("the lead coupling is not a multiple of the identity")
+        last = GreenError("Eigen")
+        for shift in SHIFTS:
+            e = energy + shift * self.scale
+            try:
+                lam_l, lam_r = self._definite_roots(e)
+                return 1.0 / lam_l, lam_r, e
+            except GreenError as err:
+                last = err
+        raise last
+
     # -- h01 = s c 1: one Hermitian problem ------------------------------------------------------
     def _definite(self, e):
+        s, c, theta, y = self.cell
+        lam_l, lam_r = self._definite_roots(e)
+        # Σ_R = h01 F_+ with F_+ = Y λ_R Y†;  Σ_L = h01† F_-^-1 with F_-^-1 = Y λ_L^-1 Y†.
+        sig_r = (s * c) * (y * lam_r) @ y.conj().T
+        sig_l = (s * c) * (y * (1.0 / lam_l)) @ y.conj().T
+        return sig_l, sig_r
+
+    def _definite_roots(self, e):
         s, c, theta, y = self.cell
         mu = -(theta - e) / (s * c)
         lam_r = np.empty(len(mu), np.complex128)
@@ -110,10 +134,7 @@ class LeadSolver:
                 if abs(big) <= 1.0 + UNIT_TOL:
                     raise GreenError("Singular", f"subband edge near E = {e}")
                 lam_r[k], lam_l[k] = 1.0 / big, big
-        # Σ_R = h01 F_+ with F_+ = Y λ_R Y†;  Σ_L = h01† F_-^-1 with F_-^-1 = Y λ_L^-1 Y†.
-        sig_r = (s * c) * (y * lam_r) @ y.conj().T
-        sig_l = (s * c) * (y * (1.0 / lam_l)) @ y.conj().T
-        return sig_l, sig_r
+        return lam_l, lam_r
 
     # -- general coupling: the 2n pencil ---------------------------------------------------------
     def _general(self, e):

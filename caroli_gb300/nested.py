@@ -63,6 +63,19 @@ class LeadSelfEnergies:
         return self._w_left
 
 
+@dataclass
+class ModeSelfEnergies:
+    """Self-energies of every block at one energy, to be formed on the GPU from the leads' modes
+    (``caroli_sigma_from_modes``): per block ``(1/λ_L, λ_R, open channels, channel weights)`` of
+    leads with a scalar coupling (the definite fast path of ``modes.rs:540-710``)."""
+
+    energy: float
+    blocks: list
+
+    def key(self):
+        return id(self)
+
+
 _CONTEXTS = {}
 
 
@@ -200,7 +213,45 @@ class NestedTwoTerminal:
         self._plan.generate_values(self.system.values[0], structs, nconfigs, first_config)
         del keep
 
-    def _slot(self, sigma: LeadSelfEnergies):
+    def leads_on_device(self):
+        """Whether every block's leads have a scalar coupling ``h01 = s c 1`` (square and cubic
+        leads): their self-energies can then be formed on the GPU (``self_energies_on_device``)."""
+        return all(l.cell is not None and r.cell is not None for l, r in self._solvers)
+
+    def self_energies_on_device(self, energy) -> ModeSelfEnergies:
+        """The self-energies of ``self_energies(energy)``, classified here per transverse mode
+        (O(n) per lead) and formed on the GPU when used: no host products, no eigendecomposition
+        of Γ_R, no copies of Σ."""
+        if not self.leads_on_device():
+            raise ValueError("a lead coupling is not a multiple of the identity")
+        blocks = []
+        for left, right in self._solvers:
+            dl = left.definite_roots(energy)[0]
+            _, lam_r, _ = right.definite_roots(energy)
+            s, c = right.cell[0], right.cell[1]
+            open_ = np.nonzero(lam_r.imag != 0.0)[0]
+            weights = np.sqrt(-2.0 * s * c * lam_r.imag[open_])
+            blocks.append((dl, lam_r, open_.astype(np.int32), weights))
+        return ModeSelfEnergies(float(energy), blocks)
+
+    def _upload_lead_modes(self, plan):
+        for b, (left, right) in enumerate(self._solvers):
+            for side, solver in ((0, left), (1, right)):
+                s, c, _, y = solver.cell
+                plan.lead_modes(b, side, y, s * c)
+
+    def _slot(self, sigma):
+        if isinstance(sigma, ModeSelfEnergies):
+            key = id(sigma)
+            if key not in self._slot_of or self._slot_of[key][1] is not sigma:
+                plan = self.plan()
+                if not getattr(self, "_modes_uploaded", False):
+                    self._upload_lead_modes(plan)
+                    self._modes_uploaded = True
+                slot = len(self._slot_of)
+                plan.sigma_from_modes(slot, sigma.energy, sigma.blocks)
+                self._slot_of[key] = (slot, sigma)
+            return self._slot_of[key][0]
         if len(sigma.blocks) != len(self.system.blocks):
             raise ValueError("self-energies of a system with other blocks")
         for (sl, sr), b in zip(sigma.blocks, self.system.blocks):

@@ -15,6 +15,8 @@
  *   caroli_solve_batch                       transmission_with / transmission_with_precision /
  *                                            transmissions                        nested.rs:618-713
  *   caroli_scattering_states                 NestedTwoTerminal::scattering_states nested.rs:851-899
+ *   caroli_lead_modes, caroli_sigma_from_modes  self_energies with a Hermitian definite lead coupling
+ *                                            (DefiniteCoupling, modes.rs:514-713), Σ formed on the GPU
  *   caroli_values_generate                   the CLI's per-configuration disorder  caroli-cli/src/build.rs:251-310
  *   caroli_values_download                   (reads the generated values back)
  *   caroli_multi_leads                       NestedMultiTerminal::from_model      nested_multi.rs:61-153
@@ -137,6 +139,23 @@ int caroli_values_download(caroli_ctx* ctx, int plan_id, int config, double* val
  * (Γ_R slightly indefinite). */
 int caroli_sigma_upload(caroli_ctx* ctx, int plan_id, int slot, double energy, const double* const* sigma_l,
                         const double* const* sigma_r, const double* const* w_right, const int32_t* channels);
+
+/* Self-energies formed on the GPU for leads with a Hermitian definite coupling H1 = s c 1 (square
+ * and cubic leads; the fast path of modes.rs:540-710, "P = c 1": the eigenvectors Y of the cell
+ * Hamiltonian serve every energy).
+ * caroli_lead_modes: once per block and side (0 left, 1 right), Y (n x n column-major complex128,
+ * n = the slice's orbitals in lead-cell order) and sc = s c.
+ * caroli_sigma_from_modes: one energy into slot `slot`, from the per-mode roots the caller
+ * classified (O(n) scalar work, modes.rs:641-668): d_left[b] = 1/λ_L and d_right[b] = λ_R (n
+ * complex128 each), and the right lead's open channels (channel_modes[b], channels[b] of them, with
+ * weights sqrt(-2 s c Im λ_R)). On the device: Σ_R = sc Y diag(λ_R) Y^†, Σ_L = sc Y diag(1/λ_L) Y^†
+ * (FP64), Γ = i (Σ - Σ^†), and W_R = Y[:, channel_modes] diag(weights) with W_R W_R^† = Γ_R: what
+ * caroli_sigma_upload would receive, without the host products, the eigendecomposition of Γ_R and
+ * the copies. */
+int caroli_lead_modes(caroli_ctx* ctx, int plan_id, int block, int side, int n, const double* y, double sc);
+int caroli_sigma_from_modes(caroli_ctx* ctx, int plan_id, int slot, double energy, const double* const* d_left,
+                            const double* const* d_right, const int32_t* channels, const int32_t* const* channel_modes,
+                            const double* const* channel_weights);
 
 /* T for `count` instances (energy slot, configuration), summed over the blocks.
  *   precision       CAROLI_DOUBLE, CAROLI_SINGLE or CAROLI_MIXED
