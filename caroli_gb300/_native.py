@@ -47,6 +47,7 @@ SIGNATURES = {
     "caroli_solve_multi": (ctypes.c_int, [P, ctypes.c_int, P, P, P, ctypes.c_int, P, P, P]),
     "caroli_scattering_states": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P, P, P, P]),
     "caroli_multi_leads": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P]),
+    "caroli_multi_scattering_states": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P]),
     "caroli_values_generate": (ctypes.c_int, [P, ctypes.c_int, P, ctypes.c_int, P, ctypes.c_int, ctypes.c_int]),
     "caroli_lead_modes": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, P,
                                          ctypes.c_double]),
@@ -365,6 +366,30 @@ class Plan:
         mats = [None if m is None else np.asfortranarray(m, dtype=np.complex128) for row in sigmas for m in row]
         pt = np.array([0 if m is None or m.size == 0 else m.ctypes.data for m in mats] or [0], dtype=np.uintp)
         self.ctx.check(self.ctx.lib.caroli_multi_sigma_upload(self.ctx.h, self.id, slot, energy, ptr(pt)))
+
+    def multi_scattering_states(self, slots, configs, w, n, nleads):
+        """``w[i][b][p]``: W of lead p in block b for instance i (np x channels, or None).
+        Returns ``(states, status)`` with ``states[i]`` the list of ψ_p (n x channels)."""
+        slots = np.ascontiguousarray(slots, np.int32)
+        configs = np.ascontiguousarray(configs, np.int32)
+        cnt = len(slots)
+        mats = [None if m is None else np.asfortranarray(m, dtype=np.complex128)
+                for inst in w for blk in inst for m in blk]
+        pw = np.array([0 if m is None or m.size == 0 else m.ctypes.data for m in mats] or [0], dtype=np.uintp)
+        ch = np.array([0 if m is None else m.shape[1] for m in mats] or [0], dtype=np.int32)
+        nb = self.nblocks
+        outs = []
+        for i in range(cnt):
+            per = []
+            for p in range(nleads):
+                cols = sum(int(ch[(i * nb + b) * nleads + p]) for b in range(nb))
+                per.append(np.zeros((n, cols), np.complex128, order="F"))
+            outs.append(per)
+        po = np.array([m.ctypes.data if m.size else 0 for per in outs for m in per] or [0], dtype=np.uintp)
+        st = np.zeros(max(cnt, 1), np.int32)
+        self.ctx.check(self.ctx.lib.caroli_multi_scattering_states(self.ctx.h, self.id, cnt, ptr(slots), ptr(configs),
+                                                                   ptr(pw), ptr(ch), ptr(po), ptr(st)))
+        return outs, st[:cnt]
 
     def multi_solve(self, slots, configs, precision, nleads):
         slots = np.ascontiguousarray(slots, np.int32)

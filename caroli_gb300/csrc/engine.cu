@@ -231,6 +231,8 @@ struct StatesRequest {
   std::vector<const double2*> wl, wr;
   std::vector<int> cl, cr;
   std::vector<std::vector<double2>>* psi = nullptr;
+  // Multi-terminal sources: an explicit right-hand side per job (nblk x (cl + cr)) instead of W_L, W_R.
+  std::vector<const double2*> rhs;
 };
 
 // One tree level of a batch: its fronts split by size class, and their algorithmic work.
@@ -287,6 +289,7 @@ struct caroli_ctx {
   TaskCache tcache;
   Buf grhs, gptr, gdv, gdp;
   Buf states_w;  // lead factors W_L, W_R of a scattering-states call
+  Buf states_rhs;  // multi-terminal sources
   Buf mjobs, mscratch, mout;  // multi-terminal traces
   Buf dent, dspin, dscal, dcoef, dflag, dtab, dclean;  // on-device disorder
   Buf lead_d, lead_cols, lead_w;                       // self-energies from lead modes
@@ -435,8 +438,12 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
     R.whole = adjoint;
     R.rhs = adjoint ? rhs[j] : nullptr;
     if (states) {
-      R.w_l = states->wl[begin + j];
-      R.w_r = states->wr[begin + j];
+      if (!states->rhs.empty()) {
+        R.rhs = states->rhs[begin + j];
+      } else {
+        R.w_l = states->wl[begin + j];
+        R.w_r = states->wr[begin + j];
+      }
       R.cl = states->cl[begin + j];
       R.c = R.cl + states->cr[begin + j];
       R.whole = 1;
@@ -2132,6 +2139,130 @@ SigmaSlot& slot_buffers(System* sys, int slot) {
 }  // namespace
 
 extern "C" {
+
+int caroli_multi_scattering_states(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots,
+                                   const int32_t* configs, const double* const* w, const int32_t* channels,
+                                   double* const* psi, int32_t* status) {
+  System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
+  if (!sys || count < 0 || (count > 0 && (!slots || !configs || !w || !channels || !psi || !status)))
+    return fail_with(ctx, CAROLI_EINVAL, "caroli_multi_scattering_states: bad arguments");
+  if (sys->nleads <= 0) return fail_with(ctx, CAROLI_EINVAL, "caroli_multi_scattering_states: no leads");
+  if (!sys->vals) return fail_with(ctx, CAROLI_EINVAL, "no H values uploaded");
+  const int nb = (int)sys->plans.size(), P = sys->nleads;
+  for (int i = 0; i < count; ++i) {
+    if (slots[i] < 0 || slots[i] >= (int)sys->slots.size() || !sys->slots[slots[i]].set ||
+        sys->slots[slots[i]].mtab.empty())
+      return fail_with(ctx, CAROLI_EINVAL, "energy slot without multi-terminal self-energies");
+    if (configs[i] < 0 || configs[i] >= sys->nconfigs) return fail_with(ctx, CAROLI_EINVAL, "configuration out of range");
+    for (int p = 0; p < P; ++p) {
+      int64_t cols = 0;
+      for (int b = 0; b < nb; ++b) {
+        const size_t q = ((size_t)i * nb + b) * P + p;
+        const int np = sys->mptr[b][p + 1] - sys->mptr[b][p];
+        if (channels[q] < 0 || channels[q] > np || (channels[q] && !w[q]))
+          return fail_with(ctx, CAROLI_EINVAL, "caroli_multi_scattering_states: bad lead factor");
+        cols += channels[q];
+      }
+      if (cols && !psi[(size_t)i * P + p]) return fail_with(ctx, CAROLI_EINVAL, "caroli_multi_scattering_states: missing output");
+    }
+  }
+  try {
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    ctx->last_ms = 0.0;
+    ctx->last_launches = 0;
+    ctx->factor_ms = ctx->root_ms = ctx->tail_ms = 0.0;
+    ctx->refine_iters = 0;
+    ctx->fallbacks = 0;
+    ctx->refine_job_steps = ctx->refine_batch_steps = 0;
+    std::vector<JobSpec> specs;
+    StatesRequest rq;
+    std::vector<size_t> roff, woff;
+    size_t relems = 0, welems = 0;
+    for (int i = 0; i < count; ++i)
+      for (int b = 0; b < nb; ++b) {
+        specs.push_back({b, slots[i], configs[i], sys->plans[b].get(), sys});
+        int c = 0;
+        for (int p = 0; p < P; ++p) {
+          const size_t q = ((size_t)i * nb + b) * P + p;
+          woff.push_back(welems);
+          welems += (size_t)(sys->mptr[b][p + 1] - sys->mptr[b][p]) * channels[q];
+          c += channels[q];
+        }
+        rq.cl.push_back(c);
+        rq.cr.push_back(0);
+        roff.push_back(relems);
+        relems += (size_t)sys->blocks[b].nblk * c;
+      }
+    double2* rhs = static_cast<double2*>(ctx->states_rhs.get(std::max<size_t>(relems, 1) * sizeof(double2)));
+    double2* wd = static_cast<double2*>(ctx->states_w.get(std::max<size_t>(welems, 1) * sizeof(double2)));
+    CK(cudaMemsetAsync(rhs, 0, std::max<size_t>(relems, 1) * sizeof(double2), s));
+    for (size_t j = 0; j < specs.size(); ++j) {
+      const int b = specs[j].block;
+      int c0 = 0;
+      for (int p = 0; p < P; ++p) {
+        const size_t q = j * P + p;
+        const int np = sys->mptr[b][p + 1] - sys->mptr[b][p], c = channels[q];
+        if (np && c) {
+          CK(cudaMemcpyAsync(wd + woff[q], w[q], (size_t)np * c * sizeof(double2), cudaMemcpyHostToDevice, s));
+          scatter_sources_kernel<<<(unsigned)(((int64_t)np * c + 255) / 256), 256, 0, s>>>(
+              rhs + roff[j], sys->blocks[b].nblk, c0, sys->blocks[b].left_local, sys->dmpos[b] + sys->mptr[b][p], np,
+              wd + woff[q], c);
+          CK(cudaGetLastError());
+        }
+        c0 += c;
+      }
+      rq.rhs.push_back(rhs + roff[j]);
+      rq.wl.push_back(nullptr);
+      rq.wr.push_back(nullptr);
+    }
+    CK(cudaStreamSynchronize(s));
+    std::vector<std::vector<double2>> x(specs.size());
+    rq.psi = &x;
+    std::vector<JobOut> jo;
+    run_jobs<float, float>(ctx, sys, specs, MODE_MIXED, jo, nullptr, &rq);
+    const int64_t n = sys->desc.n;
+    for (int i = 0; i < count; ++i) {
+      int32_t st = ST_OK;
+      for (int p = 0; p < P; ++p) {
+        int64_t cols = 0;
+        for (int b = 0; b < nb; ++b) cols += channels[((size_t)i * nb + b) * P + p];
+        if (cols) std::fill(psi[(size_t)i * P + p], psi[(size_t)i * P + p] + 2 * (size_t)n * cols, 0.0);
+      }
+      std::vector<int64_t> c0p(P, 0);  // next output column of each lead
+      for (int b = 0; b < nb; ++b) {
+        const size_t j = (size_t)i * nb + b;
+        if (st == ST_OK) st = jo[j].status;
+        const auto& orbs = sys->trees[b].orbitals;
+        const size_t nblk = orbs.size();
+        int c0 = 0;
+        for (int p = 0; p < P; ++p) {
+          const int c = channels[j * P + p];
+          for (int k = 0; k < c; ++k) {
+            if (x[j].size() < nblk * (size_t)(c0 + k + 1)) {
+              if (st == ST_OK) st = ST_NONFINITE;
+              continue;
+            }
+            double* dst = psi[(size_t)i * P + p] + 2 * (size_t)n * (c0p[p] + k);
+            for (size_t a = 0; a < nblk; ++a) {
+              const double2 v = x[j][a + (size_t)(c0 + k) * nblk];
+              if (st == ST_OK && !(std::isfinite(v.x) && std::isfinite(v.y))) st = ST_NONFINITE;
+              dst[2 * orbs[a]] = v.x;
+              dst[2 * orbs[a] + 1] = v.y;
+            }
+          }
+          c0 += c;
+          c0p[p] += c;
+        }
+      }
+      status[i] = st;
+    }
+    return CAROLI_OK;
+  } catch (const CudaError& e) {
+    return fail_with(ctx, e.e == cudaErrorMemoryAllocation ? CAROLI_ENOMEM : CAROLI_ECUDA,
+                     std::string(e.what) + ": " + cudaGetErrorString(e.e));
+  }
+}
 
 int caroli_lead_modes(caroli_ctx* ctx, int plan_id, int block, int side, int n, const double* y, double sc) {
   System* sys = ctx ? get_system(ctx, plan_id) : nullptr;

@@ -477,6 +477,20 @@ __global__ void gm_residual_kernel(RefineDesc* __restrict__ rd, int njobs) {
 
 namespace caroli {
 
+// Multi-terminal sources: W_p (np x c, column-major) on the block-local rows of lead p's orbitals,
+// rows[a] = left_local[pos[a]], into columns c0 .. c0 + c of B (nblk rows). grid: np x c elements.
+__global__ void scatter_sources_kernel(double2* __restrict__ B, int nblk, int c0, const int32_t* __restrict__ left_local,
+                                       const int32_t* __restrict__ pos, int np, const double2* __restrict__ W, int c) {
+  const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (idx >= (int64_t)np * c) return;
+  const int a = (int)(idx % np), k = (int)(idx / np);
+  const int row = left_local[pos[a]];
+  const double2 w = W[idx];
+  double2& dst = B[row + (int64_t)(c0 + k) * nblk];
+  dst.x += w.x;
+  dst.y += w.y;
+}
+
 // Right-hand side of the adjoint solve: Γ_L x_j on the left slice (x from the forward solve).
 // grid (jobs, row chunks).
 __global__ void __launch_bounds__(256) grad_rhs_kernel(const RefineDesc* __restrict__ fwd, double2* const* rhs) {

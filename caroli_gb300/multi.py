@@ -256,6 +256,55 @@ class NestedMultiTerminal:
         return [t[i] if st[i] == _native.OK else GreenError("Singular", f"solve status {st[i]} at E = {e}")
                 for i, e in enumerate(energies)]
 
+    # -- scattering states (nested_multi.rs:382-438) and what is built from them --------------
+    def scattering_states_batch(self, energies, configs=None):
+        """``ScatteringStates`` (one ψ_p per lead) of each (energy, configuration) pair in one GPU
+        batch; a failed point is a ``GreenError`` in its place."""
+        from .leads import gamma_root
+        from .states import ScatteringStates
+
+        if configs is None:
+            configs = [0] * len(energies)
+        sig = {}
+        for e in energies:
+            if float(e) not in sig:
+                sig[float(e)] = self.self_energies(e)
+        sigmas = [sig[float(e)] for e in energies]
+        slots = [self._slot(s) for s in sigmas]
+        roots = {id(s): [[None if x is None else gamma_root(x) for x in blk] for blk in s.blocks] for s in sigmas}
+        outs, st = self.plan().multi_scattering_states(slots, configs, [roots[id(s)] for s in sigmas],
+                                                       self.system.n, self.nleads)
+        res = []
+        for psi, code, e, c in zip(outs, st, energies, configs):
+            if code != _native.OK:
+                res.append(GreenError("Singular", f"solve status {code} at E = {e}"))
+            else:
+                res.append(ScatteringStates(float(e), psi, int(c)))
+        return res
+
+    def scattering_states(self, energy, config=0):
+        """``ψ_p = G W_p`` on every device orbital for every lead (nested_multi.rs:382)."""
+        out = self.scattering_states_batch([energy], [config])[0]
+        if isinstance(out, GreenError):
+            raise out
+        return out
+
+    def bond_currents(self, states, f):
+        """``2 Re Tr[H_ij G^<_ji]`` of every bond, one occupation per lead (nested_multi.rs:497)."""
+        from . import states as st
+
+        return st.bond_currents(self.system, states, f, None, self.sites)
+
+    def operator_currents(self, states, f, op):
+        from . import states as st
+
+        return st.bond_currents(self.system, states, f, op, self.sites)
+
+    def site_densities(self, states, f, op=None):
+        from . import states as st
+
+        return st.site_densities(self.system, states, f, op)
+
 
 def lead_voltages(t, currents, ground):
     """Lead voltages in linear response (Landauer–Büttiker) from the transmissions ``t[p][q]`` and

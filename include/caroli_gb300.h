@@ -22,6 +22,7 @@
  *   caroli_multi_leads                       NestedMultiTerminal::from_model      nested_multi.rs:61-153
  *   caroli_multi_sigma_upload                its self_energies                    nested_multi.rs:188-199
  *   caroli_multi_transmissions               transmissions_with_precision         nested_multi.rs:171-186
+ *   caroli_multi_scattering_states           its scattering_states                nested_multi.rs:382-438
  *   caroli_transmission_with_grad            no counterpart: the reference has no derivative code;
  *   caroli_derivs_upload                     the adjoint of transmission_with (dT/dV, dT/dJ)
  *   caroli_last_error                        GreenError / GpuError text           caroli-green/src/lib.rs:34-47
@@ -246,6 +247,16 @@ int caroli_scattering_states(caroli_ctx* ctx, int plan_id, int count, const int3
  *    instances (energy slot, configuration); CAROLI_DOUBLE or CAROLI_SINGLE, as the reference's
  *    Precision. The two-terminal entry points refuse a plan with leads. */
 int caroli_multi_leads(caroli_ctx* ctx, int plan_id, int nleads, const int64_t* lead_ptr, const int64_t* lead_orbitals);
+/* Scattering states of a multi-terminal device (NestedMultiTerminal::scattering_states,
+ * nested_multi.rs:382-438): ψ_p = G W_p for every lead p. For instance i, block b and lead p
+ * (q = (i * nblocks + b) * nleads + p), w[q] is np x channels[q] column-major complex128 with
+ * W W^† = Γ_p on the lead's orbitals in the order of caroli_multi_leads (NULL for no channel).
+ * psi[i * nleads + p] receives n x Σ_b channels columns, block b's after those of the blocks
+ * before it, zero outside the block. Runs the mixed path (f32 factors, FP64 GMRES converged on the
+ * whole of X), as caroli_scattering_states. */
+int caroli_multi_scattering_states(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots,
+                                   const int32_t* configs, const double* const* w, const int32_t* channels,
+                                   double* const* psi, int32_t* status);
 int caroli_multi_sigma_upload(caroli_ctx* ctx, int plan_id, int slot, double energy, const double* const* sigma);
 int caroli_multi_transmissions(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots, const int32_t* configs,
                                int precision, double* t, int32_t* status);

@@ -48,3 +48,21 @@ def transmissions(system, leads, energy, config=0):
             gpq = g[np.ix_(leads[p].orbitals, leads[q].orbitals)]
             t[p, q] = float(np.real(np.trace(gp @ gpq @ gq @ gpq.conj().T)))
     return t
+
+
+def spectral(system, leads, energy, config=0):
+    """G Γ_p G^† (dense, whole device) of every lead: the spectral function the scattering states
+    of lead p carry, ψ_p ψ_p^† (nested_multi.rs:376-381)."""
+    a = energy * np.eye(system.n) - dense_h(system, config)
+    sig = []
+    for l in leads:
+        s = surface_self_energy(l, energy)
+        a[np.ix_(l.orbitals, l.orbitals)] -= s
+        sig.append(s)
+    g = np.linalg.inv(a)
+    out = []
+    for l, s in zip(leads, sig):
+        gam = np.zeros((system.n, system.n), np.complex128)
+        gam[np.ix_(l.orbitals, l.orbitals)] = 1j * (s - s.conj().T)
+        out.append(g @ gam @ g.conj().T)
+    return out

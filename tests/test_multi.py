@@ -151,3 +151,45 @@ def test_gpu_multi_configs_and_errors():
         multi.plan().solve([slot], [0], int(Precision.DOUBLE))
     t, st = multi.plan().multi_solve([], [], int(Precision.DOUBLE), 4)
     assert t.shape == (0, 4, 4)
+
+
+# -- multi-terminal scattering states ------------------------------------------------------------
+def _arm_current(currents, lead):
+    """Net bond current from the centre of a cross into the arm of `lead` (left, right, bottom,
+    top): across x = 0 / x = w - 1 / y = 0 / y = w - 1."""
+    tot = 0.0
+    for b in currents:
+        a, c = b.from_.cell, b.to.cell
+        inside = {0: lambda s: s[0] < 0, 1: lambda s: s[0] >= W_ARM, 2: lambda s: s[1] < 0,
+                  3: lambda s: s[1] >= W_ARM}[lead]
+        if inside(c) and not inside(a):
+            tot += b.current
+        elif inside(a) and not inside(c):
+            tot -= b.current
+    return tot
+
+
+W_ARM = 12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("model,seed,w,energy", [("square", 5, 1.0, 0.9), ("bhz", 3, 0.5, 0.05)])
+def test_gpu_multi_states_spectral_and_currents(model, seed, w, energy):
+    """ψ_p ψ_p^† = G Γ_p G^† of the dense oracle for every lead, and with lead p filled (f = e_p)
+    the current into the arm of lead q equals T_qp."""
+    from oracle import multi as om
+
+    s = cross_system(W_ARM, model=model, seed=seed, anderson=w)
+    dev, clean, region, interfaces = cross_problem(W_ARM, model=model, seed=seed, anderson=w)
+    leads = _full_leads(dev, clean, region, interfaces)
+    st = s.scattering_states(energy)
+    ref = om.spectral(s.system, leads, energy)
+    for psi, g in zip(st.leads, ref):
+        assert np.max(np.abs(psi @ psi.conj().T - g)) <= 1e-9 * max(1.0, np.abs(g).max())
+    t = s.transmissions(energy)
+    for p in range(4):
+        f = [1.0 if k == p else 0.0 for k in range(4)]
+        cur = s.bond_currents(st, f)
+        for q in range(4):
+            if q != p:
+                assert abs(_arm_current(cur, q) - t[q][p]) < 1e-9
