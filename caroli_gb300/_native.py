@@ -48,6 +48,8 @@ SIGNATURES = {
     "caroli_scattering_states": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P, P, P, P]),
     "caroli_multi_leads": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P]),
     "caroli_multi_scattering_states": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P]),
+    "caroli_multi_sector_transmissions": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, ctypes.c_int,
+                                                         ctypes.c_int, P, P, P, P]),
     "caroli_values_generate": (ctypes.c_int, [P, ctypes.c_int, P, ctypes.c_int, P, ctypes.c_int, ctypes.c_int]),
     "caroli_lead_modes": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, P,
                                          ctypes.c_double]),
@@ -390,6 +392,22 @@ class Plan:
         self.ctx.check(self.ctx.lib.caroli_multi_scattering_states(self.ctx.h, self.id, cnt, ptr(slots), ptr(configs),
                                                                    ptr(pw), ptr(ch), ptr(po), ptr(st)))
         return outs, st[:cnt]
+
+    def multi_sector(self, slot, config, precision, label_lead, gammas):
+        """One instance of ``caroli_multi_sector_transmissions``: ``gammas[b][k]`` per block and
+        label (or None). Returns ``(t, status)`` with t nlabels x nlabels."""
+        nl = len(label_lead)
+        mats = [None if g is None else np.asfortranarray(g, dtype=np.complex128) for row in gammas for g in row]
+        pg = np.array([0 if m is None or m.size == 0 else m.ctypes.data for m in mats] or [0], dtype=np.uintp)
+        ll = np.ascontiguousarray(label_lead, np.int32)
+        sl = np.array([slot], np.int32)
+        cf = np.array([config], np.int32)
+        t = np.zeros((nl, nl))
+        st = np.zeros(1, np.int32)
+        self.ctx.check(self.ctx.lib.caroli_multi_sector_transmissions(self.ctx.h, self.id, 1, ptr(sl), ptr(cf),
+                                                                      precision, nl, ptr(ll), ptr(pg), ptr(t),
+                                                                      ptr(st)))
+        return t, int(st[0])
 
     def multi_solve(self, slots, configs, precision, nleads):
         slots = np.ascontiguousarray(slots, np.int32)

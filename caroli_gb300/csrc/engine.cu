@@ -209,6 +209,17 @@ struct JobSpec {
   int block, slot, config;
   const DevPlan* plan;
   System* sys;
+  int inst = -1;  // the caller's instance (sector transmissions)
+};
+
+// Sector transmissions of multi-terminal jobs: trace labels in place of the leads. Label k of a
+// block sits at the positions of its lead (lptr/lpos per block, device and host copies); its Γ per
+// (instance, block) in a device table of P pointers.
+struct SectorRequest {
+  int P = 0, nblocks = 0;
+  std::vector<std::vector<int32_t>> hptr;
+  std::vector<const int32_t*> lptr, lpos;       // per block
+  std::vector<const double2* const*> gam;       // per (instance, block)
 };
 
 // Device state of one refinement (forward, or the adjoint of the gradient).
@@ -290,6 +301,8 @@ struct caroli_ctx {
   Buf grhs, gptr, gdv, gdp;
   Buf states_w;  // lead factors W_L, W_R of a scattering-states call
   Buf states_rhs;  // multi-terminal sources
+  const SectorRequest* sector = nullptr;  // set during caroli_multi_sector_transmissions
+  Buf sec_pos, sec_ptr, sec_gam, sec_tab;
   Buf mjobs, mscratch, mout;  // multi-terminal traces
   Buf dent, dspin, dscal, dcoef, dflag, dtab, dclean;  // on-device disorder
   Buf lead_d, lead_cols, lead_w;                       // self-energies from lead modes
@@ -1133,22 +1146,31 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
       std::vector<size_t> midx;
       int64_t smax = 1;
       int pmax = 0;
+      const SectorRequest* sec = ctx->sector;
       for (size_t j = 0; j < cj; ++j) {
         const JobSpec& sp = specs[begin + j];
         if (sp.sys->nleads <= 0) continue;
-        const std::vector<int32_t>& lp = sp.sys->mptr[sp.block];
-        for (int a = 0; a < sp.sys->nleads; ++a)
-          for (int b = 0; b < sp.sys->nleads; ++b)
+        const bool labels = sec && sp.inst >= 0;
+        const int P = labels ? sec->P : sp.sys->nleads;
+        const std::vector<int32_t>& lp = labels ? sec->hptr[sp.block] : sp.sys->mptr[sp.block];
+        for (int a = 0; a < P; ++a)
+          for (int b = 0; b < P; ++b)
             smax = std::max<int64_t>(smax, (int64_t)(lp[a + 1] - lp[a]) * (lp[b + 1] - lp[b]));
-        pmax = std::max(pmax, sp.sys->nleads);
+        pmax = std::max(pmax, P);
         MultiJob m{};
         m.g = rarena + root_off[j];
-        m.lpos = sp.sys->dmpos[sp.block];
-        m.lptr = sp.sys->dmptr[sp.block];
-        m.gamma = sp.sys->slots[sp.slot].mtab[sp.block];
+        if (labels) {
+          m.lpos = sec->lpos[sp.block];
+          m.lptr = sec->lptr[sp.block];
+          m.gamma = sec->gam[(size_t)sp.inst * sec->nblocks + sp.block];
+        } else {
+          m.lpos = sp.sys->dmpos[sp.block];
+          m.lptr = sp.sys->dmptr[sp.block];
+          m.gamma = sp.sys->slots[sp.slot].mtab[sp.block];
+        }
         m.m = sp.plan->host.fronts[sp.plan->host.root].n;
         m.nd = sp.plan->host.nd;
-        m.P = sp.sys->nleads;
+        m.P = P;
         mj.push_back(m);
         midx.push_back(j);
       }
@@ -1268,7 +1290,7 @@ void solve_with_delays(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>&
       auto dp = std::make_unique<DevPlan>();
       dp->host = make_plan(specs[j].sys->desc, tree, delayed[j]);
       dp->upload(ctx->stream);
-      again.push_back({specs[j].block, specs[j].slot, specs[j].config, dp.get(), specs[j].sys});
+      again.push_back({specs[j].block, specs[j].slot, specs[j].config, dp.get(), specs[j].sys, specs[j].inst});
       plans.push_back(std::move(dp));
     }
     std::vector<JobOut> res;
@@ -2139,6 +2161,126 @@ SigmaSlot& slot_buffers(System* sys, int slot) {
 }  // namespace
 
 extern "C" {
+
+int caroli_multi_sector_transmissions(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots,
+                                      const int32_t* configs, int precision, int nlabels, const int32_t* label_lead,
+                                      const double* const* gammas, double* t, int32_t* status) {
+  System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
+  if (!sys || count < 0 || nlabels <= 0 || !label_lead ||
+      (count > 0 && (!slots || !configs || !gammas || !t || !status)))
+    return fail_with(ctx, CAROLI_EINVAL, "caroli_multi_sector_transmissions: bad arguments");
+  if (sys->nleads <= 0) return fail_with(ctx, CAROLI_EINVAL, "caroli_multi_sector_transmissions: no leads");
+  if (precision != CAROLI_DOUBLE && precision != CAROLI_SINGLE)
+    return fail_with(ctx, CAROLI_EINVAL, "caroli_multi_sector_transmissions: CAROLI_DOUBLE or CAROLI_SINGLE");
+  if (!sys->vals) return fail_with(ctx, CAROLI_EINVAL, "no H values uploaded");
+  const int nb = (int)sys->plans.size(), P = nlabels;
+  for (int k = 0; k < P; ++k)
+    if (label_lead[k] < 0 || label_lead[k] >= sys->nleads)
+      return fail_with(ctx, CAROLI_EINVAL, "caroli_multi_sector_transmissions: label of an unknown lead");
+  for (int i = 0; i < count; ++i) {
+    if (slots[i] < 0 || slots[i] >= (int)sys->slots.size() || !sys->slots[slots[i]].set ||
+        sys->slots[slots[i]].mtab.empty())
+      return fail_with(ctx, CAROLI_EINVAL, "energy slot without multi-terminal self-energies");
+    if (configs[i] < 0 || configs[i] >= sys->nconfigs) return fail_with(ctx, CAROLI_EINVAL, "configuration out of range");
+    for (int b = 0; b < nb; ++b)
+      for (int k = 0; k < P; ++k) {
+        const int p = label_lead[k];
+        if (sys->mptr[b][p + 1] > sys->mptr[b][p] && !gammas[((size_t)i * nb + b) * P + k])
+          return fail_with(ctx, CAROLI_EINVAL, "caroli_multi_sector_transmissions: missing Γ");
+      }
+  }
+  try {
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    ctx->last_ms = 0.0;
+    ctx->last_launches = 0;
+    ctx->factor_ms = ctx->root_ms = ctx->tail_ms = 0.0;
+    ctx->fallbacks = 0;
+    ctx->refine_iters = 0;
+    ctx->refine_job_steps = ctx->refine_batch_steps = 0;
+    SectorRequest rq;
+    rq.P = P;
+    rq.nblocks = nb;
+    // Label positions per block: those of the label's lead.
+    std::vector<int32_t> hpos, hptr;
+    std::vector<size_t> pos_off(nb), ptr_off(nb);
+    for (int b = 0; b < nb; ++b) {
+      std::vector<int32_t> lp(1, 0);
+      pos_off[b] = hpos.size();
+      for (int k = 0; k < P; ++k) {
+        const int p = label_lead[k];
+        for (int32_t q = sys->mptr[b][p]; q < sys->mptr[b][p + 1]; ++q) hpos.push_back(sys->mpos[b][q]);
+        lp.push_back((int32_t)(hpos.size() - pos_off[b]));
+      }
+      ptr_off[b] = hptr.size();
+      hptr.insert(hptr.end(), lp.begin(), lp.end());
+      rq.hptr.push_back(lp);
+    }
+    int32_t* dpos = static_cast<int32_t*>(ctx->sec_pos.get(std::max<size_t>(hpos.size(), 1) * sizeof(int32_t)));
+    int32_t* dptr = static_cast<int32_t*>(ctx->sec_ptr.get(std::max<size_t>(hptr.size(), 1) * sizeof(int32_t)));
+    if (!hpos.empty()) CK(cudaMemcpyAsync(dpos, hpos.data(), hpos.size() * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dptr, hptr.data(), hptr.size() * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    for (int b = 0; b < nb; ++b) {
+      rq.lpos.push_back(dpos + pos_off[b]);
+      rq.lptr.push_back(dptr + ptr_off[b]);
+    }
+    // Γ of every (instance, block, label), and per (instance, block) a table of P pointers.
+    size_t gel = 0;
+    std::vector<size_t> goff((size_t)count * nb * P);
+    for (int i = 0; i < count; ++i)
+      for (int b = 0; b < nb; ++b)
+        for (int k = 0; k < P; ++k) {
+          const size_t np = (size_t)(rq.hptr[b][k + 1] - rq.hptr[b][k]);
+          goff[((size_t)i * nb + b) * P + k] = gel;
+          gel += np * np;
+        }
+    double2* dg = static_cast<double2*>(ctx->sec_gam.get(std::max<size_t>(gel, 1) * sizeof(double2)));
+    const double2** dtab =
+        static_cast<const double2**>(ctx->sec_tab.get(std::max<size_t>((size_t)count * nb * P, 1) * sizeof(double2*)));
+    std::vector<const double2*> htab((size_t)count * nb * P);
+    for (int i = 0; i < count; ++i)
+      for (int b = 0; b < nb; ++b)
+        for (int k = 0; k < P; ++k) {
+          const size_t q = ((size_t)i * nb + b) * P + k;
+          const size_t np = (size_t)(rq.hptr[b][k + 1] - rq.hptr[b][k]);
+          htab[q] = dg + goff[q];
+          if (np) CK(cudaMemcpyAsync(dg + goff[q], gammas[q], np * np * sizeof(double2), cudaMemcpyHostToDevice, s));
+        }
+    if (!htab.empty())
+      CK(cudaMemcpyAsync(dtab, htab.data(), htab.size() * sizeof(double2*), cudaMemcpyHostToDevice, s));
+    for (int i = 0; i < count; ++i)
+      for (int b = 0; b < nb; ++b) rq.gam.push_back(dtab + ((size_t)i * nb + b) * P);
+    CK(cudaStreamSynchronize(s));
+    std::vector<JobSpec> specs;
+    for (int i = 0; i < count; ++i)
+      for (int b = 0; b < nb; ++b) specs.push_back({b, slots[i], configs[i], sys->plans[b].get(), sys, i});
+    std::vector<JobOut> jo;
+    ctx->sector = &rq;
+    try {
+      solve_jobs(ctx, sys, specs, (Mode)precision, jo);
+    } catch (...) {
+      ctx->sector = nullptr;
+      throw;
+    }
+    ctx->sector = nullptr;
+    for (int i = 0; i < count; ++i) {
+      double* ti = t + (size_t)i * P * P;
+      std::fill(ti, ti + (size_t)P * P, 0.0);
+      int32_t st = ST_OK;
+      for (int b = 0; b < nb; ++b) {
+        const JobOut& o = jo[(size_t)i * nb + b];
+        if (st == ST_OK) st = o.status;
+        for (size_t q = 0; q < o.tm.size() && q < (size_t)P * P; ++q) ti[q] += o.tm[q];
+      }
+      status[i] = st;
+    }
+    return CAROLI_OK;
+  } catch (const CudaError& e) {
+    ctx->sector = nullptr;
+    return fail_with(ctx, e.e == cudaErrorMemoryAllocation ? CAROLI_ENOMEM : CAROLI_ECUDA,
+                     std::string(e.what) + ": " + cudaGetErrorString(e.e));
+  }
+}
 
 int caroli_multi_scattering_states(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots,
                                    const int32_t* configs, const double* const* w, const int32_t* channels,

@@ -49,6 +49,7 @@ class AttachedLead:
     h01: np.ndarray
     orbitals: np.ndarray
     coupling: np.ndarray
+    cell: np.ndarray = None  # indices of these cell orbitals in the full lead cell (a block's part)
 
 
 def attach_leads(lead: Model, region: Region, interfaces) -> list:
@@ -158,7 +159,7 @@ class NestedMultiTerminal:
                     bl.append(None)
                     continue
                 bl.append(AttachedLead(l.h00[np.ix_(kc, kc)], l.h01[np.ix_(kc, kc)], l.orbitals[kd],
-                                       l.coupling[np.ix_(kd, kc)]))
+                                       l.coupling[np.ix_(kd, kc)], kc))
             if all(x is None for x in bl):
                 continue
             labels[mine[:n]] = len(blocks)
@@ -173,6 +174,9 @@ class NestedMultiTerminal:
                         interior=interior, labels=labels, blocks=blocks, axis=0)
         out = NestedMultiTerminal(system, block_leads, len(leads), device)
         out.sites = list(region.sites)
+        # For each lead, the index of every orbital of its cell within its site (nested_multi.rs:147-150).
+        out.orbital_kinds = [[o for i in range(len(itf.slice)) for o in range(itf.slice.site_orbitals(i))]
+                             for itf in interfaces]
         return out
 
     def lead_count(self):
@@ -185,7 +189,9 @@ class NestedMultiTerminal:
         return self.system.config_count()
 
     # -- self-energies (nested_multi.rs:188-224, multi.rs:43-55) ---------------------------------
-    def self_energies(self, energy) -> MultiSelfEnergies:
+    def surfaces(self, energy):
+        """Surface Green's functions g of every block's leads (None where a block has no part of
+        a lead), once per distinct lead cell (nested_multi.rs:201-224)."""
         z = complex(energy, 0.0)
         out = []
         for leads, solvers in zip(self.block_leads, self._solvers):
@@ -198,10 +204,56 @@ class NestedMultiTerminal:
                     rest = s.self_energies(energy)[1]
                     m = l.h00.shape[0]
                     done[id(s)] = np.linalg.inv(z * np.eye(m) - l.h00 - rest)
-                g = done[id(s)]
-                row.append(l.coupling @ g @ l.coupling.conj().T)
+                row.append(done[id(s)])
             out.append(row)
+        return out
+
+    def self_energies(self, energy) -> MultiSelfEnergies:
+        out = []
+        for leads, gs in zip(self.block_leads, self.surfaces(energy)):
+            out.append([None if l is None else l.coupling @ g @ l.coupling.conj().T for l, g in zip(leads, gs)])
         return MultiSelfEnergies(float(energy), out)
+
+    def sector_transmissions(self, energy, sectors, config=0, precision=Precision.DOUBLE):
+        """Transmissions between sectors of the leads (``sector_transmissions``,
+        nested_multi.rs:226-295): ``sectors[p]`` labels the orbitals of each site of lead p (e.g.
+        ``[0, 0, 1, 1]`` for the two spins of BHZ) or is None for the lead as a whole. Returns
+        ``(labels, t)``: ``labels`` the (lead, sector) of each row and column, ``t[k][l]`` from
+        label l into label k."""
+        if len(sectors) != self.nleads:
+            raise ValueError("one sector labelling per lead")
+
+        def label(p, cell_orbital):
+            return 0 if sectors[p] is None else sectors[p][self.orbital_kinds[p][cell_orbital]]
+
+        labels = []
+        for p, kinds in enumerate(self.orbital_kinds):
+            labels += [(p, a) for a in sorted({label(p, o) for o in range(len(kinds))})]
+        sigma = self.self_energies(energy)
+        surf = self.surfaces(energy)
+        gam = []
+        for leads, gs in zip(self.block_leads, surf):
+            row = [None] * len(labels)
+            for p, (l, g) in enumerate(zip(leads, gs)):
+                if l is None:
+                    continue
+                tags = np.array([label(p, o) for o in l.cell])
+                for m in (l.h00, l.h01):
+                    if np.any((tags[:, None] != tags[None, :]) & (m != 0)):
+                        raise ValueError(f"the Hamiltonian of lead {p} couples different sectors")
+                gamma = 1j * (g - g.conj().T)
+                for k, (lead, sec) in enumerate(labels):
+                    if lead != p:
+                        continue
+                    sel = tags == sec
+                    proj = np.where(sel[:, None] & sel[None, :], gamma, 0.0)
+                    row[k] = l.coupling @ proj @ l.coupling.conj().T
+            gam.append(row)
+        slot = self._slot(sigma)
+        t, st = self.plan().multi_sector(slot, config, int(precision), [lab[0] for lab in labels], gam)
+        if st != _native.OK:
+            raise GreenError("Singular", f"solve status {st} at E = {energy}")
+        return labels, t
 
     # -- GPU plumbing ---------------------------------------------------------------------------
     def plan(self):

@@ -23,6 +23,7 @@
  *   caroli_multi_sigma_upload                its self_energies                    nested_multi.rs:188-199
  *   caroli_multi_transmissions               transmissions_with_precision         nested_multi.rs:171-186
  *   caroli_multi_scattering_states           its scattering_states                nested_multi.rs:382-438
+ *   caroli_multi_sector_transmissions        its sector_transmissions             nested_multi.rs:226-295
  *   caroli_transmission_with_grad            no counterpart: the reference has no derivative code;
  *   caroli_derivs_upload                     the adjoint of transmission_with (dT/dV, dT/dJ)
  *   caroli_last_error                        GreenError / GpuError text           caroli-green/src/lib.rs:34-47
@@ -247,6 +248,16 @@ int caroli_scattering_states(caroli_ctx* ctx, int plan_id, int count, const int3
  *    instances (energy slot, configuration); CAROLI_DOUBLE or CAROLI_SINGLE, as the reference's
  *    Precision. The two-terminal entry points refuse a plan with leads. */
 int caroli_multi_leads(caroli_ctx* ctx, int plan_id, int nleads, const int64_t* lead_ptr, const int64_t* lead_orbitals);
+/* Transmissions between sectors of the leads (NestedMultiTerminal::sector_transmissions,
+ * nested_multi.rs:226-295): `nlabels` trace labels, label k on the orbitals of lead label_lead[k],
+ * with its own broadening: gammas[(i * nblocks + b) * nlabels + k] (np x np column-major
+ * complex128, in the order of that lead's orbitals in block b; NULL where the block has no part of
+ * the lead) is Γ of the lead projected on the sector, V P_a i(g - g^†) P_a V^†. The root is the
+ * one of the slot's self-energies (all leads whole). t[(i * nlabels + k) * nlabels + l] =
+ * Tr[Γ_k G Γ_l G^†] from label l into label k, summed over blocks. CAROLI_DOUBLE or CAROLI_SINGLE. */
+int caroli_multi_sector_transmissions(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots,
+                                      const int32_t* configs, int precision, int nlabels, const int32_t* label_lead,
+                                      const double* const* gammas, double* t, int32_t* status);
 /* Scattering states of a multi-terminal device (NestedMultiTerminal::scattering_states,
  * nested_multi.rs:382-438): ψ_p = G W_p for every lead p. For instance i, block b and lead p
  * (q = (i * nblocks + b) * nleads + p), w[q] is np x channels[q] column-major complex128 with

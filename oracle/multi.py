@@ -66,3 +66,32 @@ def spectral(system, leads, energy, config=0):
         gam[np.ix_(l.orbitals, l.orbitals)] = 1j * (s - s.conj().T)
         out.append(g @ gam @ g.conj().T)
     return out
+
+
+def sector_transmissions(system, leads, energy, labels, tags, config=0):
+    """t[k][l] = Tr[Γ_k G Γ_l G^†] between (lead, sector) labels (nested_multi.rs:226-295) on the
+    whole device: Γ_(p,a) = V_p P_a i(g_p - g_p^†) P_a V_p^† with P_a the projector on the cell
+    orbitals of lead p tagged a (`tags[p]`, one tag per cell orbital)."""
+    from caroli_gb300.leads import LeadSolver
+
+    a_mat = energy * np.eye(system.n) - dense_h(system, config)
+    gcell = []
+    for l in leads:
+        rest = LeadSolver(l.h00, l.h01).self_energies(energy)[1]
+        m = l.h00.shape[0]
+        g = np.linalg.inv(energy * np.eye(m) - l.h00 - rest)
+        a_mat[np.ix_(l.orbitals, l.orbitals)] -= l.coupling @ g @ l.coupling.conj().T
+        gcell.append(g)
+    gfull = np.linalg.inv(a_mat)
+    gam = []
+    for p, a in labels:
+        sel = np.asarray(tags[p]) == a
+        gc = 1j * (gcell[p] - gcell[p].conj().T)
+        proj = np.where(sel[:, None] & sel[None, :], gc, 0.0)
+        gam.append(leads[p].coupling @ proj @ leads[p].coupling.conj().T)
+    t = np.zeros((len(labels), len(labels)))
+    for k, (p, _) in enumerate(labels):
+        for l, (q, _) in enumerate(labels):
+            gpq = gfull[np.ix_(leads[p].orbitals, leads[q].orbitals)]
+            t[k, l] = float(np.real(np.trace(gam[k] @ gpq @ gam[l] @ gpq.conj().T)))
+    return t

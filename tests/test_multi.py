@@ -193,3 +193,47 @@ def test_gpu_multi_states_spectral_and_currents(model, seed, w, energy):
         for q in range(4):
             if q != p:
                 assert abs(_arm_current(cur, q) - t[q][p]) < 1e-9
+
+
+# -- sector transmissions --------------------------------------------------------------------------
+def _spin_labels(s):
+    tags = [[[0, 0, 1, 1][k] for k in kinds] for kinds in s.orbital_kinds]
+    labels = [(p, a) for p in range(4) for a in (0, 1)]
+    return labels, tags
+
+
+def test_sector_oracle_adds_up_to_leads():
+    """Summed over the sectors of both leads, the oracle's sector transmissions are its T_pq."""
+    from oracle import multi as om
+
+    s = cross_system(8, model="bhz", seed=3, anderson=0.5)
+    dev, clean, region, interfaces = cross_problem(8, model="bhz", seed=3, anderson=0.5)
+    leads = _full_leads(dev, clean, region, interfaces)
+    labels, tags = _spin_labels(s)
+    ts = om.sector_transmissions(s.system, leads, 0.05, labels, tags)
+    t = om.transmissions(s.system, leads, 0.05)
+    folded = ts.reshape(4, 2, 4, 2).sum(axis=(1, 3))
+    assert np.max(np.abs(folded - t)) < 1e-10
+
+
+@pytest.mark.gpu
+def test_gpu_spin_sector_transmissions():
+    """BHZ cross with spin-conserving disorder, sectors [0, 0, 1, 1] (spin up, spin down) on every
+    lead: against the dense oracle, no spin flips, and the sum over sectors equals T_pq."""
+    from oracle import multi as om
+
+    s = cross_system(W_ARM, model="bhz", seed=3, anderson=0.5)
+    dev, clean, region, interfaces = cross_problem(W_ARM, model="bhz", seed=3, anderson=0.5)
+    leads = _full_leads(dev, clean, region, interfaces)
+    for e in (-0.2, 0.05):
+        labels, t = s.sector_transmissions(e, [[0, 0, 1, 1]] * 4)
+        ref_labels, tags = _spin_labels(s)
+        assert labels == ref_labels
+        ref = om.sector_transmissions(s.system, leads, e, labels, tags)
+        assert np.max(np.abs(t - ref)) < 1e-9 * (1.0 + np.abs(ref).max())
+        spin = np.array([a for _, a in labels])
+        assert np.max(np.abs(t[spin[:, None] != spin[None, :]])) < 1e-10
+        folded = t.reshape(4, 2, 4, 2).sum(axis=(1, 3))
+        assert np.max(np.abs(folded - s.transmissions(e))) < 1e-9
+    with pytest.raises(ValueError):
+        s.sector_transmissions(0.05, [[0, 0, 1, 1]] * 3)
