@@ -47,6 +47,7 @@ SIGNATURES = {
     "caroli_solve_multi": (ctypes.c_int, [P, ctypes.c_int, P, P, P, ctypes.c_int, P, P, P]),
     "caroli_scattering_states": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P, P, P, P]),
     "caroli_multi_leads": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P]),
+    "caroli_transmission_matrix": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P, P]),
     "caroli_multi_scattering_states": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P]),
     "caroli_multi_sector_transmissions": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, ctypes.c_int,
                                                          ctypes.c_int, P, P, P, P]),
@@ -355,6 +356,32 @@ class Plan:
         out = np.zeros(nnz, np.complex128)
         self.ctx.check(self.ctx.lib.caroli_values_download(self.ctx.h, self.id, config, ptr(out)))
         return out
+
+    def transmission_matrices(self, slots, configs, w_left, nr):
+        """t = W_L^† G_LR W_R per (instance, block) (``caroli_transmission_matrix``); ``w_left[i][b]``
+        and ``nr[b]`` the right slice sizes. Returns ``(t, status)`` with ``t[i][b]`` cl x cr."""
+        slots = np.ascontiguousarray(slots, np.int32)
+        configs = np.ascontiguousarray(configs, np.int32)
+        cnt = len(slots)
+        mats = [np.asfortranarray(w, dtype=np.complex128) for inst in w_left for w in inst]
+        pw = np.array([m.ctypes.data if m.size else 0 for m in mats] or [0], dtype=np.uintp)
+        cl = np.array([m.shape[1] for m in mats] or [0], dtype=np.int32)
+        nb = self.nblocks
+        outs = [np.zeros((max(int(cl[q]), 1) * max(int(nr[q % nb]), 1),), np.complex128) for q in range(len(mats))]
+        po = np.array([o.ctypes.data for o in outs] or [0], dtype=np.uintp)
+        cr = np.zeros(max(len(mats), 1), np.int32)
+        st = np.zeros(max(cnt, 1), np.int32)
+        self.ctx.check(self.ctx.lib.caroli_transmission_matrix(self.ctx.h, self.id, cnt, ptr(slots), ptr(configs),
+                                                               ptr(pw), ptr(cl), ptr(po), ptr(cr), ptr(st)))
+        res = []
+        for i in range(cnt):
+            row = []
+            for b in range(nb):
+                q = i * nb + b
+                k, c = int(cl[q]), int(cr[q])
+                row.append(outs[q][:k * c].reshape((k, c), order="F"))
+            res.append(row)
+        return res, st[:cnt]
 
     def multi_leads(self, nleads, lead_ptr, lead_orbitals):
         """Leads of a multi-terminal plan (``caroli_multi_leads``)."""

@@ -244,6 +244,9 @@ struct StatesRequest {
   std::vector<std::vector<double2>>* psi = nullptr;
   // Multi-terminal sources: an explicit right-hand side per job (nblk x (cl + cr)) instead of W_L, W_R.
   std::vector<const double2*> rhs;
+  // Transmission matrices instead of ψ: t = W_L^† x_L with these W_L (nl x tcl, device) per job.
+  std::vector<const double2*> twl;
+  std::vector<int> tcl;
 };
 
 // One tree level of a batch: its fronts split by size class, and their algorithmic work.
@@ -301,6 +304,7 @@ struct caroli_ctx {
   Buf grhs, gptr, gdv, gdp;
   Buf states_w;  // lead factors W_L, W_R of a scattering-states call
   Buf states_rhs;  // multi-terminal sources
+  Buf tm_out, tm_tab, tm_cls;  // transmission matrices
   const SectorRequest* sector = nullptr;  // set during caroli_multi_sector_transmissions
   Buf sec_pos, sec_ptr, sec_gam, sec_tab;
   Buf mjobs, mscratch, mout;  // multi-terminal traces
@@ -631,13 +635,44 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
     CK(cudaMemcpyAsync(th.data(), rt_out, cj * sizeof(double), cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(eh.data(), rerr, cj * sizeof(double), cudaMemcpyDeviceToHost, s));
   }
-  if (states)
+  if (states && !states->twl.empty()) {
+    // t = W_L^† x_L per job into the ψ buffers (tcl x c each).
+    size_t to = 0;
+    std::vector<size_t> toffs(cj);
+    for (size_t j = 0; j < cj; ++j) {
+      toffs[j] = to;
+      to += (size_t)states->tcl[begin + j] * rdh[j].c;
+    }
+    double2* tdev = static_cast<double2*>(ctx->tm_out.get(std::max<size_t>(to, 1) * sizeof(double2)));
+    std::vector<const void*> tabs(3 * cj);
+    std::vector<int32_t> cls(cj);
+    for (size_t j = 0; j < cj; ++j) {
+      tabs[j] = states->twl[begin + j];
+      tabs[cj + j] = tdev + toffs[j];
+      cls[j] = states->tcl[begin + j];
+    }
+    void** dtabs = static_cast<void**>(ctx->tm_tab.get(3 * cj * sizeof(void*)));
+    int32_t* dcls = static_cast<int32_t*>(ctx->tm_cls.get(cj * sizeof(int32_t)));
+    CK(cudaMemcpyAsync(dtabs, tabs.data(), 2 * cj * sizeof(void*), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dcls, cls.data(), cj * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    launch(K_REF_CHECK, 0.0, 0.0, [&] {
+      tmatrix_kernel<<<(unsigned)cj, 256, 0, s>>>(drd, reinterpret_cast<const double2* const*>(dtabs), dcls,
+                                                   reinterpret_cast<double2* const*>(dtabs + cj));
+    });
+    for (size_t j = 0; j < cj; ++j) {
+      std::vector<double2>& t = (*states->psi)[begin + j];
+      t.resize((size_t)states->tcl[begin + j] * rdh[j].c);
+      if (!t.empty())
+        CK(cudaMemcpyAsync(t.data(), tdev + toffs[j], t.size() * sizeof(double2), cudaMemcpyDeviceToHost, s));
+    }
+  } else if (states) {
     for (size_t j = 0; j < cj; ++j) {
       std::vector<double2>& psi = (*states->psi)[begin + j];
       psi.resize((size_t)rdh[j].nblk * rdh[j].c);
       if (!psi.empty())
         CK(cudaMemcpyAsync(psi.data(), rx + xoffs[j], psi.size() * sizeof(double2), cudaMemcpyDeviceToHost, s));
     }
+  }
   std::vector<RefineDesc> fin(cj);
   CK(cudaMemcpyAsync(fin.data(), drd, cj * sizeof(RefineDesc), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
@@ -2161,6 +2196,86 @@ SigmaSlot& slot_buffers(System* sys, int slot) {
 }  // namespace
 
 extern "C" {
+
+int caroli_transmission_matrix(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots, const int32_t* configs,
+                               const double* const* w_left, const int32_t* left_channels, double* const* t,
+                               int32_t* right_channels, int32_t* status) {
+  System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
+  if (!sys || count < 0 ||
+      (count > 0 && (!slots || !configs || !w_left || !left_channels || !t || !right_channels || !status)))
+    return fail_with(ctx, CAROLI_EINVAL, "caroli_transmission_matrix: bad arguments");
+  if (sys->nleads > 0) return fail_with(ctx, CAROLI_EINVAL, "caroli_transmission_matrix: a multi-terminal plan");
+  if (!sys->vals) return fail_with(ctx, CAROLI_EINVAL, "no H values uploaded");
+  const int nb = (int)sys->plans.size();
+  for (int i = 0; i < count; ++i) {
+    if (slots[i] < 0 || slots[i] >= (int)sys->slots.size() || !sys->slots[slots[i]].set)
+      return fail_with(ctx, CAROLI_EINVAL, "energy slot without self-energies");
+    if (configs[i] < 0 || configs[i] >= sys->nconfigs) return fail_with(ctx, CAROLI_EINVAL, "configuration out of range");
+    for (int b = 0; b < nb; ++b) {
+      const size_t q = (size_t)i * nb + b;
+      if (left_channels[q] < 0 || left_channels[q] > sys->plans[b]->host.nl || (left_channels[q] && !w_left[q]) ||
+          !t[q])
+        return fail_with(ctx, CAROLI_EINVAL, "caroli_transmission_matrix: bad lead factor or output");
+    }
+  }
+  try {
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    ctx->last_ms = 0.0;
+    ctx->last_launches = 0;
+    ctx->factor_ms = ctx->root_ms = ctx->tail_ms = 0.0;
+    ctx->refine_iters = 0;
+    ctx->fallbacks = 0;
+    ctx->refine_job_steps = ctx->refine_batch_steps = 0;
+    std::vector<JobSpec> specs;
+    StatesRequest rq;
+    size_t welems = 0;
+    std::vector<size_t> woff;
+    for (int i = 0; i < count; ++i)
+      for (int b = 0; b < nb; ++b) {
+        const size_t q = (size_t)i * nb + b;
+        const SigmaSlot& sg = sys->slots[slots[i]];
+        specs.push_back({b, slots[i], configs[i], sys->plans[b].get(), sys, i});
+        rq.wl.push_back(nullptr);
+        rq.wr.push_back(sg.wr[b]);
+        rq.cl.push_back(0);
+        rq.cr.push_back(sg.channels[b]);
+        rq.tcl.push_back(left_channels[q]);
+        woff.push_back(welems);
+        welems += (size_t)sys->plans[b]->host.nl * left_channels[q];
+      }
+    double2* wd = static_cast<double2*>(ctx->states_w.get(std::max<size_t>(welems, 1) * sizeof(double2)));
+    for (size_t q = 0; q < specs.size(); ++q) {
+      const size_t nl = (size_t)specs[q].plan->host.nl * rq.tcl[q];
+      if (nl) CK(cudaMemcpyAsync(wd + woff[q], w_left[q], nl * sizeof(double2), cudaMemcpyHostToDevice, s));
+      rq.twl.push_back(wd + woff[q]);
+    }
+    CK(cudaStreamSynchronize(s));
+    std::vector<std::vector<double2>> tm(specs.size());
+    rq.psi = &tm;
+    std::vector<JobOut> jo;
+    run_jobs<float, float>(ctx, sys, specs, MODE_MIXED, jo, nullptr, &rq);
+    for (int i = 0; i < count; ++i) {
+      int32_t st = ST_OK;
+      for (int b = 0; b < nb; ++b) {
+        const size_t q = (size_t)i * nb + b;
+        if (st == ST_OK) st = jo[q].status;
+        right_channels[q] = rq.cr[q];
+        const size_t cnt = (size_t)rq.tcl[q] * rq.cr[q];
+        for (size_t e = 0; e < cnt && e < tm[q].size(); ++e) {
+          t[q][2 * e] = tm[q][e].x;
+          t[q][2 * e + 1] = tm[q][e].y;
+          if (st == ST_OK && !(std::isfinite(tm[q][e].x) && std::isfinite(tm[q][e].y))) st = ST_NONFINITE;
+        }
+      }
+      status[i] = st;
+    }
+    return CAROLI_OK;
+  } catch (const CudaError& e) {
+    return fail_with(ctx, e.e == cudaErrorMemoryAllocation ? CAROLI_ENOMEM : CAROLI_ECUDA,
+                     std::string(e.what) + ": " + cudaGetErrorString(e.e));
+  }
+}
 
 int caroli_multi_sector_transmissions(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots,
                                       const int32_t* configs, int precision, int nlabels, const int32_t* label_lead,

@@ -477,6 +477,27 @@ __global__ void gm_residual_kernel(RefineDesc* __restrict__ rd, int njobs) {
 
 namespace caroli {
 
+// Transmission matrix t = W_L^† x_L of each job after its refinement (x = G W_R): t is
+// cl x c column-major, W_L nl x cl. grid (jobs), threads over the entries of t.
+__global__ void tmatrix_kernel(const RefineDesc* __restrict__ rd, const double2* const* __restrict__ wl,
+                               const int32_t* __restrict__ cls, double2* const* __restrict__ tout) {
+  const RefineDesc& R = rd[blockIdx.x];
+  const int cl = cls[blockIdx.x];
+  const double2* W = wl[blockIdx.x];
+  double2* T = tout[blockIdx.x];
+  for (int idx = threadIdx.x; idx < cl * R.c; idx += blockDim.x) {
+    const int a = idx % cl, c = idx / cl;
+    double2 acc = make_double2(0.0, 0.0);
+    for (int i = 0; i < R.nl; ++i) {
+      const double2 w = W[i + (int64_t)a * R.nl];
+      const double2 x = R.x[R.left_local[i] + (int64_t)c * R.nblk];
+      acc.x += w.x * x.x + w.y * x.y;  // conj(w) x
+      acc.y += w.x * x.y - w.y * x.x;
+    }
+    T[idx] = acc;
+  }
+}
+
 // Multi-terminal sources: W_p (np x c, column-major) on the block-local rows of lead p's orbitals,
 // rows[a] = left_local[pos[a]], into columns c0 .. c0 + c of B (nblk rows). grid: np x c elements.
 __global__ void scatter_sources_kernel(double2* __restrict__ B, int nblk, int c0, const int32_t* __restrict__ left_local,

@@ -358,6 +358,36 @@ class NestedTwoTerminal:
         """``Σ_p f_p ψ_p† O ψ_p / 2π`` of every site (nested.rs:916-918)."""
         return _states.site_densities(self.system, states, f, op)
 
+    # -- transmission eigenvalues (nested.rs:753-780) --------------------------------------
+    def transmission_eigenvalues_batch(self, sigmas, configs=None):
+        """Transmission eigenvalues of each ``(sigma, config)`` pair, decreasing: the squared
+        singular values of t = W_L^† G_LR W_R of every block (t from the GPU, the small SVD here);
+        a failed point is a ``GreenError``."""
+        if configs is None:
+            configs = [0] * len(sigmas)
+        slots = [self._slot(s) for s in sigmas]
+        nr = [len(b.right) for b in self.system.blocks]
+        ts, st = self.plan().transmission_matrices(slots, configs, [s.w_left() for s in sigmas], nr)
+        out = []
+        for tb, code, s in zip(ts, st, sigmas):
+            if code != _native.OK:
+                out.append(GreenError("Singular", f"solve status {code} at E = {s.energy}"))
+                continue
+            taus = np.concatenate([np.linalg.svd(t, compute_uv=False) ** 2 if t.size else np.zeros(0) for t in tb])
+            out.append(np.sort(taus)[::-1])
+        return out
+
+    def transmission_eigenvalues(self, energy, config=0):
+        out = self.transmission_eigenvalues_batch([self.self_energies(energy)], [config])[0]
+        if isinstance(out, GreenError):
+            raise out
+        return out
+
+    def fano_factor(self, energy, config=0):
+        """F = Σ τ (1 - τ) / Σ τ (nested.rs:773-780)."""
+        taus = self.transmission_eigenvalues(energy, config)
+        return float(np.sum(taus * (1.0 - taus)) / np.sum(taus))
+
     def transmissions_checked(self, energies, options: PrecisionOptions, config=0):
         sigmas = {float(e): self.self_energies(e) for e in energies}
 

@@ -24,6 +24,7 @@
  *   caroli_multi_transmissions               transmissions_with_precision         nested_multi.rs:171-186
  *   caroli_multi_scattering_states           its scattering_states                nested_multi.rs:382-438
  *   caroli_multi_sector_transmissions        its sector_transmissions             nested_multi.rs:226-295
+ *   caroli_transmission_matrix               transmission_eigenvalues / fano_factor nested.rs:753-780
  *   caroli_transmission_with_grad            no counterpart: the reference has no derivative code;
  *   caroli_derivs_upload                     the adjoint of transmission_with (dT/dV, dT/dJ)
  *   caroli_last_error                        GreenError / GpuError text           caroli-green/src/lib.rs:34-47
@@ -271,6 +272,17 @@ int caroli_multi_scattering_states(caroli_ctx* ctx, int plan_id, int count, cons
 int caroli_multi_sigma_upload(caroli_ctx* ctx, int plan_id, int slot, double energy, const double* const* sigma);
 int caroli_multi_transmissions(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots, const int32_t* configs,
                                int precision, double* t, int32_t* status);
+
+/* Transmission matrices t = W_L^† G_LR W_R of every block (transmission_eigenvalues and
+ * fano_factor, nested.rs:753-780, take the squared singular values of t). For instance i and block
+ * b (q = i * nblocks + b): w_left[q] is nl_b x left_channels[q] column-major complex128 with
+ * W_L W_L^† = Γ_L; W_R is the slot's (caroli_sigma_upload). t[q] receives left_channels[q] x
+ * right_channels[q] column-major complex128 (room for nr_b columns), right_channels[q] the slot's
+ * channel count. Runs the mixed path: X = G W_R refined in FP64 (as the transmission), then
+ * t = W_L^† X_L on the device. */
+int caroli_transmission_matrix(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots, const int32_t* configs,
+                               const double* const* w_left, const int32_t* left_channels, double* const* t,
+                               int32_t* right_channels, int32_t* status);
 
 /* caroli_solve_batch over instances of several systems (plans) at once: instance i is
  * (plan_ids[i], slots[i], configs[i]), slots and configurations of that plan. Systems of different

@@ -200,3 +200,38 @@ def test_gpu_states_invalid_arguments():
         plan.scattering_states([slot], [0], [wl], [sigma.w_right()], sys_.system.n)
     with pytest.raises(_native.NativeError):
         plan.scattering_states([slot], [5], [sigma.w_left()], [sigma.w_right()], sys_.system.n)
+
+
+# -- transmission eigenvalues (nested.rs:753-780; the reference's test tests/nested.rs:131-156) ----
+@pytest.mark.gpu
+def test_gpu_transmission_eigenvalues_and_shot_noise():
+    m = square()
+    region = Region.cuboid(m.lattice, [12, 7, 0])
+    dirty = NestedTwoTerminal.from_model(m.with_onsite_term(_hash_disorder(2.0, 1)), m, region, 0)
+    clean = NestedTwoTerminal.from_model(m, m, region, 0)
+    barrier = m.with_onsite_term(lambda s: np.eye(1) * 40.0 if s.cell[0] == 6 else None)
+    tunnel = NestedTwoTerminal.from_model(barrier, m, region, 0)
+    for e in (-2.3, -0.7, 0.9):
+        taus = dirty.transmission_eigenvalues(e)
+        t = dirty.transmission(e)
+        assert abs(taus.sum() - t) < 1e-10
+        assert np.all((taus >= -1e-10) & (taus <= 1.0 + 1e-10))
+        perfect = clean.transmission_eigenvalues(e)
+        assert np.all(np.abs(perfect - 1.0) < 1e-9) and abs(clean.fano_factor(e)) < 1e-8
+        assert tunnel.fano_factor(e) > 0.99
+    # Against the oracle's G_LR on a BHZ ribbon (two blocks): the same eigenvalues.
+    from oracle import states as ost
+
+    b = bhz()
+    sys_ = NestedTwoTerminal.from_model(b.with_onsite_term(_hash_disorder(0.6, 4)), b,
+                                        Region.cuboid(b.lattice, [8, 6, 0]), 0)
+    sigma = sys_.self_energies(0.03)
+    taus = sys_.transmission_eigenvalues(0.03)
+    psi = ost.scattering_states(sys_.system, 0.03, sigma.blocks, sigma.w_left(), sigma.w_right())[1]
+    ref = []
+    c0 = 0
+    for blk, wl, wr in zip(sys_.system.blocks, sigma.w_left(), sigma.w_right()):
+        tm = wl.conj().T @ psi[blk.left, c0:c0 + wr.shape[1]]
+        ref.extend(np.linalg.svd(tm, compute_uv=False) ** 2)
+        c0 += wr.shape[1]
+    assert np.max(np.abs(taus - np.sort(ref)[::-1])) < 1e-10
