@@ -48,6 +48,7 @@ SIGNATURES = {
     "caroli_scattering_states": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P, P, P, P]),
     "caroli_multi_leads": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P]),
     "caroli_transmission_matrix": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P, P]),
+    "caroli_root_green": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P, P]),
     "caroli_multi_scattering_states": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P]),
     "caroli_multi_sector_transmissions": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, ctypes.c_int,
                                                          ctypes.c_int, P, P, P, P]),
@@ -356,6 +357,24 @@ class Plan:
         out = np.zeros(nnz, np.complex128)
         self.ctx.check(self.ctx.lib.caroli_values_download(self.ctx.h, self.id, config, ptr(out)))
         return out
+
+    def root_green(self, slots, configs, kept_sizes):
+        """The FP64 root Green's function on the kept orbitals of every (instance, block)
+        (``caroli_root_green``): ``(g, status)`` with ``g[i][b]`` kept x kept."""
+        slots = np.ascontiguousarray(slots, np.int32)
+        configs = np.ascontiguousarray(configs, np.int32)
+        cnt, nb = len(slots), self.nblocks
+        outs = [np.zeros((max(kept_sizes[b], 1), max(kept_sizes[b], 1)), np.complex128, order="F")
+                for _ in range(cnt) for b in range(nb)]
+        po = np.array([o.ctypes.data for o in outs] or [0], dtype=np.uintp)
+        kept = np.zeros(max(cnt * nb, 1), np.int32)
+        st = np.zeros(max(cnt, 1), np.int32)
+        self.ctx.check(self.ctx.lib.caroli_root_green(self.ctx.h, self.id, cnt, ptr(slots), ptr(configs), ptr(po),
+                                                      ptr(kept), ptr(st)))
+        res = []
+        for i in range(cnt):
+            res.append([outs[i * nb + b][:kept[i * nb + b], :kept[i * nb + b]] for b in range(nb)])
+        return res, st[:cnt]
 
     def transmission_matrices(self, slots, configs, w_left, nr):
         """t = W_L^† G_LR W_R per (instance, block) (``caroli_transmission_matrix``); ``w_left[i][b]``

@@ -306,6 +306,10 @@ struct caroli_ctx {
   Buf states_rhs;  // multi-terminal sources
   Buf tm_out, tm_tab, tm_cls;  // transmission matrices
   const SectorRequest* sector = nullptr;  // set during caroli_multi_sector_transmissions
+  // Set during caroli_root_green: the FP64 root Green's function on the kept orbitals of each
+  // (instance, block) job, copied out after the root inverse.
+  std::vector<std::vector<double2>>* green_out = nullptr;
+  int green_blocks = 0;
   Buf sec_pos, sec_ptr, sec_gam, sec_tab;
   Buf mjobs, mscratch, mout;  // multi-terminal traces
   Buf dent, dspin, dscal, dcoef, dflag, dtab, dclean;  // on-device disorder
@@ -1176,6 +1180,21 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
       launch(K_TRACE, 0.0, 0.0, [&] {
         trace_finish_kernel<<<(unsigned)((cj + 127) / 128), 128, 0, s>>>(part, (int)parts_per_job, (int)cj, tdev, status);
       });
+      if constexpr (std::is_same<TR, double>::value) {
+        if (ctx->green_out)
+          for (size_t j = 0; j < cj; ++j) {
+            const JobSpec& sp = specs[begin + j];
+            if (sp.inst < 0) continue;
+            const FrontPlan& P = sp.plan->host;
+            const int m = P.fronts[P.root].n, nd = P.nd, k = m - nd;
+            std::vector<double2>& g = (*ctx->green_out)[(size_t)sp.inst * ctx->green_blocks + sp.block];
+            g.resize((size_t)k * k);
+            if (k)
+              CK(cudaMemcpy2DAsync(g.data(), (size_t)k * sizeof(double2), rarena + root_off[j] + nd + (size_t)nd * m,
+                                   (size_t)m * sizeof(double2), (size_t)k * sizeof(double2), (size_t)k,
+                                   cudaMemcpyDeviceToHost, s));
+          }
+      }
       // Multi-terminal blocks: every T_pq from the root inverse.
       std::vector<MultiJob> mj;
       std::vector<size_t> midx;
@@ -2196,6 +2215,65 @@ SigmaSlot& slot_buffers(System* sys, int slot) {
 }  // namespace
 
 extern "C" {
+
+int caroli_root_green(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots, const int32_t* configs,
+                      double* const* g, int32_t* kept, int32_t* status) {
+  System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
+  if (!sys || count < 0 || (count > 0 && (!slots || !configs || !g || !kept || !status)))
+    return fail_with(ctx, CAROLI_EINVAL, "caroli_root_green: bad arguments");
+  if (!sys->vals) return fail_with(ctx, CAROLI_EINVAL, "no H values uploaded");
+  const int nb = (int)sys->plans.size();
+  for (int i = 0; i < count; ++i) {
+    if (slots[i] < 0 || slots[i] >= (int)sys->slots.size() || !sys->slots[slots[i]].set)
+      return fail_with(ctx, CAROLI_EINVAL, "energy slot without self-energies");
+    if (configs[i] < 0 || configs[i] >= sys->nconfigs) return fail_with(ctx, CAROLI_EINVAL, "configuration out of range");
+    for (int b = 0; b < nb; ++b)
+      if (!g[(size_t)i * nb + b]) return fail_with(ctx, CAROLI_EINVAL, "caroli_root_green: missing output");
+  }
+  try {
+    CK(cudaSetDevice(ctx->device));
+    ctx->last_ms = 0.0;
+    ctx->last_launches = 0;
+    ctx->factor_ms = ctx->root_ms = ctx->tail_ms = 0.0;
+    ctx->fallbacks = 0;
+    ctx->refine_iters = 0;
+    ctx->refine_job_steps = ctx->refine_batch_steps = 0;
+    std::vector<JobSpec> specs;
+    for (int i = 0; i < count; ++i)
+      for (int b = 0; b < nb; ++b) specs.push_back({b, slots[i], configs[i], sys->plans[b].get(), sys, i});
+    std::vector<std::vector<double2>> out((size_t)count * nb);
+    std::vector<JobOut> jo;
+    ctx->green_out = &out;
+    ctx->green_blocks = nb;
+    try {
+      solve_jobs(ctx, sys, specs, MODE_DOUBLE, jo);
+    } catch (...) {
+      ctx->green_out = nullptr;
+      throw;
+    }
+    ctx->green_out = nullptr;
+    for (int i = 0; i < count; ++i) {
+      int32_t st = ST_OK;
+      for (int b = 0; b < nb; ++b) {
+        const size_t q = (size_t)i * nb + b;
+        if (st == ST_OK) st = jo[q].status;
+        const FrontPlan& P = sys->plans[b]->host;
+        const int k = P.nl + (P.rpos == 0 && P.nr ? 0 : P.nr);
+        kept[q] = k;
+        for (size_t e = 0; e < out[q].size() && e < (size_t)k * k; ++e) {
+          g[q][2 * e] = out[q][e].x;
+          g[q][2 * e + 1] = out[q][e].y;
+        }
+      }
+      status[i] = st;
+    }
+    return CAROLI_OK;
+  } catch (const CudaError& e) {
+    ctx->green_out = nullptr;
+    return fail_with(ctx, e.e == cudaErrorMemoryAllocation ? CAROLI_ENOMEM : CAROLI_ECUDA,
+                     std::string(e.what) + ": " + cudaGetErrorString(e.e));
+  }
+}
 
 int caroli_transmission_matrix(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots, const int32_t* configs,
                                const double* const* w_left, const int32_t* left_channels, double* const* t,

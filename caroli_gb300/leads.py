@@ -105,6 +105,32 @@ class LeadSolver:
                 last = err
         raise last
 
+    def modes(self, energy):
+        """Propagating modes at ``energy`` (shifted off band edges as ``self_energies``), each
+        carrying unit current (``LeadModes``, modes.rs:52-76), for a lead whose cells go away from
+        the device with ``h01``: ``(right_modes, right_lambdas, left_modes, left_lambdas, Σ_rest,
+        energy used)``; right = outgoing (away from the device), left = incoming, Σ_rest = h01 F the
+        self-energy of the cells beyond the first."""
+        last = GreenError("Eigen")
+        for shift in SHIFTS:
+            e = energy + shift * self.scale
+            try:
+                if self.cell is not None:
+                    sig = self._definite(e)
+                    s, c, theta, y = self.cell
+                    lam_l, lam_r = self._definite_roots(e)
+                    prop = np.nonzero(lam_r.imag != 0.0)[0]
+                    flux = y[:, prop] / np.sqrt(c) / np.sqrt(2.0 * np.abs(lam_r.imag[prop]))[None, :]
+                    return flux, lam_r[prop], flux.copy(), lam_l[prop], sig[1], e
+                sig = self._general(e)
+                (rm, rl), (lm, ll) = self._last_modes
+                return rm, rl, lm, ll, sig[1], e
+            except GreenError as err:
+                last = err
+            except (np.linalg.LinAlgError, ValueError) as err:
+                last = GreenError("Eigen", str(err))
+        raise last
+
     # -- h01 = s c 1: one Hermitian problem ------------------------------------------------------
     def _definite(self, e):
         s, c, theta, y = self.cell
@@ -155,6 +181,7 @@ class LeadSolver:
         vr = vr / np.linalg.norm(vr, axis=0)
 
         right_vecs, left_vecs = [], []
+        right_modes, left_modes = [], []  # (unit-current φ, λ) of the propagating modes
         pidx = np.nonzero(prop)[0]
         # Degenerate propagating groups by single linkage.
         groups = []
@@ -186,6 +213,13 @@ class LeadSolver:
                 if not np.isfinite(vk) or abs(vk) < VELOCITY_TOL * self.scale:
                     raise GreenError("Singular", f"subband edge near E = {e}")
                 (right_vecs if vk > 0 else left_vecs).append(newv[:, k])
+                (right_modes if vk > 0 else left_modes).append((ph / np.sqrt(abs(vel[k])), lg.mean()))
+        def stack(ms):
+            if not ms:
+                return np.zeros((n, 0), np.complex128), np.zeros(0, np.complex128)
+            return np.array([m[0] for m in ms]).T, np.array([m[1] for m in ms])
+
+        self._last_modes = (stack(right_modes), stack(left_modes))
         nr = int(right_ev.sum()) + len(right_vecs)
         nl = int(left_ev.sum()) + len(left_vecs)
         if nr != n or nl != n:

@@ -308,6 +308,35 @@ class NestedMultiTerminal:
         return [t[i] if st[i] == _native.OK else GreenError("Singular", f"solve status {st[i]} at E = {e}")
                 for i, e in enumerate(energies)]
 
+    # -- scattering matrix (nested_multi.rs:440-495) --------------------------------------------
+    def smatrix(self, energy, config=0):
+        """Scattering matrix in the basis of the propagating lead modes, from the FP64 root Green's
+        function on the GPU (``caroli_root_green``)."""
+        from .smatrix import ScatteringLead, assemble, scattering_blocks
+
+        sigma = self.self_energies(energy)
+        slot = self._slot(sigma)
+        kept = [len(b.left) for b in self.system.blocks]
+        greens, st = self.plan().root_green([slot], [config], kept)
+        if st[0] != _native.OK:
+            raise GreenError("Singular", f"solve status {st[0]} at E = {energy}")
+        parts = []
+        for blk, leads, solvers, g in zip(self.system.blocks, self.block_leads, self._solvers, greens[0]):
+            kept_orbs = np.asarray(blk.left)
+            done, sl, h00s = {}, [], []
+            for l, s in zip(leads, solvers):
+                if l is None:
+                    sl.append(None)
+                    h00s.append(None)
+                    continue
+                if id(s) not in done:
+                    done[id(s)] = s.modes(energy)
+                sl.append(ScatteringLead(np.searchsorted(kept_orbs, l.orbitals), l.coupling, l.h01, done[id(s)],
+                                         energy))
+                h00s.append(l.h00)
+            parts.append(scattering_blocks(g, sl, h00s, energy))
+        return assemble(energy, parts)
+
     # -- scattering states (nested_multi.rs:382-438) and what is built from them --------------
     def scattering_states_batch(self, energies, configs=None):
         """``ScatteringStates`` (one ψ_p per lead) of each (energy, configuration) pair in one GPU

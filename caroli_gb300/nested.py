@@ -358,6 +358,34 @@ class NestedTwoTerminal:
         """``Σ_p f_p ψ_p† O ψ_p / 2π`` of every site (nested.rs:916-918)."""
         return _states.site_densities(self.system, states, f, op)
 
+    # -- scattering matrix (nested.rs:717-752) -------------------------------------------------
+    def smatrix(self, energy, config=0):
+        """Scattering matrix in the basis of the propagating lead modes (left lead 0, right lead
+        1), from the FP64 root Green's function on the GPU (``caroli_root_green``)."""
+        from .leads import LeadSolver
+        from .smatrix import ScatteringLead, assemble, scattering_blocks
+
+        sigma = self.self_energies(energy)
+        slot = self._slot(sigma)
+        kept = []
+        for blk in self.system.blocks:
+            same = np.array_equal(blk.left, blk.right)
+            kept.append(len(blk.left) + (0 if same else len(blk.right)))
+        greens, st = self.plan().root_green([slot], [config], kept)
+        if st[0] != _native.OK:
+            raise GreenError("Singular", f"solve status {st[0]} at E = {energy}")
+        parts = []
+        for blk, g in zip(self.system.blocks, greens[0]):
+            nl, nr = len(blk.left), len(blk.right)
+            rpos = 0 if np.array_equal(blk.left, blk.right) else nl
+            left_out = blk.left_h01.conj().T  # cells going away from the device: -axis
+            lm = LeadSolver(blk.left_h00, left_out).modes(energy)
+            rm = LeadSolver(blk.right_h00, blk.right_h01).modes(energy)
+            leads = [ScatteringLead(np.arange(nl), left_out, left_out, lm, energy),
+                     ScatteringLead(np.arange(rpos, rpos + nr), blk.right_h01, blk.right_h01, rm, energy)]
+            parts.append(scattering_blocks(g, leads, [blk.left_h00, blk.right_h00], energy))
+        return assemble(energy, parts)
+
     # -- transmission eigenvalues (nested.rs:753-780) --------------------------------------
     def transmission_eigenvalues_batch(self, sigmas, configs=None):
         """Transmission eigenvalues of each ``(sigma, config)`` pair, decreasing: the squared

@@ -25,6 +25,7 @@
  *   caroli_multi_scattering_states           its scattering_states                nested_multi.rs:382-438
  *   caroli_multi_sector_transmissions        its sector_transmissions             nested_multi.rs:226-295
  *   caroli_transmission_matrix               transmission_eigenvalues / fano_factor nested.rs:753-780
+ *   caroli_root_green                        lead_green / the root of smatrix     nested.rs:717-802
  *   caroli_transmission_with_grad            no counterpart: the reference has no derivative code;
  *   caroli_derivs_upload                     the adjoint of transmission_with (dT/dV, dT/dJ)
  *   caroli_last_error                        GreenError / GpuError text           caroli-green/src/lib.rs:34-47
@@ -272,6 +273,15 @@ int caroli_multi_scattering_states(caroli_ctx* ctx, int plan_id, int count, cons
 int caroli_multi_sigma_upload(caroli_ctx* ctx, int plan_id, int slot, double energy, const double* const* sigma);
 int caroli_multi_transmissions(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots, const int32_t* configs,
                                int precision, double* t, int32_t* status);
+
+/* The FP64 Green's function on the kept orbitals of every block's root (lead_green, nested.rs:783-802;
+ * the root of NestedMultiTerminal::smatrix, nested_multi.rs:440-495): for instance i and block b
+ * (q = i * nblocks + b), g[q] receives the kept x kept block of (z - H - Σ)^-1, column-major
+ * complex128, kept[q] = its size. The kept orbitals are the left slice then the right one (or the
+ * single list of a multi-terminal block), in the plan's order. The scattering matrix is formed
+ * from it on the host. */
+int caroli_root_green(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots, const int32_t* configs,
+                      double* const* g, int32_t* kept, int32_t* status);
 
 /* Transmission matrices t = W_L^† G_LR W_R of every block (transmission_eigenvalues and
  * fano_factor, nested.rs:753-780, take the squared singular values of t). For instance i and block
