@@ -48,6 +48,7 @@ SIGNATURES = {
     "caroli_scattering_states": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P, P, P, P]),
     "caroli_multi_leads": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P]),
     "caroli_transmission_matrix": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P, P]),
+    "caroli_last_job_steps": (ctypes.c_int, [P, ctypes.c_int64, P, P]),
     "caroli_root_green": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P, P]),
     "caroli_multi_scattering_states": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P]),
     "caroli_multi_sector_transmissions": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, ctypes.c_int,
@@ -464,6 +465,14 @@ class Plan:
         self.ctx.check(self.ctx.lib.caroli_multi_transmissions(self.ctx.h, self.id, cnt, ptr(slots), ptr(configs),
                                                                precision, ptr(t), ptr(st)))
         return t[:cnt], st[:cnt]
+
+    def last_job_steps(self):
+        """GMRES steps of each block solve of the last batch (``caroli_last_job_steps``)."""
+        cnt = ctypes.c_int64()
+        self.ctx.check(self.ctx.lib.caroli_last_job_steps(self.ctx.h, 0, None, ctypes.byref(cnt)))
+        out = np.zeros(max(cnt.value, 1), np.int32)
+        self.ctx.check(self.ctx.lib.caroli_last_job_steps(self.ctx.h, cnt.value, ptr(out), ctypes.byref(cnt)))
+        return out[:cnt.value]
 
     def last_job_info(self):
         cnt = ctypes.c_int64()

@@ -324,7 +324,8 @@ struct caroli_ctx {
   int64_t refine_iters = 0;
   int64_t refine_job_steps = 0;    // Arnoldi steps summed over the solves
   int64_t refine_batch_steps = 0;  // Arnoldi steps launched for the batch (the slowest solve's)
-  std::vector<int32_t> job_iters, job_perturbed, job_status;
+  std::vector<int32_t> job_iters, job_perturbed, job_status, job_steps;
+  std::vector<int32_t> steps_tmp;  // Arnoldi steps of each job of the last refinement
   size_t mem_budget = 0;
 };
 
@@ -682,6 +683,8 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
   CK(cudaStreamSynchronize(s));
   for (size_t j = 0; j < cj; ++j) {
     ih[j] = std::max(ih[j], fin[j].iters);
+    if (j == 0) ctx->steps_tmp.assign(cj, 0);
+    ctx->steps_tmp[j] = fin[j].steps;
     ctx->refine_job_steps += fin[j].steps;
     if (rdh[j].c == 0 || states) {
       if (!adjoint) { th[j] = 0.0; eh[j] = 0.0; }
@@ -698,6 +701,7 @@ struct JobOut {
   double t = 0.0, err = 0.0;
   int32_t status = ST_OK;
   int32_t iters = 0;
+  int32_t steps = 0;  // Arnoldi steps of the mixed refinement
   int32_t perturbed = 0;
   std::vector<double> dv, dp;  // gradient: dT/dV of the block's orbitals (block order), dT/dp
   std::vector<double> tm;      // multi-terminal: T[p * P + q] of the block
@@ -1273,6 +1277,7 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
         }
         RefineDesc* fwd = refine(ctx, sys, specs, begin, cj, lr, max_root, dtasks, jd, arena, arena_off, rarena,
                                  root_off, launch, th, eh, sh, ih, ctx->rb[0], 0, {}, states);
+        for (size_t j = 0; j < cj && j < ctx->steps_tmp.size(); ++j) out[begin + j].steps = ctx->steps_tmp[j];
         if (grad) gradient(ctx, sys, specs, begin, cj, lr, max_root, dtasks, jd, arena, arena_off, rarena, root_off,
                            launch, th, eh, sh, ih, fwd, *grad, out);
       }
@@ -2702,37 +2707,37 @@ int caroli_sigma_upload(caroli_ctx* ctx, int plan_id, int slot, double energy, c
     for (size_t b = 0; b < nblocks; ++b) {
       const FrontPlan& p = sys->plans[b]->host;
       const size_t nl = p.nl, nr = p.nr;
-      // Γ = i (Σ - Σ^†) (caroli-green/src/lib.rs:67-71).
-      std::vector<double> gl(2 * nl * nl), gr(2 * nr * nr);
-      auto gamma = [](const double* s, size_t m, std::vector<double>& g) {
-        for (size_t j = 0; j < m; ++j)
-          for (size_t i = 0; i < m; ++i) {
-            double dr = s[2 * (i + j * m)] - s[2 * (j + i * m)];
-            double di = s[2 * (i + j * m) + 1] + s[2 * (j + i * m) + 1];
-            g[2 * (i + j * m)] = -di;
-            g[2 * (i + j * m) + 1] = dr;
-          }
-      };
-      gamma(sigma_l[b], nl, gl);
-      gamma(sigma_r[b], nr, gr);
-      std::vector<double> wr;
+      put(sg.sl[b], sigma_l[b], nl * nl);
+      put(sg.sr[b], sigma_r[b], nr * nr);
+      // Γ = i (Σ - Σ^†) (caroli-green/src/lib.rs:67-71), formed on the device.
+      if (nl) {
+        lead_gamma_kernel<<<(unsigned)((nl * nl + 255) / 256), 256, 0, ctx->stream>>>(sg.sl[b], (int)nl, sg.gl[b]);
+        CK(cudaGetLastError());
+      }
+      if (nr) {
+        lead_gamma_kernel<<<(unsigned)((nr * nr + 255) / 256), 256, 0, ctx->stream>>>(sg.sr[b], (int)nr, sg.gr[b]);
+        CK(cudaGetLastError());
+      }
       int ch;
       if (w_right && channels) {
         ch = channels[b];
         if (ch < 0 || (size_t)ch > nr) return fail_with(ctx, CAROLI_EINVAL, "caroli_sigma_upload: bad channel count");
-        wr.assign(w_right[b], w_right[b] + 2 * nr * (size_t)ch);
+        if (ch && !w_right[b]) return fail_with(ctx, CAROLI_EINVAL, "caroli_sigma_upload: missing W_R");
+        put(sg.wr[b], w_right[b], nr * (size_t)ch);
       } else {
+        // W_R by pivoted Cholesky of the host's Γ_R.
+        std::vector<double> gr(2 * nr * nr), wr;
+        const double* sr = sigma_r[b];
+        for (size_t j = 0; j < nr; ++j)
+          for (size_t i = 0; i < nr; ++i) {
+            gr[2 * (i + j * nr)] = -(sr[2 * (i + j * nr) + 1] + sr[2 * (j + i * nr) + 1]);
+            gr[2 * (i + j * nr) + 1] = sr[2 * (i + j * nr)] - sr[2 * (j + i * nr)];
+          }
         ch = gamma_factor(gr, nr, wr);
+        put(sg.wr[b], wr.data(), nr * (size_t)ch);
+        keep.push_back(std::move(wr));
       }
       sg.channels[b] = ch;
-      put(sg.wr[b], wr.data(), nr * (size_t)ch);
-      put(sg.sl[b], sigma_l[b], nl * nl);
-      put(sg.sr[b], sigma_r[b], nr * nr);
-      put(sg.gl[b], gl.data(), nl * nl);
-      put(sg.gr[b], gr.data(), nr * nr);
-      keep.push_back(std::move(wr));
-      keep.push_back(std::move(gl));
-      keep.push_back(std::move(gr));
     }
     CK(cudaStreamSynchronize(ctx->stream));
     sg.energy = energy;
@@ -2786,10 +2791,12 @@ int solve_instances(caroli_ctx* ctx, const std::vector<System*>& isys, int count
     ctx->refine_job_steps = ctx->refine_batch_steps = 0;
     solve_jobs(ctx, count ? isys[0] : nullptr, specs, (Mode)precision, jo);
     ctx->job_iters.clear();
+    ctx->job_steps.clear();
     ctx->job_perturbed.clear();
     ctx->job_status.clear();
     for (const JobOut& o : jo) {
       ctx->job_iters.push_back(o.iters);
+      ctx->job_steps.push_back(o.steps);
       ctx->job_perturbed.push_back(o.perturbed);
       ctx->job_status.push_back(o.status);
     }
@@ -2840,6 +2847,15 @@ int caroli_last_phases(const caroli_ctx* ctx, double* factor_ms, double* root_ms
   if (factor_ms) *factor_ms = ctx->factor_ms;
   if (root_ms) *root_ms = ctx->root_ms;
   if (tail_ms) *tail_ms = ctx->tail_ms;
+  return CAROLI_OK;
+}
+
+int caroli_last_job_steps(const caroli_ctx* ctx, int64_t capacity, int32_t* steps, int64_t* count) {
+  if (!ctx || !count) return CAROLI_EINVAL;
+  const int64_t n = (int64_t)ctx->job_steps.size();
+  for (int64_t j = 0; j < n && j < capacity; ++j)
+    if (steps) steps[j] = ctx->job_steps[j];
+  *count = n;
   return CAROLI_OK;
 }
 

@@ -313,6 +313,9 @@ int caroli_last_stats(const caroli_ctx* ctx, int64_t* fallbacks, int64_t* max_re
 /* Per block solve of the last caroli_solve_batch (instance-major, blocks fastest; up to
  * `capacity` entries, *count = all): refinement iterations, pivots perturbed by static pivoting,
  * and status (100 + s: status s in reduced precision, then recomputed in double precision). */
+/* Per block solve of the last caroli_solve_batch (as caroli_last_job_info): GMRES (Arnoldi) steps
+ * of the mixed refinement, summed over its outer iterations (0 outside CAROLI_MIXED). */
+int caroli_last_job_steps(const caroli_ctx* ctx, int64_t capacity, int32_t* steps, int64_t* count);
 int caroli_last_job_info(const caroli_ctx* ctx, int64_t capacity, int32_t* iters, int32_t* perturbed,
                          int32_t* status, int64_t* count);
 
