@@ -153,6 +153,21 @@ class Model:
         m.hopping_terms.append(term)
         return m
 
+    def with_peierls(self, phase):
+        """Peierls phases: the block <i|H|j> times exp(i phase(r_i, r_j)) (``Model::with_peierls``,
+        ``caroli-model/src/lib.rs:276-280``, ``:369-378``), ``r`` the sites' positions."""
+        lat = self.lattice
+
+        def term(frm, to, t):
+            return t * np.exp(1j * phase(lat.position(frm), lat.position(to)))
+
+        return self.with_hopping_term(term)
+
+    def with_field(self, b):
+        """A uniform field b z in the Landau gauge A = (-b y, 0, 0) (``gauge::landau_x``,
+        ``caroli-model/src/lib.rs:157-164``): invariant along x, so for leads along x."""
+        return self.with_peierls(landau_x(b))
+
     def onsite_matrix(self, site: Site):
         m = self.onsite_m[site.sub].copy()
         for term in self.extra:
@@ -337,6 +352,11 @@ def gamma44():
 
 def gamma55():
     return np.diag([1, -1, 1, -1]).astype(np.complex128)
+
+
+def landau_x(b):
+    """Peierls phase of A = (-b y, 0, 0) between positions r_i, r_j: -b (y_i + y_j) (x_i - x_j) / 2."""
+    return lambda ri, rj: -b * 0.5 * (ri[1] + rj[1]) * (ri[0] - rj[0])
 
 
 def combine(terms):
