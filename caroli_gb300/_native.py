@@ -49,6 +49,7 @@ SIGNATURES = {
     "caroli_multi_leads": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P]),
     "caroli_transmission_matrix": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P, P]),
     "caroli_last_job_steps": (ctypes.c_int, [P, ctypes.c_int64, P, P]),
+    "caroli_gamma_override": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P]),
     "caroli_root_green": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P, P]),
     "caroli_multi_scattering_states": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P]),
     "caroli_multi_sector_transmissions": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, ctypes.c_int,
@@ -465,6 +466,14 @@ class Plan:
         self.ctx.check(self.ctx.lib.caroli_multi_transmissions(self.ctx.h, self.id, cnt, ptr(slots), ptr(configs),
                                                                precision, ptr(t), ptr(st)))
         return t[:cnt], st[:cnt]
+
+    def gamma_override(self, slot, gammas):
+        """``gammas[b] = (Γ_L, Γ_R)`` replacing the slot's trace broadenings (``caroli_gamma_override``)."""
+        gl = [np.asfortranarray(a, dtype=np.complex128) for a, _ in gammas]
+        gr = [np.asfortranarray(b, dtype=np.complex128) for _, b in gammas]
+        pl = np.array([a.ctypes.data for a in gl], dtype=np.uintp)
+        pr = np.array([b.ctypes.data for b in gr], dtype=np.uintp)
+        self.ctx.check(self.ctx.lib.caroli_gamma_override(self.ctx.h, self.id, slot, ptr(pl), ptr(pr)))
 
     def last_job_steps(self):
         """GMRES steps of each block solve of the last batch (``caroli_last_job_steps``)."""

@@ -2604,6 +2604,28 @@ int caroli_multi_scattering_states(caroli_ctx* ctx, int plan_id, int count, cons
   }
 }
 
+int caroli_gamma_override(caroli_ctx* ctx, int plan_id, int slot, const double* const* gamma_l,
+                          const double* const* gamma_r) {
+  System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
+  if (!sys || slot < 0 || slot >= (int)sys->slots.size() || !sys->slots[slot].set || !gamma_l || !gamma_r)
+    return fail_with(ctx, CAROLI_EINVAL, "caroli_gamma_override: bad arguments");
+  try {
+    CK(cudaSetDevice(ctx->device));
+    SigmaSlot& sg = sys->slots[slot];
+    for (size_t b = 0; b < sys->plans.size(); ++b) {
+      const size_t nl = sys->plans[b]->host.nl, nr = sys->plans[b]->host.nr;
+      if (nl && gamma_l[b])
+        CK(cudaMemcpyAsync(sg.gl[b], gamma_l[b], nl * nl * sizeof(double2), cudaMemcpyHostToDevice, ctx->stream));
+      if (nr && gamma_r[b])
+        CK(cudaMemcpyAsync(sg.gr[b], gamma_r[b], nr * nr * sizeof(double2), cudaMemcpyHostToDevice, ctx->stream));
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    return CAROLI_OK;
+  } catch (const CudaError& e) {
+    return fail_with(ctx, CAROLI_ECUDA, cudaGetErrorString(e.e));
+  }
+}
+
 int caroli_lead_modes(caroli_ctx* ctx, int plan_id, int block, int side, int n, const double* y, double sc) {
   System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
   if (!sys || block < 0 || block >= (int)sys->plans.size() || (side != 0 && side != 1) || !y)

@@ -180,6 +180,31 @@ class NestedTwoTerminal:
             blocks.append((sl, sr))
         return LeadSelfEnergies(float(energy), blocks)
 
+    def self_energies_broadened(self, energy, eta) -> LeadSelfEnergies:
+        """Σ at E + iη with the device at the real E (``SelfEnergyMethod::ModesBroadened``,
+        caroli-green/src/lib.rs:49-66): no propagating lead mode, as the thesis codes compute it."""
+        z = complex(energy, eta)
+        blocks = []
+        for left, right in self._solvers:
+            sl, sr_same, _ = left.self_energies(z)
+            sr = sr_same if right is left else right.self_energies(z)[1]
+            blocks.append((sl, sr))
+        return LeadSelfEnergies(float(energy), blocks)
+
+    def transmission_thesis(self, sigma, config=0):
+        """Tr[Re(Γ_L) G Re(Γ_R) G^†]: the thesis' transmission, broadenings truncated to their
+        element-wise real part (caroli-validation/src/thesis.rs:84-95), FP64 on the GPU."""
+        slot = self._slot(sigma)
+        re = [(np.real(1j * (sl - sl.conj().T)).astype(np.complex128),
+               np.real(1j * (sr - sr.conj().T)).astype(np.complex128)) for sl, sr in sigma.blocks]
+        self.plan().gamma_override(slot, re)
+        try:
+            t, st, _ = self.plan().solve([slot], [config], int(Precision.DOUBLE))
+        finally:
+            # The slot no longer holds the exact Γ: the next use of `sigma` uploads a fresh slot.
+            self._slot_of[id(sigma)] = (slot, None)
+        return _result(t[0], st[0], sigma.energy)
+
     # -- GPU plumbing -------------------------------------------------------------------------
     def plan(self):
         if self._plan is None:

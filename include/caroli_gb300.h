@@ -161,6 +161,13 @@ int caroli_sigma_from_modes(caroli_ctx* ctx, int plan_id, int slot, double energ
                             const double* const* d_right, const int32_t* channels, const int32_t* const* channel_modes,
                             const double* const* channel_weights);
 
+/* Replaces the broadenings Γ_L, Γ_R of a slot's trace (after caroli_sigma_upload; NULL keeps a
+ * block's), e.g. by their element-wise real part, the convention of the thesis codes
+ * (caroli-validation/src/thesis.rs:84-95) that reproduce their published conductances. Affects the
+ * CAROLI_DOUBLE and CAROLI_SINGLE traces. */
+int caroli_gamma_override(caroli_ctx* ctx, int plan_id, int slot, const double* const* gamma_l,
+                          const double* const* gamma_r);
+
 /* T for `count` instances (energy slot, configuration), summed over the blocks.
  *   precision       CAROLI_DOUBLE, CAROLI_SINGLE or CAROLI_MIXED
  *   t[count]        transmissions; status[count] per-instance status (CAROLI_OK ...)

@@ -53,8 +53,10 @@ def _dense(system, values, rows, cols):
     return out
 
 
-def transmission(system, energy, sigmas, config=0):
-    """T at real energy `energy` with `sigmas[b] = (Σ_L, Σ_R)` per block, summed over blocks."""
+def transmission(system, energy, sigmas, config=0, gamma=None):
+    """T at real energy `energy` with `sigmas[b] = (Σ_L, Σ_R)` per block, summed over blocks.
+    `gamma(Γ)` transforms the broadenings before the trace (the thesis codes take their real part,
+    caroli-validation/src/thesis.rs:84-95); None keeps them."""
     values = system.values[config]
     total = 0.0
     for b, (sl, sr) in enumerate(sigmas):
@@ -82,5 +84,7 @@ def transmission(system, energy, sigmas, config=0):
             g1n = g1n @ v @ g
         gl = 1j * (sl - sl.conj().T)
         gr = 1j * (sr - sr.conj().T)
+        if gamma is not None:
+            gl, gr = gamma(gl), gamma(gr)
         total += float(np.real(np.trace(gl @ g1n @ gr @ g1n.conj().T)))
     return total

@@ -9,7 +9,9 @@ It reads
 - reference/baseline/golden/ti-cond2t-clean/{axes,cond}_00.dat: the thesis conductance of the
   clean BHZ 16 x 10 ribbon (Fortran unformatted records, int32-framed float64);
 - crates/caroli-disorder/src/rng.rs: nothing (the RNG known answers are in the test itself).
-and writes tests/golden/bench_transmissions.json and tests/golden/ti_cond2t_clean.json.
+- reference/baseline/golden/ti-cond2t-{same-g,isotropic,opposite-g}: the thesis conductance of the
+  same ribbon with magnetic impurities;
+and writes tests/golden/bench_transmissions.json, ti_cond2t_clean.json and ti_cond2t_disorder.json.
 """
 import json
 import os
@@ -59,6 +61,19 @@ def main(ref):
     with open(os.path.join(HERE, "ti_cond2t_clean.json"), "w") as f:
         json.dump({"source": "reference/baseline/golden/ti-cond2t-clean (thesis conductance-2t, BHZ 16x10)",
                    "energies": axes[nu:], "conductance": [cond[ie * nu] for ie in range(ne)]}, f, indent=1)
+    # The magnetic-impurity cases: axes = 3 exchange couplings then 5 energies, cond(Nu, Ne)
+    # column-major (caroli-validation/tests/ti_conductance_disorder.rs:16-22).
+    cases = {}
+    for case in ("ti-cond2t-same-g", "ti-cond2t-isotropic", "ti-cond2t-opposite-g"):
+        g = os.path.join(ref, "reference/baseline/golden", case)
+        axes = records(os.path.join(g, "axes_00.dat"))[0]
+        cond = records(os.path.join(g, "cond_00.dat"))[0]
+        cases[case] = {"couplings": axes[:3], "energies": axes[3:], "cond": cond}
+    with open(os.path.join(HERE, "ti_cond2t_disorder.json"), "w") as f:
+        json.dump({"source": "reference/baseline/golden/ti-cond2t-{same-g,isotropic,opposite-g} (thesis "
+                             "conductance-2t: BHZ 16x10 + one lead slice at each end, 24 impurities, gfortran "
+                             "seed 12345, Σ at E + 1e-5 i, Re Γ trace); cond[iu + 3 ie]",
+                   "cases": cases}, f, indent=1)
 
 
 if __name__ == "__main__":

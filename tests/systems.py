@@ -176,3 +176,24 @@ def cross_system(width, model="square", seed=5, anderson=1.0):
 
     dev, clean, region, interfaces = cross_problem(width, model, seed, anderson)
     return NestedMultiTerminal.from_model(dev, clean, region, interfaces)
+
+
+def thesis_ribbon(case, coupling_j):
+    """The thesis' conductance-2t setup (caroli-validation/tests/ti_conductance_disorder.rs:24-40,
+    src/thesis.rs:53-82): BHZ 16 x 10 with one clean lead slice at each end, 24 magnetic
+    impurities drawn from gfortran seed 12345 in the central 8 x 10 region (x fastest), moments
+    along z (cone of zero angle) or isotropic, exchange J (n . S) with the case's spin coupling."""
+    from caroli_gb300.disorder import MagneticImpurities, Moments, Xoshiro256
+    from caroli_gb300.lattice import Site
+
+    nx, ny, nx_imp = 16, 10, 8
+    spin, coupling = {"ti-cond2t-same-g": (1, "same-g"), "ti-cond2t-isotropic": (0, "same-g"),
+                      "ti-cond2t-opposite-g": (1, "opposite-g")}[case]
+    x0 = 1 + (nx - nx_imp) // 2
+    region_imp = [Site((x0 + x, y, 0), 0) for y in range(ny) for x in range(nx_imp)]
+    n_imp = int(0.3 * nx_imp * ny)
+    moments = Moments.isotropic() if spin == 0 else Moments.cone(0.0)
+    imp = MagneticImpurities.generate(Xoshiro256.gfortran(12345), region_imp, n_imp, moments)
+    clean = bhz()
+    dev = bhz().with_onsite_term(imp.exchange(coupling_j, bhz_spin(coupling)))
+    return NestedTwoTerminal.from_model(dev, clean, Region.cuboid(clean.lattice, [nx + 2, ny, 0]), 0)

@@ -93,3 +93,43 @@ def test_gpu_chain():
         for e, a, b in zip(energies, tc, td):
             assert abs(a - 1.0) < 1e-10
             assert abs(b - _chain_answer(e, 0.7)) < 1e-10
+
+
+# -- the thesis' magnetic-impurity conductances (ti_conductance_disorder.rs) ------------------------
+def _thesis_golden():
+    import json
+    import os
+
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ti_cond2t_disorder.json")) as f:
+        return json.load(f)["cases"]
+
+
+CASES = ["ti-cond2t-same-g", "ti-cond2t-isotropic", "ti-cond2t-opposite-g"]
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_oracle_thesis_conductance(case):
+    """RGF oracle, Σ at E + 1e-5 i and the Re Γ trace: the thesis' values to 1e-9."""
+    from oracle import rgf
+    from systems import thesis_ribbon
+
+    g = _thesis_golden()[case]
+    for iu, u in enumerate(g["couplings"]):
+        sys_ = thesis_ribbon(case, u)
+        for ie, e in enumerate(g["energies"]):
+            sig = sys_.self_energies_broadened(e, 1e-5)
+            t = rgf.transmission(sys_.system, e, sig.blocks, gamma=lambda m: np.real(m).astype(complex))
+            assert abs(t - g["cond"][iu + 3 * ie]) < 1e-9
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", CASES)
+def test_gpu_thesis_conductance(case):
+    from systems import thesis_ribbon
+
+    g = _thesis_golden()[case]
+    for iu, u in enumerate(g["couplings"]):
+        sys_ = thesis_ribbon(case, u)
+        for ie, e in enumerate(g["energies"]):
+            t = sys_.transmission_thesis(sys_.self_energies_broadened(e, 1e-5))
+            assert abs(t - g["cond"][iu + 3 * ie]) < 1e-9
