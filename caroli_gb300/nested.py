@@ -349,6 +349,8 @@ class NestedTwoTerminal:
         ``GreenError`` in its place."""
         if configs is None:
             configs = [0] * len(sigmas)
+        if any(not isinstance(s, LeadSelfEnergies) for s in sigmas):
+            raise TypeError("scattering states take host self-energies (self_energies)")
         slots = [self._slot(s) for s in sigmas]
         outs, st = self.plan().scattering_states(slots, configs, [s.w_left() for s in sigmas],
                                                  [s.w_right() for s in sigmas], self.system.n)
