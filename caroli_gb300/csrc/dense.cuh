@@ -178,7 +178,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) inv_panel_kernel(
         const int col = 16 * h + c;
         if (col >= kb) continue;
         if (col == k) a[c] = cmul(cx<V>(-ak.x, -ak.y), pk[col]);
-        else a[c] = cfms(a[c], ak, pk[col]);
+        else a[c] = cfms_pk(a[c], ak, pk[col]);
       }
     }
     if (act)
