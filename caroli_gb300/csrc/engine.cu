@@ -105,6 +105,8 @@ struct SigmaSlot {
   // pointers.
   std::vector<double2*> mgam;
   std::vector<double2**> mtab;
+  std::vector<double2*> mw;  // W_p with W_p W_p^† = Γ_p per (block, lead): sources of the mixed path
+  std::vector<int> mch;      // its columns
 };
 
 // Block data the refinement needs (block-local CSR of H, slice positions).
@@ -160,7 +162,7 @@ struct System {
     cudaFree(vals);
     cudaFree(dvals);
     for (auto& s : slots) {
-      for (auto* v : {&s.sl, &s.sr, &s.gl, &s.gr, &s.wr, &s.mgam})
+      for (auto* v : {&s.sl, &s.sr, &s.gl, &s.gr, &s.wr, &s.mgam, &s.mw})
         for (auto* p : *v) cudaFree(p);
       for (auto* p : s.mtab) cudaFree(p);
     }
@@ -247,6 +249,9 @@ struct StatesRequest {
   // Transmission matrices instead of ψ: t = W_L^† x_L with these W_L (nl x tcl, device) per job.
   std::vector<const double2*> twl;
   std::vector<int> tcl;
+  // Multi-terminal transmissions instead of ψ: per job the leads' kept positions and Γ (MultiJob:
+  // lpos, lptr, gamma, P); out receives x_c(p)^† Γ_p x_c(p) for every lead p and column c.
+  std::vector<MultiJob> mtrace;
 };
 
 // One tree level of a batch: its fronts split by size class, and their algorithmic work.
@@ -640,7 +645,40 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
     CK(cudaMemcpyAsync(th.data(), rt_out, cj * sizeof(double), cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(eh.data(), rerr, cj * sizeof(double), cudaMemcpyDeviceToHost, s));
   }
-  if (states && !states->twl.empty()) {
+  if (states && !states->mtrace.empty()) {
+    // x_c(p)^† Γ_p x_c(p) per (job, lead, column) into the ψ buffers (P x c each).
+    size_t to = 0;
+    std::vector<size_t> toffs(cj);
+    int pmax = 1;
+    for (size_t j = 0; j < cj; ++j) {
+      toffs[j] = to;
+      to += (size_t)states->mtrace[begin + j].P * rdh[j].c;
+      pmax = std::max(pmax, states->mtrace[begin + j].P);
+    }
+    double* qdev = static_cast<double*>(ctx->tm_out.get(std::max<size_t>(to, 1) * sizeof(double)));
+    std::vector<MultiJob> mj(cj);
+    for (size_t j = 0; j < cj; ++j) {
+      mj[j] = states->mtrace[begin + j];
+      mj[j].out = qdev + toffs[j];
+    }
+    MultiJob* dmj = static_cast<MultiJob*>(ctx->tm_tab.get(cj * sizeof(MultiJob)));
+    CK(cudaMemcpyAsync(dmj, mj.data(), cj * sizeof(MultiJob), cudaMemcpyHostToDevice, s));
+    in_pieces(cj, [&](size_t f0, size_t c) {
+      launch(K_REF_CHECK, 0.0, 0.0, [&] {
+        multi_quadratic_kernel<<<dim3((unsigned)c, (unsigned)pmax, (unsigned)std::max(1, cmax)), 256, 0, s>>>(
+            drd + f0, dmj + f0);
+      });
+    });
+    for (size_t j = 0; j < cj; ++j) {
+      std::vector<double2>& t = (*states->psi)[begin + j];
+      const size_t cnt = (size_t)mj[j].P * rdh[j].c;
+      std::vector<double> tmp(cnt);
+      if (cnt) CK(cudaMemcpyAsync(tmp.data(), qdev + toffs[j], cnt * sizeof(double), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      t.resize(cnt);
+      for (size_t e = 0; e < cnt; ++e) t[e] = make_double2(tmp[e], 0.0);
+    }
+  } else if (states && !states->twl.empty()) {
     // t = W_L^† x_L per job into the ψ buffers (tcl x c each).
     size_t to = 0;
     std::vector<size_t> toffs(cj);
@@ -2014,6 +2052,106 @@ int caroli_scattering_states(caroli_ctx* ctx, int plan_id, int count, const int3
   }
 }
 
+}  // extern "C"
+
+namespace {
+
+// Multi-terminal T_pq in mixed precision: X = A^-1 [W_1 ... W_P] (every lead's sources,
+// W_p W_p^† = Γ_p) refined in FP64 from the f32 factors, then T_pq = Σ over lead q's columns of
+// x^†(p) Γ_p x(p). Block solves with more than MIXED_MAX_CHANNELS sources, and those the
+// refinement cannot resolve, take the FP64 path.
+void multi_mixed(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, std::vector<JobOut>& out) {
+  cudaStream_t s = ctx->stream;
+  const int P = sys->nleads;
+  out.assign(specs.size(), JobOut{});
+  std::vector<size_t> few, many;
+  for (size_t j = 0; j < specs.size(); ++j) {
+    const SigmaSlot& sg = sys->slots[specs[j].slot];
+    int c = 0;
+    for (int p = 0; p < P; ++p) c += sg.mch[(size_t)specs[j].block * P + p];
+    (c > MIXED_MAX_CHANNELS ? many : few).push_back(j);
+  }
+  std::vector<size_t> again = many;
+  if (!few.empty()) {
+    std::vector<JobSpec> fs;
+    StatesRequest rq;
+    std::vector<size_t> roff;
+    size_t relems = 0;
+    for (size_t j : few) {
+      const JobSpec& sp = specs[j];
+      fs.push_back(sp);
+      int c = 0;
+      for (int p = 0; p < P; ++p) c += sys->slots[sp.slot].mch[(size_t)sp.block * P + p];
+      rq.cl.push_back(c);
+      rq.cr.push_back(0);
+      rq.wl.push_back(nullptr);
+      rq.wr.push_back(nullptr);
+      roff.push_back(relems);
+      relems += (size_t)sys->blocks[sp.block].nblk * c;
+    }
+    double2* rhs = static_cast<double2*>(ctx->states_rhs.get(std::max<size_t>(relems, 1) * sizeof(double2)));
+    CK(cudaMemsetAsync(rhs, 0, std::max<size_t>(relems, 1) * sizeof(double2), s));
+    for (size_t k = 0; k < fs.size(); ++k) {
+      const JobSpec& sp = fs[k];
+      const SigmaSlot& sg = sys->slots[sp.slot];
+      const int b = sp.block;
+      int c0 = 0;
+      for (int p = 0; p < P; ++p) {
+        const int np = sys->mptr[b][p + 1] - sys->mptr[b][p], c = sg.mch[(size_t)b * P + p];
+        if (np && c) {
+          scatter_sources_kernel<<<(unsigned)(((int64_t)np * c + 255) / 256), 256, 0, s>>>(
+              rhs + roff[k], sys->blocks[b].nblk, c0, sys->blocks[b].left_local, sys->dmpos[b] + sys->mptr[b][p], np,
+              sg.mw[(size_t)b * P + p], c);
+          CK(cudaGetLastError());
+        }
+        c0 += c;
+      }
+      rq.rhs.push_back(rhs + roff[k]);
+      MultiJob m{};
+      m.lpos = sys->dmpos[b];
+      m.lptr = sys->dmptr[b];
+      m.gamma = sg.mtab[b];
+      m.P = P;
+      rq.mtrace.push_back(m);
+    }
+    std::vector<std::vector<double2>> q(fs.size());
+    rq.psi = &q;
+    std::vector<JobOut> fo;
+    run_jobs<float, float>(ctx, sys, fs, MODE_MIXED, fo, nullptr, &rq);
+    for (size_t k = 0; k < fs.size(); ++k) {
+      const size_t j = few[k];
+      JobOut& o = out[j];
+      o = fo[k];
+      o.tm.assign((size_t)P * P, 0.0);
+      const SigmaSlot& sg = sys->slots[fs[k].slot];
+      const int b = fs[k].block, c = rq.cl[k];
+      if (o.status != ST_OK || q[k].size() < (size_t)P * c) {
+        again.push_back(j);
+        continue;
+      }
+      int c0 = 0;
+      for (int lq = 0; lq < P; ++lq) {
+        const int cq = sg.mch[(size_t)b * P + lq];
+        for (int p = 0; p < P; ++p)
+          for (int cc = c0; cc < c0 + cq; ++cc) o.tm[(size_t)p * P + lq] += q[k][(size_t)p * c + cc].x;
+        c0 += cq;
+      }
+    }
+  }
+  if (!again.empty()) {
+    std::vector<JobSpec> as;
+    for (size_t j : again) as.push_back(specs[j]);
+    std::vector<JobOut> ao;
+    solve_jobs(ctx, sys, as, MODE_DOUBLE, ao);
+    for (size_t k = 0; k < again.size(); ++k) out[again[k]] = std::move(ao[k]);
+    ctx->fallbacks += (int64_t)(again.size() - many.size());  // the refinement's failures, not the routing
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
 int caroli_multi_leads(caroli_ctx* ctx, int plan_id, int nleads, const int64_t* lead_ptr, const int64_t* lead_orbitals) {
   System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
   if (!sys || nleads <= 0 || !lead_ptr || !lead_orbitals)
@@ -2101,12 +2239,15 @@ int caroli_multi_sigma_upload(caroli_ctx* ctx, int plan_id, int slot, double ene
     if (sg.mgam.size() != (size_t)nb * P) {
       for (auto* p : sg.mgam) cudaFree(p);
       for (auto* p : sg.mtab) cudaFree(p);
+      for (auto* p : sg.mw) cudaFree(p);
       sg.mgam.clear();
       sg.mtab.clear();
+      sg.mw.clear();
       for (int b = 0; b < nb; ++b) {
         for (int p = 0; p < P; ++p) {
           const size_t np = (size_t)(sys->mptr[b][p + 1] - sys->mptr[b][p]);
           sg.mgam.push_back(dalloc<double2>(std::max<size_t>(np * np, 1)));
+          sg.mw.push_back(dalloc<double2>(std::max<size_t>(np * np, 1)));
         }
         sg.mtab.push_back(dalloc<double2*>((size_t)P));
         CK(cudaMemcpyAsync(sg.mtab[b], sg.mgam.data() + (size_t)b * P, P * sizeof(double2*), cudaMemcpyHostToDevice,
@@ -2114,6 +2255,7 @@ int caroli_multi_sigma_upload(caroli_ctx* ctx, int plan_id, int slot, double ene
       }
     }
     std::vector<std::vector<double>> keep;
+    sg.mch.assign((size_t)nb * P, 0);
     for (int b = 0; b < nb; ++b)
       for (int p = 0; p < P; ++p) {
         const size_t np = (size_t)(sys->mptr[b][p + 1] - sys->mptr[b][p]);
@@ -2130,7 +2272,13 @@ int caroli_multi_sigma_upload(caroli_ctx* ctx, int plan_id, int slot, double ene
           }
         CK(cudaMemcpyAsync(sg.mgam[(size_t)b * P + p], g.data(), np * np * sizeof(double2), cudaMemcpyHostToDevice,
                            ctx->stream));
+        std::vector<double> w;
+        sg.mch[(size_t)b * P + p] = gamma_factor(g, np, w);
+        if (!w.empty())
+          CK(cudaMemcpyAsync(sg.mw[(size_t)b * P + p], w.data(), w.size() / 2 * sizeof(double2), cudaMemcpyHostToDevice,
+                             ctx->stream));
         keep.push_back(std::move(g));
+        keep.push_back(std::move(w));
       }
     CK(cudaStreamSynchronize(ctx->stream));
     sg.set = true;
@@ -2146,8 +2294,8 @@ int caroli_multi_transmissions(caroli_ctx* ctx, int plan_id, int count, const in
   if (!sys || count < 0 || (count > 0 && (!slots || !configs || !t || !status)))
     return fail_with(ctx, CAROLI_EINVAL, "caroli_multi_transmissions: bad arguments");
   if (sys->nleads <= 0) return fail_with(ctx, CAROLI_EINVAL, "caroli_multi_transmissions: no leads (caroli_multi_leads)");
-  if (precision != CAROLI_DOUBLE && precision != CAROLI_SINGLE)
-    return fail_with(ctx, CAROLI_EINVAL, "caroli_multi_transmissions: CAROLI_DOUBLE or CAROLI_SINGLE");
+  if (precision != CAROLI_DOUBLE && precision != CAROLI_SINGLE && precision != CAROLI_MIXED)
+    return fail_with(ctx, CAROLI_EINVAL, "caroli_multi_transmissions: unknown precision");
   if (!sys->vals) return fail_with(ctx, CAROLI_EINVAL, "no H values uploaded");
   for (int i = 0; i < count; ++i) {
     if (slots[i] < 0 || slots[i] >= (int)sys->slots.size() || !sys->slots[slots[i]].set ||
@@ -2168,7 +2316,8 @@ int caroli_multi_transmissions(caroli_ctx* ctx, int plan_id, int count, const in
     for (int i = 0; i < count; ++i)
       for (int b = 0; b < nb; ++b) specs.push_back({b, slots[i], configs[i], sys->plans[b].get(), sys});
     std::vector<JobOut> jo;
-    solve_jobs(ctx, sys, specs, (Mode)precision, jo);
+    if (precision == CAROLI_MIXED) multi_mixed(ctx, sys, specs, jo);
+    else solve_jobs(ctx, sys, specs, (Mode)precision, jo);
     for (int i = 0; i < count; ++i) {
       double* ti = t + (size_t)i * P * P;
       std::fill(ti, ti + (size_t)P * P, 0.0);

@@ -498,6 +498,38 @@ __global__ void tmatrix_kernel(const RefineDesc* __restrict__ rd, const double2*
   }
 }
 
+// Multi-terminal transmissions from the refined solution: for lead p and column c of job j,
+// out[p * c_j + c] = x_c(p)^† Γ_p x_c(p), x_c(p) the rows of lead p's orbitals (block-local rows
+// left_local[lpos[...]]). T_pq sums these over the columns sourced by lead q. grid (jobs, P, c).
+__global__ void __launch_bounds__(256) multi_quadratic_kernel(const RefineDesc* __restrict__ rd,
+                                                              const MultiJob* __restrict__ mj) {
+  __shared__ double red[32];
+  const RefineDesc& R = rd[blockIdx.x];
+  const MultiJob& J = mj[blockIdx.x];
+  const int p = blockIdx.y, c = blockIdx.z;
+  if (p >= J.P || c >= R.c) return;
+  const int np = J.lptr[p + 1] - J.lptr[p];
+  const int32_t* pos = J.lpos + J.lptr[p];
+  const double2* G = J.gamma[p];
+  const double2* x = R.x + (int64_t)c * R.nblk;
+  double local = 0.0;
+  for (int a = threadIdx.x; a < np; a += blockDim.x) {
+    double2 y = make_double2(0.0, 0.0);
+    for (int b = 0; b < np; ++b) y = cfma(y, G[a + (int64_t)b * np], x[R.left_local[pos[b]]]);
+    const double2 xa = x[R.left_local[pos[a]]];
+    local += xa.x * y.x + xa.y * y.y;
+  }
+  for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) red[w] = local;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sum = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) sum += red[k];
+    J.out[p * R.c + c] = sum;
+  }
+}
+
 // Multi-terminal sources: W_p (np x c, column-major) on the block-local rows of lead p's orbitals,
 // rows[a] = left_local[pos[a]], into columns c0 .. c0 + c of B (nblk rows). grid: np x c elements.
 __global__ void scatter_sources_kernel(double2* __restrict__ B, int nblk, int c0, const int32_t* __restrict__ left_local,

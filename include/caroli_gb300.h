@@ -255,7 +255,10 @@ int caroli_scattering_states(caroli_ctx* ctx, int plan_id, int count, const int3
  * 4. caroli_multi_transmissions: t[(i * nleads + p) * nleads + q] = T_pq = Tr[Γ_p G_pq Γ_q G_pq^†]
  *    from lead q into lead p, summed over the blocks (nested_multi.rs:337-364), for `count`
  *    instances (energy slot, configuration); CAROLI_DOUBLE or CAROLI_SINGLE, as the reference's
- *    Precision. The two-terminal entry points refuse a plan with leads. */
+ *    Precision, or CAROLI_MIXED (no counterpart): X = A^-1 [W_1 ... W_P], W_p W_p^† = Γ_p, refined in
+ *    FP64 from f32 factors and T_pq = Σ over lead q's columns of x(p)^† Γ_p x(p); block solves with
+ *    more than 96 sources in all, or that the refinement cannot resolve, take the FP64 path.
+ *    The two-terminal entry points refuse a plan with leads. */
 int caroli_multi_leads(caroli_ctx* ctx, int plan_id, int nleads, const int64_t* lead_ptr, const int64_t* lead_orbitals);
 /* Transmissions between sectors of the leads (NestedMultiTerminal::sector_transmissions,
  * nested_multi.rs:226-295): `nlabels` trace labels, label k on the orbitals of lead label_lead[k],

@@ -146,7 +146,7 @@ def test_gpu_multi_configs_and_errors():
     sig = multi.self_energies(0.1)
     slot = multi._slot(sig)
     with pytest.raises(_native.NativeError):
-        multi.plan().multi_solve([slot], [0], int(Precision.MIXED), 4)
+        multi.plan().multi_solve([slot], [0], 7, 4)  # no such precision
     with pytest.raises(_native.NativeError):
         multi.plan().solve([slot], [0], int(Precision.DOUBLE))
     t, st = multi.plan().multi_solve([], [], int(Precision.DOUBLE), 4)
@@ -237,3 +237,31 @@ def test_gpu_spin_sector_transmissions():
         assert np.max(np.abs(folded - s.transmissions(e))) < 1e-9
     with pytest.raises(ValueError):
         s.sector_transmissions(0.05, [[0, 0, 1, 1]] * 3)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("model,seed,w,energies", [("square", 5, 1.0, (-2.5, 0.1, 1.7)),
+                                                   ("bhz", 3, 0.5, (-0.2, 0.05, 0.3))])
+def test_gpu_multi_mixed_matches_double(model, seed, w, energies):
+    """CAROLI_MIXED T_pq (few channels per lead: refined in FP64) against FP64: ≤ 1e-8."""
+    from caroli_gb300 import Precision
+
+    s = cross_system(8, model=model, seed=seed, anderson=w)
+    td = s.transmissions_batch(list(energies))
+    tm = s.transmissions_batch(list(energies), precision=Precision.MIXED)
+    for a, b in zip(td, tm):
+        assert np.max(np.abs(a - b)) < 1e-8
+
+
+@pytest.mark.gpu
+def test_gpu_multi_mixed_routes_many_channels():
+    """The W = 32 square cross has up to 128 sources per block solve: CAROLI_MIXED takes the FP64
+    path for those and still gives the published values."""
+    from caroli_gb300 import Precision
+
+    g = bench_golden()["caroli/square-cross/32"]
+    runs = np.array(g["runs"])
+    s = cross_system(32)
+    got = s.transmissions_batch(g["energies"], precision=Precision.MIXED)
+    for k, t in enumerate(got):
+        assert np.max(np.abs(_off_diagonal(t) - runs[0][12 * k:12 * k + 12])) < 1e-8
