@@ -211,12 +211,15 @@ class Model:
                 pos = np.searchsorted(sorted_keys, pk)
                 pos = np.minimum(pos, len(sorted_keys) - 1)
                 found = sorted_keys[pos] == pk
+                # One matrix object per hopping and direction when no term depends on the bond
+                # (the builder groups identical blocks by object).
+                fixed = hop.matrix.conj().T.copy() if adjoint else hop.matrix
                 for i, j in zip(idx[found], order[pos[found]]):
                     if self.hopping_terms:
                         si, sj = a.sites[i], b.sites[j]
                         m = self._hop_matrix(hop, sj, si).conj().T if adjoint else self._hop_matrix(hop, si, sj)
                     else:
-                        m = hop.matrix.conj().T if adjoint else hop.matrix
+                        m = fixed
                     yield int(i), int(j), m
 
     def sparse_hamiltonian(self, region: Region) -> SparseMatrix:
