@@ -1,0 +1,68 @@
+"""Host lead algebra (CPU): the unit-current propagating modes the scattering matrix uses, the two
+eigen paths of the general lead problem (standard eigenproblem of B^-1 A and QZ of the pencil)
+agreeing, and the Landauer-Büttiker voltages of a four-terminal device."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from caroli_gb300 import NestedTwoTerminal, Region, bhz, graphene, lead_voltages, square
+from caroli_gb300.leads import LeadSolver
+
+
+def _lead(model, width):
+    s = NestedTwoTerminal.from_model(model, model, Region.cuboid(model.lattice, [3, width, 0]), 0)
+    b = s.system.blocks[0]
+    return LeadSolver(b.right_h00, b.right_h01)
+
+
+def _current(h01, phi, lam):
+    return (1j * (lam * np.vdot(phi, h01 @ phi) - np.conj(lam) * np.vdot(phi, h01.conj().T @ phi))).real
+
+
+@pytest.mark.parametrize("model,width,energies", [(square(), 7, (-2.5, -0.3, 1.1)), (bhz(), 12, (0.3, 0.6)),
+                                                  (graphene(), 6, (-1.2, 0.4))])
+def test_modes_carry_unit_current(model, width, energies):
+    ls = _lead(model, width)
+    for e in energies:
+        rm, rl, lm, ll, rest, _ = ls.modes(e)
+        assert rm.shape[1] == lm.shape[1] and rm.shape[1] > 0
+        for k in range(rm.shape[1]):
+            assert abs(_current(ls.h01, rm[:, k], rl[k]) - 1.0) < 1e-9
+            assert abs(_current(ls.h01, lm[:, k], ll[k]) + 1.0) < 1e-9
+            assert abs(abs(rl[k]) - 1.0) < 1e-6 and abs(abs(ll[k]) - 1.0) < 1e-6
+        # The channel count is the rank of Γ_R = i (Σ - Σ^†).
+        g = 1j * (rest - rest.conj().T)
+        assert np.sum(np.linalg.eigvalsh(0.5 * (g + g.conj().T)) > 1e-9) == rm.shape[1]
+
+
+def test_standard_and_qz_paths_agree():
+    ls = _lead(bhz(), 16)
+    assert ls.h01_inv is not None
+    for e in (-0.13, 0.02, 0.3, complex(0.05, 1e-5)):
+        fast = ls.self_energies(e)
+        inv, ls.h01_inv = ls.h01_inv, None
+        try:
+            slow = ls.self_energies(e)
+        finally:
+            ls.h01_inv = inv
+        for a, b in zip(fast[:2], slow[:2]):
+            assert np.max(np.abs(a - b)) < 1e-11 * max(1.0, np.abs(b).max())
+
+
+def test_graphene_coupling_takes_qz():
+    assert _lead(graphene(), 6).h01_inv is None
+
+
+def test_lead_voltages_four_terminal():
+    """A symmetric four-terminal cross, T_pq = t between neighbouring leads and d across: a unit
+    current from lead 0 to lead 1 (opposite) with 2 and 3 floating puts the floating leads halfway,
+    and the voltages reproduce the imposed currents."""
+    t, d = 0.7, 0.2
+    # Leads 0, 1 opposite; 2, 3 opposite.
+    T = np.array([[0, d, t, t], [d, 0, t, t], [t, t, 0, d], [t, t, d, 0]], float)
+    v = lead_voltages(T, [1.0, -1.0, 0.0, 0.0], 1)
+    assert abs(v[2] - v[3]) < 1e-12 and abs(v[2] - 0.5 * v[0]) < 1e-12
+    # I_p = Σ_q (T_qp V_p - T_pq V_q) reproduces the imposed currents.
+    cur = [sum(T[q][p] * v[p] - T[p][q] * v[q] for q in range(4)) for p in range(4)]
+    assert np.allclose(cur, [1.0, -1.0, 0.0, 0.0], atol=1e-12)
