@@ -174,6 +174,7 @@ class NestedMultiTerminal:
                         interior=interior, labels=labels, blocks=blocks, axis=0)
         out = NestedMultiTerminal(system, block_leads, len(leads), device)
         out.sites = list(region.sites)
+        out._region = region
         # For each lead, the index of every orbital of its cell within its site (nested_multi.rs:147-150).
         out.orbital_kinds = [[o for i in range(len(itf.slice)) for o in range(itf.slice.site_orbitals(i))]
                              for itf in interfaces]
@@ -181,6 +182,10 @@ class NestedMultiTerminal:
 
     def lead_count(self):
         return self.nleads
+
+    def region(self):
+        """The device region (orbital layout of the scattering states, nested_multi.rs:512-515)."""
+        return getattr(self, "_region", None)
 
     def block_count(self):
         return len(self.system.blocks)

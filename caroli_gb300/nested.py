@@ -104,6 +104,7 @@ class NestedTwoTerminal:
     def from_model(device_model, lead, region, axis, device=0):
         out = NestedTwoTerminal(build_system([device_model], lead, region, axis), device)
         out.sites = list(region.sites)
+        out._region = region
         return out
 
     @staticmethod
@@ -111,6 +112,7 @@ class NestedTwoTerminal:
         """One system per disorder configuration of the same geometry and leads."""
         out = NestedTwoTerminal(build_system(list(device_models), lead, region, axis), device)
         out.sites = list(region.sites)
+        out._region = region
         return out
 
     @staticmethod
@@ -156,6 +158,7 @@ class NestedTwoTerminal:
         system = build_system([clean_model], lead, region, axis, extra=extra)
         out = NestedTwoTerminal(system, device)
         out.sites = list(region.sites)
+        out._region = region
         out._disorder = (entries, int(nconfigs), int(first_config))
         return out
 
@@ -165,6 +168,11 @@ class NestedTwoTerminal:
 
     def block_count(self):
         return len(self.system.blocks)
+
+    def region(self):
+        """The device region (orbital layout of the scattering states, nested.rs:920-923), or None
+        for a system not built from a region."""
+        return getattr(self, "_region", None)
 
     def config_count(self):
         if getattr(self, "_disorder", None) is not None:
