@@ -1,4 +1,4 @@
-/* caroli_gb300 — C ABI of the GB300 (sm_103a) nested-dissection transmission of caroli.
+/* caroli_gb300 — C ABI of the GB300 (sm_103a) nested-dissection transport of caroli.
  *
  * This is the boundary a caroli caller binds: plain pointers and sizes, an int status on every
  * call, no exceptions across the ABI. The caller owns its host buffers; the library owns the
@@ -28,6 +28,10 @@
  *   caroli_root_green                        lead_green / the root of smatrix     nested.rs:717-802
  *   caroli_transmission_with_grad            no counterpart: the reference has no derivative code;
  *   caroli_derivs_upload                     the adjoint of transmission_with (dT/dV, dT/dJ)
+ *   caroli_gamma_override                    the thesis' Re Γ trace               caroli-validation/src/thesis.rs:84-95
+ *   caroli_solve_multi, caroli_solve_batch_noalloc, caroli_set_*, caroli_last_*, caroli_region_*,
+ *   caroli_kernel_*, caroli_probe_kernel     no counterpart: batching across systems, an
+ *                                            allocation-free FP64 entry, controls and accounting
  *   caroli_last_error                        GreenError / GpuError text           caroli-green/src/lib.rs:34-47
  */
 #ifndef CAROLI_GB300_H
