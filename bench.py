@@ -461,7 +461,7 @@ def main():
     ap.add_argument("--configs", type=int, default=8)
     ap.add_argument("--energies", type=int, default=33)
     ap.add_argument("--cpu-sample", type=int, default=264)
-    ap.add_argument("--ref-sample", type=int, default=132)
+    ap.add_argument("--ref-sample", type=int, default=264)
     ap.add_argument("--profile-run", action="store_true", help="warm-up steps and one step, no timing (profilers)")
     ap.add_argument("--no-gradient", dest="gradient", action="store_false", help="skip the grad/fwd measurement")
     args = ap.parse_args()

@@ -44,6 +44,8 @@ SIGNATURES = {
     "caroli_last_refine_steps": (ctypes.c_int, [P, P, P]),
     "caroli_set_refine_options": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_double, ctypes.c_double]),
     "caroli_set_tensor_cores": (ctypes.c_int, [P, ctypes.c_int]),
+    "caroli_set_mixed_max_channels": (ctypes.c_int, [P, ctypes.c_int]),
+    "caroli_set_wait_limit": (ctypes.c_int, [P, ctypes.c_int64]),
     "caroli_solve_multi": (ctypes.c_int, [P, ctypes.c_int, P, P, P, ctypes.c_int, P, P, P]),
     "caroli_scattering_states": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P, P, P, P]),
     "caroli_multi_leads": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P]),
@@ -139,6 +141,14 @@ class Context:
     def set_tensor_cores(self, enable=True):
         """f32 rank-32 updates on the tcgen05 tensor cores (True) or the CUDA cores."""
         self.check(self.lib.caroli_set_tensor_cores(self.h, 1 if enable else 0))
+
+    def set_mixed_max_channels(self, channels=96):
+        """Mixed-precision block solves with more sources than ``channels`` take the FP64 path."""
+        self.check(self.lib.caroli_set_mixed_max_channels(self.h, int(channels)))
+
+    def set_wait_limit(self, polls=-1):
+        """Polls of a tensor-core pipeline wait before it gives up (negative: the default)."""
+        self.check(self.lib.caroli_set_wait_limit(self.h, int(polls)))
 
     def solve_multi(self, plans, slots, configs, precision=DOUBLE):
         """T for instances of several plans of this context in one batch (``caroli_solve_multi``)."""

@@ -290,8 +290,9 @@ __global__ void __launch_bounds__(256) inv_update_kernel(const InvTask* __restri
 //   warps 2-9 (two per 32-lane quarter of tensor memory, 32 columns each) add each finished tile to
 //   the old values (zero on the pivot rows) while the next tile is copied and multiplied.
 // Barriers: bfull (B' copied), bempty (its MMAs done), tfull[a] (accumulator a ready), tempty[a]
-// (accumulator a drained). Every wait is bounded; one that runs out sets ST_TIMEOUT for the
-// solve and stops the CTA after the copies and MMAs it issued have drained.
+// (accumulator a drained). Every wait is bounded: the pipeline waits by `wait_limit` polls (TCU_WAIT
+// unless the caller lowers it), the final drain by TCU_WAIT. A pipeline wait that runs out sets
+// ST_TIMEOUT for the solve and stops the CTA after the copies and MMAs it issued have drained.
 // grid (row tiles, matrices, column groups), 320 threads: a CTA walks TCU_GROUP column tiles,
 // so a few very wide fronts still spread over many CTAs.
 constexpr int TCU_EPI_WARPS = 16;
@@ -301,7 +302,7 @@ constexpr int TCU_SMEM = 2 * TCU_A_BYTES + 2 * TCU_B_BYTES + 1024;
 constexpr uint32_t TCU_WAIT = 1u << 22;
 
 __global__ void __launch_bounds__(TCU_THREADS, 2) tc_update_kernel(const InvTask* __restrict__ tasks, int k0,
-                                                                int32_t* __restrict__ status) {
+                                                                int32_t* __restrict__ status, uint32_t wait_limit) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ uint32_t tslot;
   __shared__ __align__(8) uint64_t bfull, bempty, tfull[2], tempty[2];
@@ -364,7 +365,7 @@ __global__ void __launch_bounds__(TCU_THREADS, 2) tc_update_kernel(const InvTask
   if (w == 0) {
     if (lane == 0)
       for (int ct = 0; ct < tiles && !*abort_v; ++ct) {
-        if (ct >= 1 && !tc::mbar_wait(&bempty, (uint32_t)((ct - 1) & 1), TCU_WAIT)) { fail(); break; }
+        if (ct >= 1 && !tc::mbar_wait(&bempty, (uint32_t)((ct - 1) & 1), wait_limit)) { fail(); break; }
         tc::mbar_arrive_expect_tx(&bfull, 2 * TCU_B_BYTES);
         const size_t tile = (size_t)(tile0 + ct) * 2 * TCU_B_BYTES;
         tc::bulk_copy_g2s(b_hi, bt + tile, TCU_B_BYTES, &bfull);
@@ -377,8 +378,8 @@ __global__ void __launch_bounds__(TCU_THREADS, 2) tc_update_kernel(const InvTask
       const int slices = (2 * kb + 7) / 8;
       for (int ct = 0; ct < tiles && !*abort_v; ++ct) {
         const int a = ct & 1;
-        if (!tc::mbar_wait(&bfull, (uint32_t)(ct & 1), TCU_WAIT)) { fail(); break; }
-        if (ct >= 2 && !tc::mbar_wait(&tempty[a], (uint32_t)(((ct >> 1) - 1) & 1), TCU_WAIT)) { fail(); break; }
+        if (!tc::mbar_wait(&bfull, (uint32_t)(ct & 1), wait_limit)) { fail(); break; }
+        if (ct >= 2 && !tc::mbar_wait(&tempty[a], (uint32_t)(((ct >> 1) - 1) & 1), wait_limit)) { fail(); break; }
         tc::fence_after_sync();
         const uint32_t d = tbase + (uint32_t)(a * TCU_COLS);
         for (int sl = 0; sl < slices; ++sl) {
@@ -414,7 +415,7 @@ __global__ void __launch_bounds__(TCU_THREADS, 2) tc_update_kernel(const InvTask
         old[j] = 0.f;
         if (row_in && !pivot_row && r < rest) old[j] = Af[2 * (gi + (int64_t)(r < k0 ? r : r + kb) * ld)];
       }
-      bool ok = !*abort_v && tc::mbar_wait(&tfull[a], (uint32_t)((ct >> 1) & 1), TCU_WAIT);
+      bool ok = !*abort_v && tc::mbar_wait(&tfull[a], (uint32_t)((ct >> 1) & 1), wait_limit);
       ok = __all_sync(0xffffffffu, ok);
       if (!ok) {
         if (lane == 0) fail();

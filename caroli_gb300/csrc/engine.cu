@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <numeric>
 #include <string>
 #include <type_traits>
@@ -332,7 +333,18 @@ struct caroli_ctx {
   std::vector<int32_t> job_iters, job_perturbed, job_status, job_steps;
   std::vector<int32_t> steps_tmp;  // Arnoldi steps of each job of the last refinement
   size_t mem_budget = 0;
+  int mixed_max_channels = MIXED_MAX_CHANNELS;  // CAROLI_MIXED block solves with more channels run in FP64
+  uint32_t tc_wait_limit = TCU_WAIT;            // polls of a pipeline wait in tc_update_kernel
+  unsigned char* noalloc_base = nullptr;        // device address of the allocation-free scratch array
+  // Every entry point taking the context holds this for its whole call, so that threads sharing a
+  // context are serialised (recursive: an entry point may reach another one's helpers).
+  mutable std::recursive_mutex mu;
 };
+
+// Serialises the calls of threads sharing a context.
+#define CTX_LOCK(ctx) \
+  std::unique_lock<std::recursive_mutex> _ctx_lock = (ctx) ? std::unique_lock<std::recursive_mutex>((ctx)->mu) \
+                                                           : std::unique_lock<std::recursive_mutex>()
 
 namespace {
 
@@ -1145,7 +1157,7 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
               tc_update_kernel<<<dim3((unsigned)((nmax + TCU_ROWS - 1) / TCU_ROWS), (unsigned)c,
                                       (unsigned)((nmax + TCU_COLS * TCU_GROUP - 1) / (TCU_COLS * TCU_GROUP))),
                                  TCU_THREADS, TCU_SMEM, s>>>(
-                  dinv + first + f0, k0, status);
+                  dinv + first + f0, k0, status, ctx->tc_wait_limit);
             else
               inv_update_kernel<TT><<<dim3(rt, rt, (unsigned)c), 256, 0, s>>>(dinv + first + f0, k0);
           });
@@ -1349,11 +1361,14 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
       const size_t nf = specs[begin + j].plan->host.fronts.size();
       bool delayed = false;
       for (size_t k = 0; k < nf; ++k) delayed |= fh[fail_off[j] + k] != 0;
-      if (delayed && !mixed) {
-        st = ST_PIVOT_DELAYED;
-        o.fail.assign(fh.begin() + fail_off[j], fh.begin() + fail_off[j] + nf);
-      } else if (delayed) {
-        st = ST_REFINE_STALLED;
+      // A timed-out solve keeps its status: its fronts hold garbage that re-planning cannot fix.
+      if (delayed && st != ST_TIMEOUT) {
+        if (!mixed) {
+          st = ST_PIVOT_DELAYED;
+          o.fail.assign(fh.begin() + fail_off[j], fh.begin() + fail_off[j] + nf);
+        } else {
+          st = ST_REFINE_STALLED;
+        }
       }
       o.status = st;
       o.perturbed = ph[j];
@@ -1417,14 +1432,14 @@ void solve_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs,
     solve_with_delays<float, double>(ctx, sys, specs, mode, out);
   } else {
     // Block solves with many right-lead channels go to the FP64 path directly: the refinement
-    // carries one right-hand side per channel through every sweep, and past MIXED_MAX_CHANNELS
+    // carries one right-hand side per channel through every sweep, and past ctx->mixed_max_channels
     // that costs more than the FP64 factorization it replaces (a 32 x 32-site cubic lead has
     // hundreds of open channels; the two-dimensional ribbons have a few).
     std::vector<JobSpec> few;
     std::vector<size_t> few_idx, many_idx;
     for (size_t j = 0; j < specs.size(); ++j) {
       const int c = specs[j].sys->slots[specs[j].slot].channels[specs[j].block];
-      if (c > MIXED_MAX_CHANNELS) many_idx.push_back(j);
+      if (c > ctx->mixed_max_channels) many_idx.push_back(j);
       else { few.push_back(specs[j]); few_idx.push_back(j); }
     }
     out.assign(specs.size(), JobOut{});
@@ -1520,6 +1535,9 @@ double2* upload_c64(const double* host, size_t count, cudaStream_t s) {
 
 }  // namespace
 
+// Defined beside caroli_solve_batch_noalloc, which uses it.
+cudaError_t noalloc_lookup(unsigned char** out);
+
 extern "C" {
 
 int caroli_ctx_create(int device_ordinal, caroli_ctx** out) {
@@ -1563,6 +1581,9 @@ int caroli_ctx_create(int device_ordinal, caroli_ctx** out) {
       const int room = std::min<int>(SMEM_LIMIT, optin - (int)fa.sharedSizeBytes);
       CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, room));
     }
+    // The allocation-free entry point's static scratch: its device address on this device, once,
+    // so that caroli_solve_batch_noalloc itself only launches kernels and copies.
+    CK(noalloc_lookup(&ctx->noalloc_base));
   } catch (const CudaError& e) {
     g_create_error = std::string(e.what) + ": " + cudaGetErrorString(e.e);
     return CAROLI_ECUDA;
@@ -1573,6 +1594,8 @@ int caroli_ctx_create(int device_ordinal, caroli_ctx** out) {
 
 void caroli_ctx_destroy(caroli_ctx* ctx) {
   if (!ctx) return;
+  // Waits for a call of another thread still inside the context (none may start after this).
+  { std::lock_guard<std::recursive_mutex> wait(ctx->mu); }
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   ctx->systems.clear();
@@ -1597,6 +1620,7 @@ int caroli_plan_upload(caroli_ctx* ctx, int64_t n, const int64_t* row_ptr, const
                        const int64_t* range, int64_t n_interior, const int64_t* interior, int nblocks,
                        const int32_t* labels, const int64_t* left_ptr, const int64_t* left,
                        const int64_t* right_ptr, const int64_t* right, int* plan_id) {
+  CTX_LOCK(ctx);
   if (!ctx || !plan_id || n < 0 || !row_ptr || (n > 0 && !cols) || dim < 1 || dim > 3 || nblocks < 0)
     return fail_with(ctx, CAROLI_EINVAL, "caroli_plan_upload: bad arguments");
   try {
@@ -1673,6 +1697,7 @@ int caroli_plan_upload(caroli_ctx* ctx, int64_t n, const int64_t* row_ptr, const
 
 int caroli_plan_info(caroli_ctx* ctx, int plan_id, int block, int64_t* fronts, int64_t* max_n, int64_t* max_ne,
                      int64_t* root_n, int64_t* arena_elems) {
+  CTX_LOCK(ctx);
   System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
   if (!sys) return fail_with(ctx, CAROLI_EINVAL, "unknown plan");
   if (block < 0 || block >= (int)sys->plans.size()) {
@@ -1690,6 +1715,7 @@ int caroli_plan_info(caroli_ctx* ctx, int plan_id, int block, int64_t* fronts, i
 
 int caroli_plan_fronts(caroli_ctx* ctx, int plan_id, int block, int64_t capacity, int32_t* n, int32_t* ne,
                        int32_t* level, int64_t* count) {
+  CTX_LOCK(ctx);
   System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
   if (!sys || block < 0 || block >= (int)sys->plans.size()) return fail_with(ctx, CAROLI_EINVAL, "unknown plan or block");
   const auto& fr = sys->plans[block]->host.fronts;
@@ -1704,6 +1730,7 @@ int caroli_plan_fronts(caroli_ctx* ctx, int plan_id, int block, int64_t capacity
 }
 
 int caroli_values_upload(caroli_ctx* ctx, int plan_id, int nconfigs, const double* values) {
+  CTX_LOCK(ctx);
   System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
   if (!sys || nconfigs <= 0 || !values) return fail_with(ctx, CAROLI_EINVAL, "caroli_values_upload: bad arguments");
   try {
@@ -1728,6 +1755,7 @@ int caroli_values_upload(caroli_ctx* ctx, int plan_id, int nconfigs, const doubl
 
 int caroli_values_generate(caroli_ctx* ctx, int plan_id, const double* clean_values, int nentries,
                            const caroli_disorder* entries, int nconfigs, int first_config) {
+  CTX_LOCK(ctx);
   System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
   if (!sys || !clean_values || nentries < 0 || (nentries > 0 && !entries) || nconfigs <= 0 || first_config < 0)
     return fail_with(ctx, CAROLI_EINVAL, "caroli_values_generate: bad arguments");
@@ -1853,6 +1881,7 @@ int caroli_values_generate(caroli_ctx* ctx, int plan_id, const double* clean_val
 }
 
 int caroli_values_download(caroli_ctx* ctx, int plan_id, int config, double* values) {
+  CTX_LOCK(ctx);
   System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
   if (!sys || !values || !sys->vals || config < 0 || config >= sys->nconfigs)
     return fail_with(ctx, CAROLI_EINVAL, "caroli_values_download: bad arguments");
@@ -1870,6 +1899,7 @@ int caroli_values_download(caroli_ctx* ctx, int plan_id, int config, double* val
 }
 
 int caroli_derivs_upload(caroli_ctx* ctx, int plan_id, int nparams, const double* values) {
+  CTX_LOCK(ctx);
   System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
   if (!sys || nparams < 0 || (nparams > 0 && !values) || sys->nconfigs <= 0)
     return fail_with(ctx, CAROLI_EINVAL, "caroli_derivs_upload: bad arguments (upload the values first)");
@@ -1889,6 +1919,7 @@ int caroli_derivs_upload(caroli_ctx* ctx, int plan_id, int nparams, const double
 
 int caroli_transmission_with_grad(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots,
                                   const int32_t* configs, double* t, int32_t* status, double* dt_dv, double* dt_dp) {
+  CTX_LOCK(ctx);
   System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
   if (!sys || count < 0 || (count > 0 && (!slots || !configs || !t || !status || !dt_dv)))
     return fail_with(ctx, CAROLI_EINVAL, "caroli_transmission_with_grad: bad arguments");
@@ -1947,6 +1978,7 @@ int caroli_scattering_states(caroli_ctx* ctx, int plan_id, int count, const int3
                              const double* const* w_left, const int32_t* left_channels, const double* const* w_right,
                              const int32_t* right_channels, double* const* psi_left, double* const* psi_right,
                              int32_t* status) {
+  CTX_LOCK(ctx);
   System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
   if (!sys || count < 0 ||
       (count > 0 && (!slots || !configs || !w_left || !left_channels || !w_right || !right_channels || !psi_left ||
@@ -2058,7 +2090,7 @@ namespace {
 
 // Multi-terminal T_pq in mixed precision: X = A^-1 [W_1 ... W_P] (every lead's sources,
 // W_p W_p^† = Γ_p) refined in FP64 from the f32 factors, then T_pq = Σ over lead q's columns of
-// x^†(p) Γ_p x(p). Block solves with more than MIXED_MAX_CHANNELS sources, and those the
+// x^†(p) Γ_p x(p). Block solves with more than ctx->mixed_max_channels sources, and those the
 // refinement cannot resolve, take the FP64 path.
 void multi_mixed(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, std::vector<JobOut>& out) {
   cudaStream_t s = ctx->stream;
@@ -2069,7 +2101,7 @@ void multi_mixed(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs
     const SigmaSlot& sg = sys->slots[specs[j].slot];
     int c = 0;
     for (int p = 0; p < P; ++p) c += sg.mch[(size_t)specs[j].block * P + p];
-    (c > MIXED_MAX_CHANNELS ? many : few).push_back(j);
+    (c > ctx->mixed_max_channels ? many : few).push_back(j);
   }
   std::vector<size_t> again = many;
   if (!few.empty()) {
@@ -2153,6 +2185,7 @@ void multi_mixed(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs
 extern "C" {
 
 int caroli_multi_leads(caroli_ctx* ctx, int plan_id, int nleads, const int64_t* lead_ptr, const int64_t* lead_orbitals) {
+  CTX_LOCK(ctx);
   System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
   if (!sys || nleads <= 0 || !lead_ptr || !lead_orbitals)
     return fail_with(ctx, CAROLI_EINVAL, "caroli_multi_leads: bad arguments");
@@ -2203,6 +2236,7 @@ int caroli_multi_leads(caroli_ctx* ctx, int plan_id, int nleads, const int64_t* 
 }
 
 int caroli_multi_sigma_upload(caroli_ctx* ctx, int plan_id, int slot, double energy, const double* const* sigma) {
+  CTX_LOCK(ctx);
   System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
   if (!sys || slot < 0 || !sigma) return fail_with(ctx, CAROLI_EINVAL, "caroli_multi_sigma_upload: bad arguments");
   if (sys->nleads <= 0) return fail_with(ctx, CAROLI_EINVAL, "caroli_multi_sigma_upload: no leads (caroli_multi_leads)");
@@ -2290,6 +2324,7 @@ int caroli_multi_sigma_upload(caroli_ctx* ctx, int plan_id, int slot, double ene
 
 int caroli_multi_transmissions(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots, const int32_t* configs,
                                int precision, double* t, int32_t* status) {
+  CTX_LOCK(ctx);
   System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
   if (!sys || count < 0 || (count > 0 && (!slots || !configs || !t || !status)))
     return fail_with(ctx, CAROLI_EINVAL, "caroli_multi_transmissions: bad arguments");
@@ -2372,6 +2407,7 @@ extern "C" {
 
 int caroli_root_green(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots, const int32_t* configs,
                       double* const* g, int32_t* kept, int32_t* status) {
+  CTX_LOCK(ctx);
   System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
   if (!sys || count < 0 || (count > 0 && (!slots || !configs || !g || !kept || !status)))
     return fail_with(ctx, CAROLI_EINVAL, "caroli_root_green: bad arguments");
@@ -2432,6 +2468,7 @@ int caroli_root_green(caroli_ctx* ctx, int plan_id, int count, const int32_t* sl
 int caroli_transmission_matrix(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots, const int32_t* configs,
                                const double* const* w_left, const int32_t* left_channels, double* const* t,
                                int32_t* right_channels, int32_t* status) {
+  CTX_LOCK(ctx);
   System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
   if (!sys || count < 0 ||
       (count > 0 && (!slots || !configs || !w_left || !left_channels || !t || !right_channels || !status)))
@@ -2512,6 +2549,7 @@ int caroli_transmission_matrix(caroli_ctx* ctx, int plan_id, int count, const in
 int caroli_multi_sector_transmissions(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots,
                                       const int32_t* configs, int precision, int nlabels, const int32_t* label_lead,
                                       const double* const* gammas, double* t, int32_t* status) {
+  CTX_LOCK(ctx);
   System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
   if (!sys || count < 0 || nlabels <= 0 || !label_lead ||
       (count > 0 && (!slots || !configs || !gammas || !t || !status)))
@@ -2632,6 +2670,7 @@ int caroli_multi_sector_transmissions(caroli_ctx* ctx, int plan_id, int count, c
 int caroli_multi_scattering_states(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots,
                                    const int32_t* configs, const double* const* w, const int32_t* channels,
                                    double* const* psi, int32_t* status) {
+  CTX_LOCK(ctx);
   System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
   if (!sys || count < 0 || (count > 0 && (!slots || !configs || !w || !channels || !psi || !status)))
     return fail_with(ctx, CAROLI_EINVAL, "caroli_multi_scattering_states: bad arguments");
@@ -2755,6 +2794,7 @@ int caroli_multi_scattering_states(caroli_ctx* ctx, int plan_id, int count, cons
 
 int caroli_gamma_override(caroli_ctx* ctx, int plan_id, int slot, const double* const* gamma_l,
                           const double* const* gamma_r) {
+  CTX_LOCK(ctx);
   System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
   if (!sys || slot < 0 || slot >= (int)sys->slots.size() || !sys->slots[slot].set || !gamma_l || !gamma_r)
     return fail_with(ctx, CAROLI_EINVAL, "caroli_gamma_override: bad arguments");
@@ -2776,6 +2816,7 @@ int caroli_gamma_override(caroli_ctx* ctx, int plan_id, int slot, const double* 
 }
 
 int caroli_lead_modes(caroli_ctx* ctx, int plan_id, int block, int side, int n, const double* y, double sc) {
+  CTX_LOCK(ctx);
   System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
   if (!sys || block < 0 || block >= (int)sys->plans.size() || (side != 0 && side != 1) || !y)
     return fail_with(ctx, CAROLI_EINVAL, "caroli_lead_modes: bad arguments");
@@ -2803,6 +2844,7 @@ int caroli_lead_modes(caroli_ctx* ctx, int plan_id, int block, int side, int n, 
 int caroli_sigma_from_modes(caroli_ctx* ctx, int plan_id, int slot, double energy, const double* const* d_left,
                             const double* const* d_right, const int32_t* channels, const int32_t* const* channel_modes,
                             const double* const* channel_weights) {
+  CTX_LOCK(ctx);
   System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
   if (!sys || slot < 0 || !d_left || !d_right || !channels || !channel_modes || !channel_weights)
     return fail_with(ctx, CAROLI_EINVAL, "caroli_sigma_from_modes: bad arguments");
@@ -2865,6 +2907,7 @@ int caroli_sigma_from_modes(caroli_ctx* ctx, int plan_id, int slot, double energ
 
 int caroli_sigma_upload(caroli_ctx* ctx, int plan_id, int slot, double energy, const double* const* sigma_l,
                         const double* const* sigma_r, const double* const* w_right, const int32_t* channels) {
+  CTX_LOCK(ctx);
   System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
   if (!sys || slot < 0 || !sigma_l || !sigma_r) return fail_with(ctx, CAROLI_EINVAL, "caroli_sigma_upload: bad arguments");
   try {
@@ -2999,6 +3042,7 @@ extern "C" {
 
 int caroli_solve_batch(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots, const int32_t* configs,
                        int precision, double* t, int32_t* status, double* err) {
+  CTX_LOCK(ctx);
   System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
   if (!sys) return fail_with(ctx, CAROLI_EINVAL, "caroli_solve_batch: bad arguments");
   std::vector<System*> isys(std::max(count, 0), sys);
@@ -3007,6 +3051,7 @@ int caroli_solve_batch(caroli_ctx* ctx, int plan_id, int count, const int32_t* s
 
 int caroli_solve_multi(caroli_ctx* ctx, int count, const int32_t* plan_ids, const int32_t* slots,
                        const int32_t* configs, int precision, double* t, int32_t* status, double* err) {
+  CTX_LOCK(ctx);
   if (!ctx || count < 0 || (count > 0 && !plan_ids)) return fail_with(ctx, CAROLI_EINVAL, "caroli_solve_multi: bad arguments");
   std::vector<System*> isys(count);
   for (int i = 0; i < count; ++i) isys[i] = get_system(ctx, plan_ids[i]);
@@ -3014,6 +3059,7 @@ int caroli_solve_multi(caroli_ctx* ctx, int count, const int32_t* plan_ids, cons
 }
 
 int caroli_last_phases(const caroli_ctx* ctx, double* factor_ms, double* root_ms, double* tail_ms) {
+  CTX_LOCK(ctx);
   if (!ctx) return CAROLI_EINVAL;
   if (factor_ms) *factor_ms = ctx->factor_ms;
   if (root_ms) *root_ms = ctx->root_ms;
@@ -3022,6 +3068,7 @@ int caroli_last_phases(const caroli_ctx* ctx, double* factor_ms, double* root_ms
 }
 
 int caroli_last_job_steps(const caroli_ctx* ctx, int64_t capacity, int32_t* steps, int64_t* count) {
+  CTX_LOCK(ctx);
   if (!ctx || !count) return CAROLI_EINVAL;
   const int64_t n = (int64_t)ctx->job_steps.size();
   for (int64_t j = 0; j < n && j < capacity; ++j)
@@ -3032,6 +3079,7 @@ int caroli_last_job_steps(const caroli_ctx* ctx, int64_t capacity, int32_t* step
 
 int caroli_last_job_info(const caroli_ctx* ctx, int64_t capacity, int32_t* iters, int32_t* perturbed,
                          int32_t* status, int64_t* count) {
+  CTX_LOCK(ctx);
   if (!ctx) return CAROLI_EINVAL;
   const int64_t n = (int64_t)ctx->job_iters.size();
   if (count) *count = n;
@@ -3044,6 +3092,7 @@ int caroli_last_job_info(const caroli_ctx* ctx, int64_t capacity, int32_t* iters
 }
 
 int caroli_last_stats(const caroli_ctx* ctx, int64_t* fallbacks, int64_t* max_refine_iters) {
+  CTX_LOCK(ctx);
   if (!ctx) return CAROLI_EINVAL;
   if (fallbacks) *fallbacks = ctx->fallbacks;
   if (max_refine_iters) *max_refine_iters = ctx->refine_iters;
@@ -3051,6 +3100,7 @@ int caroli_last_stats(const caroli_ctx* ctx, int64_t* fallbacks, int64_t* max_re
 }
 
 int caroli_last_refine_steps(const caroli_ctx* ctx, int64_t* job_steps, int64_t* batch_steps) {
+  CTX_LOCK(ctx);
   if (!ctx) return CAROLI_EINVAL;
   if (job_steps) *job_steps = ctx->refine_job_steps;
   if (batch_steps) *batch_steps = ctx->refine_batch_steps;
@@ -3058,6 +3108,7 @@ int caroli_last_refine_steps(const caroli_ctx* ctx, int64_t* job_steps, int64_t*
 }
 
 int caroli_set_refine_options(caroli_ctx* ctx, int max_iters, double tol, double inner_tol) {
+  CTX_LOCK(ctx);
   if (!ctx) return CAROLI_EINVAL;
   if (max_iters < 1 || max_iters > 64 || !(tol > 0.0 && tol < 1.0) || !(inner_tol > 0.0 && inner_tol < 1.0))
     return fail_with(ctx, CAROLI_EINVAL, "refinement options out of range (1 <= max_iters <= 64, 0 < tol < 1)");
@@ -3068,8 +3119,24 @@ int caroli_set_refine_options(caroli_ctx* ctx, int max_iters, double tol, double
 }
 
 int caroli_set_tensor_cores(caroli_ctx* ctx, int enable) {
+  CTX_LOCK(ctx);
   if (!ctx) return CAROLI_EINVAL;
   ctx->tensor_cores = enable != 0;
+  return CAROLI_OK;
+}
+
+int caroli_set_mixed_max_channels(caroli_ctx* ctx, int channels) {
+  CTX_LOCK(ctx);
+  if (!ctx) return CAROLI_EINVAL;
+  if (channels < 0) return fail_with(ctx, CAROLI_EINVAL, "caroli_set_mixed_max_channels: negative channel count");
+  ctx->mixed_max_channels = channels;
+  return CAROLI_OK;
+}
+
+int caroli_set_wait_limit(caroli_ctx* ctx, int64_t polls) {
+  CTX_LOCK(ctx);
+  if (!ctx) return CAROLI_EINVAL;
+  ctx->tc_wait_limit = polls < 0 ? TCU_WAIT : (uint32_t)std::min<int64_t>(polls, TCU_WAIT);
   return CAROLI_OK;
 }
 
@@ -3078,6 +3145,7 @@ int caroli_kernel_classes(void) { return K_COUNT; }
 const char* caroli_kernel_class_name(int k) { return (k >= 0 && k < K_COUNT) ? kclass_names[k] : ""; }
 
 int caroli_probe_kernel(caroli_ctx* ctx, int kclass) {
+  CTX_LOCK(ctx);
   if (!ctx || kclass < -1 || kclass >= K_COUNT) return CAROLI_EINVAL;
   ctx->probe = kclass;
   return CAROLI_OK;
@@ -3085,6 +3153,7 @@ int caroli_probe_kernel(caroli_ctx* ctx, int kclass) {
 
 int caroli_kernel_stats(caroli_ctx* ctx, int kclass, int64_t* launches, double* flops, double* bytes, double* ms,
                         int reset) {
+  CTX_LOCK(ctx);
   if (!ctx || kclass < 0 || kclass >= K_COUNT) return CAROLI_EINVAL;
   KStat& st = ctx->kstat[kclass];
   if (launches) *launches = st.launches;
@@ -3096,6 +3165,7 @@ int caroli_kernel_stats(caroli_ctx* ctx, int kclass, int64_t* launches, double* 
 }
 
 int caroli_region_begin(caroli_ctx* ctx) {
+  CTX_LOCK(ctx);
   if (!ctx) return CAROLI_EINVAL;
   cudaSetDevice(ctx->device);
   ctx->region_launches = 0;
@@ -3103,6 +3173,7 @@ int caroli_region_begin(caroli_ctx* ctx) {
 }
 
 int caroli_region_end(caroli_ctx* ctx, double* device_ms, int64_t* launches) {
+  CTX_LOCK(ctx);
   if (!ctx) return CAROLI_EINVAL;
   cudaSetDevice(ctx->device);
   if (cudaEventRecord(ctx->reg1, ctx->stream) != cudaSuccess || cudaEventSynchronize(ctx->reg1) != cudaSuccess)
@@ -3115,6 +3186,7 @@ int caroli_region_end(caroli_ctx* ctx, double* device_ms, int64_t* launches) {
 }
 
 int caroli_last_timing(const caroli_ctx* ctx, double* device_ms, int64_t* launches) {
+  CTX_LOCK(ctx);
   if (!ctx) return CAROLI_EINVAL;
   if (device_ms) *device_ms = ctx->last_ms;
   if (launches) *launches = ctx->last_launches;
@@ -3135,22 +3207,19 @@ namespace {
 constexpr size_t NOALLOC_BYTES = size_t(64) << 20;  // 64 MiB
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
 
-constexpr int NOALLOC_MAX_DEVICES = 64;
-unsigned char* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
+}  // namespace
 
-// The device address of the scratch array on `device` (which must be current). Host code cannot
-// use the symbol itself: its name stands for a host-side shadow, not device memory.
-cudaError_t noalloc_scratch(int device, unsigned char** out) {
-  if (device < 0 || device >= NOALLOC_MAX_DEVICES) return cudaErrorInvalidDevice;
-  if (!g_noalloc_ptr[device]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return e;
-    g_noalloc_ptr[device] = static_cast<unsigned char*>(p);
-  }
-  *out = g_noalloc_ptr[device];
-  return cudaSuccess;
+// The device address of the scratch array on the current device, looked up once per context by
+// caroli_ctx_create (with the context's device current). Host code cannot use the symbol itself:
+// its name stands for a host-side shadow, not device memory.
+cudaError_t noalloc_lookup(unsigned char** out) {
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e == cudaSuccess) *out = static_cast<unsigned char*>(p);
+  return e;
 }
+
+namespace {
 
 // Bump allocation inside the scratch array (256-byte aligned pieces).
 struct Carve {
@@ -3167,6 +3236,7 @@ struct Carve {
 
 extern "C" int caroli_solve_batch_noalloc(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots,
                                           const int32_t* configs, double* t, int32_t* status) {
+  CTX_LOCK(ctx);
   System* sys = ctx ? get_system(ctx, plan_id) : nullptr;
   if (!sys || count < 0 || (count > 0 && (!slots || !configs || !t || !status)))
     return fail_with(ctx, CAROLI_EINVAL, "caroli_solve_batch_noalloc: bad arguments");
@@ -3180,8 +3250,8 @@ extern "C" int caroli_solve_batch_noalloc(caroli_ctx* ctx, int plan_id, int coun
   if (count == 0) return CAROLI_OK;
   try {
     CK(cudaSetDevice(ctx->device));
-    unsigned char* base = nullptr;
-    CK(noalloc_scratch(ctx->device, &base));
+    unsigned char* base = ctx->noalloc_base;
+    if (!base) return fail_with(ctx, CAROLI_ECUDA, "caroli_solve_batch_noalloc: the scratch array has no device address");
     cudaStream_t s = ctx->stream;
     const int nb = (int)sys->plans.size();
     const size_t nj = (size_t)count * nb;

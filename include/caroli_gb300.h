@@ -2,8 +2,10 @@
  *
  * This is the boundary a caroli caller binds: plain pointers and sizes, an int status on every
  * call, no exceptions across the ABI. The caller owns its host buffers; the library owns the
- * device memory. One CUDA stream per context; a context is not safe to share between threads
- * without external locking.
+ * device memory. One CUDA stream per context. Thread-safe per context: every call taking a context
+ * holds the context's lock for its whole duration, so threads sharing a context are serialised
+ * (caroli_ctx_destroy waits for a call in progress; none may start after it). Contexts are
+ * independent of each other.
  *
  * Reference interfaces each entry point replaces (caroli, crates/caroli-green/src/nested.rs):
  *   caroli_ctx_create / caroli_ctx_destroy   the "cuda" feature's device handle, CudaDevice::new
@@ -48,11 +50,14 @@ typedef struct caroli_ctx caroli_ctx;
 /* Status codes: return values of every call, and per-solve statuses of caroli_solve_batch. */
 enum {
   CAROLI_OK = 0,
-  CAROLI_PIVOT_DELAYED = 1,   /* internal: a front refused its pivots (resolved by re-planning) */
+  CAROLI_PIVOT_DELAYED = 1,   /* a front refused its pivots: caroli_solve_batch re-plans such solves
+                                 with the front delayed (never returned there);
+                                 caroli_solve_batch_noalloc returns it for the instance (re-solve it
+                                 with caroli_solve_batch) */
   CAROLI_SINGULAR = 2,        /* GreenError::Singular: the root solve is singular or not finite */
   CAROLI_NONFINITE = 3,       /* T is not finite */
   CAROLI_REFINE_STALLED = 4,  /* mixed precision: refinement did not reach its tolerance */
-  CAROLI_TIMEOUT = 5,
+  CAROLI_TIMEOUT = 5,         /* a bounded device wait ran out (caroli_set_wait_limit) */
   CAROLI_EINVAL = 16,         /* bad argument (message in caroli_last_error) */
   CAROLI_ENOMEM = 17,         /* device allocation failed */
   CAROLI_ECUDA = 18,          /* CUDA error (message in caroli_last_error) */
@@ -65,8 +70,8 @@ enum {
   CAROLI_SINGLE = 1, /* complex f32 fronts, f64 root and trace, unrefined (Precision::Single) */
   CAROLI_MIXED = 2   /* complex f32 fronts as a preconditioner of FP64 iterative refinement of the
                         whole solve (no counterpart; Precision gains a Mixed variant). Block solves
-                        whose right lead has more than 96 open channels (one refinement right-hand
-                        side each) take the FP64 path instead, which is faster there. */
+                        whose right lead has more than caroli_set_mixed_max_channels open
+                        channels (one refinement right-hand side each) take the FP64 path. */
 };
 
 int caroli_ctx_create(int device_ordinal, caroli_ctx** out);
@@ -188,10 +193,11 @@ int caroli_solve_batch(caroli_ctx* ctx, int plan_id, int count, const int32_t* s
  * static device array of 64 MiB that each GPU loading this library keeps until the process exits;
  * a batch needing more is rejected with CAROLI_EINVAL and the size in caroli_last_error (solve
  * fewer instances per call). The system, its values and self-energies must have been uploaded
- * (those calls allocate). The first call on a device looks the array up on that device; make it
- * before any stream capture. Calls share the array and run on the context's stream: calls that
- * overlap on the GPU (other contexts or threads) race. Fronts that refuse their pivots are not
- * re-planned here: those instances get CAROLI_PIVOT_DELAYED (use caroli_solve_batch for them). */
+ * (those calls allocate). caroli_ctx_create looks the array's device address up once, with the
+ * context's device current, so a call here makes only kernel launches and copies. Calls share the
+ * array and run on the context's stream: calls that overlap on the GPU (other contexts, whose
+ * streams are not ordered with this one) race. Fronts that refuse their pivots are not re-planned
+ * here: those instances get CAROLI_PIVOT_DELAYED (use caroli_solve_batch for them). */
 int caroli_solve_batch_noalloc(caroli_ctx* ctx, int plan_id, int count, const int32_t* slots, const int32_t* configs,
                                double* t, int32_t* status);
 
@@ -324,12 +330,12 @@ int caroli_last_timing(const caroli_ctx* ctx, double* device_ms, int64_t* launch
  * number of refinement iterations a solve took. */
 int caroli_last_stats(const caroli_ctx* ctx, int64_t* fallbacks, int64_t* max_refine_iters);
 
-/* Per block solve of the last caroli_solve_batch (instance-major, blocks fastest; up to
- * `capacity` entries, *count = all): refinement iterations, pivots perturbed by static pivoting,
- * and status (100 + s: status s in reduced precision, then recomputed in double precision). */
 /* Per block solve of the last caroli_solve_batch (as caroli_last_job_info): GMRES (Arnoldi) steps
  * of the mixed refinement, summed over its outer iterations (0 outside CAROLI_MIXED). */
 int caroli_last_job_steps(const caroli_ctx* ctx, int64_t capacity, int32_t* steps, int64_t* count);
+/* Per block solve of the last caroli_solve_batch (instance-major, blocks fastest; up to
+ * `capacity` entries, *count = all): refinement iterations, pivots perturbed by static pivoting,
+ * and status (100 + s: status s in reduced precision, then recomputed in double precision). */
 int caroli_last_job_info(const caroli_ctx* ctx, int64_t capacity, int32_t* iters, int32_t* perturbed,
                          int32_t* status, int64_t* count);
 
@@ -348,6 +354,18 @@ int caroli_set_refine_options(caroli_ctx* ctx, int max_iters, double tol, double
 /* Rank-32 Schur updates of f32 fronts (CAROLI_MIXED, CAROLI_SINGLE) on the tcgen05 tensor cores
  * (3xTF32, default 1) or on the CUDA cores (0). No reference counterpart. */
 int caroli_set_tensor_cores(caroli_ctx* ctx, int enable);
+
+/* CAROLI_MIXED block solves whose sources (the right lead's open channels; every lead's for a
+ * multi-terminal block) number more than `channels` take the FP64 path (default 96). No reference
+ * counterpart. */
+int caroli_set_mixed_max_channels(caroli_ctx* ctx, int channels);
+
+/* Polls a pipeline wait of the tensor-core update may make before it gives up (default and
+ * maximum 1 << 22; a negative value restores the default). A wait that runs out marks its solve
+ * CAROLI_TIMEOUT (CAROLI_MIXED then recomputes it in FP64: status 105 in caroli_last_job_info)
+ * after the copies and products already issued have drained; the context stays usable. Meant for
+ * testing that path. No reference counterpart. */
+int caroli_set_wait_limit(caroli_ctx* ctx, int64_t polls);
 
 /* Device time of the last caroli_solve_batch split into the tree factorization, the root
  * inverse, and the rest (trace, or refinement and double-precision recomputations), in ms. */

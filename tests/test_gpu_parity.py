@@ -119,6 +119,32 @@ def test_magnetic_200x64_double_and_mixed_match_oracle():
     assert np.abs(tm - ref).max() <= 1e-8, np.abs(tm - ref)
 
 
+def test_magnetic_200x64_mixed_across_the_band():
+    """The headline workload's mixed path against the oracle over the band: eight energies of the
+    bench's 33-point grid in [-0.16, 0.16] (both ends, the gap edges and mid-gap) x the eight
+    configurations (128 block solves), every point within 1e-8 and none recomputed in FP64."""
+    from oracle import Oracle
+
+    sys_ = magnetic_bhz(200, 64, configs=8)
+    energies = [-0.16, -0.13, -0.08, -0.03, 0.0, 0.06, 0.12, 0.16]
+    sigmas = [sys_.self_energies(e) for e in energies]
+    pairs = [(s, c) for s in sigmas for c in range(8)]
+    tm, stm, _ = sys_.solve_batch([p[0] for p in pairs], [p[1] for p in pairs], Precision.MIXED)
+    assert (stm == 0).all(), stm
+    fallbacks, _ = sys_.plan().last_stats()
+    assert fallbacks == 0
+    orc = Oracle(sys_.system)
+    nb = sys_.block_count()
+    ref, st = orc.solve_batch([b for _ in pairs for b in range(nb)], [s.energy for s, _ in pairs for _ in range(nb)],
+                              [sys_.system.values[c] for _, c in pairs for _ in range(nb)],
+                              [s.blocks[b][0] for s, _ in pairs for b in range(nb)],
+                              [s.blocks[b][1] for s, _ in pairs for b in range(nb)], threads=0)
+    assert (st == 0).all()
+    ref = ref.reshape(len(pairs), nb).sum(axis=1)
+    dT = np.abs(tm - ref)
+    assert dT.max() <= 1e-8, (dT.max(), pairs[int(dT.argmax())][0].energy)
+
+
 def test_tensor_core_updates_match_cuda_cores():
     """The f32 rank-32 updates on tcgen05 (3xTF32) against the same updates on the CUDA cores:
     unrefined single-precision T is as close to the oracle either way (f32 rounding differs, and
