@@ -66,3 +66,28 @@ def test_lead_voltages_four_terminal():
     # I_p = Σ_q (T_qp V_p - T_pq V_q) reproduces the imposed currents.
     cur = [sum(T[q][p] * v[p] - T[p][q] * v[q] for q in range(4)) for p in range(4)]
     assert np.allclose(cur, [1.0, -1.0, 0.0, 0.0], atol=1e-12)
+
+
+@pytest.mark.parametrize("width", [4, 10, 16])
+def test_reduced_pencil_equals_full_pencil(width):
+    """Graphene's rank-deficient coupling: the reduced 2r pencil gives the self-energies of the 2n
+    QZ path (narrow ribbons, where the QZ path's eigenvectors are well conditioned)."""
+    ls = _lead(graphene(), width)
+    assert ls.uv is not None and ls.uv[0].shape[1] < ls.n
+    for e in (-2.1, -0.4, 0.1, 0.45, 1.3):
+        sl1, sr1 = ls._general(e)
+        sl2, sr2 = ls._reduced(e)
+        assert np.abs(sl1 - sl2).max() < 1e-11 and np.abs(sr1 - sr2).max() < 1e-11, e
+
+
+@pytest.mark.parametrize("width", [24, 40, 100])
+def test_reduced_pencil_solves_the_dyson_equation(width):
+    """Σ_R = h01 (E - h00 - Σ_R)^-1 h01^† and Σ_L = h01^† (E - h00 - Σ_L)^-1 h01 to 1e-11, where the
+    edge states make the evanescent eigenvectors nearly parallel (Schur bases)."""
+    ls = _lead(graphene(), width)
+    eye = np.eye(ls.n)
+    for e in (-0.4, 0.1, 0.45):
+        sl, sr = ls._reduced(e)
+        rr = sr - ls.h01 @ np.linalg.solve(e * eye - ls.h00 - sr, ls.h01.conj().T)
+        rl = sl - ls.h01.conj().T @ np.linalg.solve(e * eye - ls.h00 - sl, ls.h01)
+        assert max(np.abs(rr).max(), np.abs(rl).max()) < 1e-11, e

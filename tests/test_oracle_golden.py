@@ -52,3 +52,15 @@ def test_bench_w64_matches_published(problem):
         e = gold["energies"][k]
         t = oracle_T(sys_, sys_.self_energies(e))
         assert abs(t - np.median(runs[:, k])) < 1e-8 * (1 + abs(t))
+
+
+def test_graphene_w64_matches_published():
+    """Graphene zigzag leads (rank-deficient coupling: the reduced 2r pencil with Schur bases of the
+    edge states) at W = 64: the published transmissions to 1e-10."""
+    gold = bench_golden()["caroli/graphene-anderson/64"]
+    dev, lead, region = bench_problem("graphene-anderson", 64)
+    sys_ = NestedTwoTerminal.from_model(dev, lead, region, 0)
+    runs = np.array(gold["runs"])
+    for k, e in enumerate(gold["energies"]):
+        t = oracle_T(sys_, sys_.self_energies(e))
+        assert abs(t - np.median(runs[:, k])) < 1e-10 * (1 + abs(t)), (e, t, runs[:, k])
