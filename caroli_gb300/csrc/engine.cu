@@ -227,7 +227,7 @@ struct SectorRequest {
 
 // Device state of one refinement (forward, or the adjoint of the gradient).
 struct RefineBufs {
-  Buf rdesc, rx, rr, rd, rtb, rhb, rt, rerr, rdone;
+  Buf rdesc, rx, rr, rd, rtb, rhb, rt, rerr, rdone, rgx, stasks;
   Buf gV, gZ, gH, gg, gcs, gsn, gy, gbeta, gcol, gflags;
   Buf segs, ctasks, ccount, cjobs;  // task lists compacted to the solves still iterating
 };
@@ -421,7 +421,7 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
       const double ne = P.fronts[k].ne, n = P.fronts[k].n;
       sweep_bytes += (ne * ne + 2 * ne * (n - ne)) * sizeof(float2);  // factors read per sweep pair
     }
-    resid_flops += 8.0 * c * ((double)B.nnz + (double)P.nl * P.nl + (double)P.nr * P.nr);
+    resid_flops += 8.0 * c * (double)B.nnz;  // the slices' dense Σ blocks: slice_products
   }
   double2* rx = static_cast<double2*>(rb.rx.get(std::max<size_t>(xo, 1) * sizeof(double2)));
   double2* rr = static_cast<double2*>(rb.rr.get(std::max<size_t>(xo, 1) * sizeof(double2)));
@@ -444,6 +444,14 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
   double* gbeta = static_cast<double*>(rb.gbeta.get(std::max<size_t>(co, 1) * sizeof(double)));
   int32_t* gcol = static_cast<int32_t*>(rb.gcol.get(std::max<size_t>(co, 1) * sizeof(int32_t)));
   int32_t* gflags = static_cast<int32_t*>(rb.gflags.get(cj * sizeof(int32_t)));
+  std::vector<size_t> gxoffs(cj);
+  size_t gxo = 0;
+  for (size_t j = 0; j < cj; ++j) {
+    const size_t cj_cols = (j + 1 < cj ? coffs[j + 1] : co) - coffs[j];
+    gxoffs[j] = gxo;
+    gxo += (size_t)specs[begin + j].plan->host.nl * cj_cols;
+  }
+  double2* rgx = static_cast<double2*>(rb.rgx.get(std::max<size_t>(gxo, 1) * sizeof(double2)));
   for (size_t j = 0; j < cj; ++j) {
     const JobSpec& sp = specs[begin + j];
     const DevPlan& P = *sp.plan;
@@ -487,10 +495,60 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
       R.c = R.cl + states->cr[begin + j];
       R.whole = 1;
     }
+    R.gx = rgx + gxoffs[j];
     R.done = R.c == 0 ? 1 : 0;  // no channel: T = 0
   }
   RefineDesc* drd = static_cast<RefineDesc*>(rb.rdesc.get(cj * sizeof(RefineDesc)));
   CK(cudaMemcpyAsync(drd, rdh.data(), cj * sizeof(RefineDesc), cudaMemcpyHostToDevice, s));
+  // Dense slice products (Σ_L, Σ_R of A and Γ_L of the trace): one task per job and product,
+  // built once. Matvec of step k: V_{k+1} -= Σ Z_k; residual: r += Σ x; check: gx = Γ_L x_L.
+  // Left and right slices run as separate launches (they may share rows).
+  const int nsides = 2;
+  const size_t per_set = cj;  // tasks of one (product, side) set
+  const size_t set_mv = 0, set_res = (size_t)GM_M * nsides, set_gam = set_res + nsides;
+  const size_t nsets = set_gam + 1;
+  std::vector<SliceTask> sth(nsets * per_set);
+  int slice_m = 1;
+  for (size_t j = 0; j < cj; ++j) {
+    const RefineDesc& R = rdh[j];
+    const RefineDesc* dR = drd + j;
+    for (int side = 0; side < nsides; ++side) {
+      const double2* sg = side == 0 ? R.sigma_l : R.sigma_r;
+      const int m = side == 0 ? R.nl : R.nr;
+      const int32_t* rows = side == 0 ? R.left_local : R.right_local;
+      slice_m = std::max(slice_m, m);
+      SliceTask base{};
+      base.rd = dR; base.s = sg; base.irow = rows; base.orow = rows; base.ldi = base.ldo = R.nblk;
+      base.m = (sg && m > 0) ? m : 0; base.c = R.c; base.adj = R.adjoint; base.accumulate = 1;
+      for (int k = 0; k < GM_M; ++k) {
+        SliceTask t = base;
+        t.in = R.Z + (size_t)k * R.nblk * R.c; t.in_f32 = 1; t.out = R.V + (size_t)(k + 1) * R.nblk * R.c;
+        t.mode = 0; t.sign = -1.0;
+        sth[(set_mv + (size_t)k * nsides + side) * per_set + j] = t;
+      }
+      SliceTask t = base;
+      t.in = R.x; t.in_f32 = 0; t.out = R.r; t.mode = 1; t.sign = 1.0;
+      sth[(set_res + side) * per_set + j] = t;
+    }
+    SliceTask t{};
+    t.rd = dR; t.s = R.gamma_l; t.irow = R.left_local; t.orow = nullptr; t.in = R.x; t.out = R.gx;
+    t.ldi = R.nblk; t.ldo = R.nl; t.m = (R.gamma_l && !R.whole) ? R.nl : 0; t.c = R.c; t.mode = 1; t.sign = 1.0;
+    sth[set_gam * per_set + j] = t;
+  }
+  SliceTask* dst_tasks = static_cast<SliceTask*>(rb.stasks.get(sth.size() * sizeof(SliceTask)));
+  CK(cudaMemcpyAsync(dst_tasks, sth.data(), sth.size() * sizeof(SliceTask), cudaMemcpyHostToDevice, s));
+  // Launches the slice products of one set (all jobs); flops for the accounting.
+  auto slice_products = [&](size_t set, KClass cls) {
+    double fl = 0.0;
+    for (size_t j = 0; j < cj; ++j) fl += 8.0 * sth[set * per_set + j].m * (double)sth[set * per_set + j].m * sth[set * per_set + j].c;
+    if (fl == 0.0) return;
+    const dim3 grid((unsigned)((slice_m + SG_ROWS - 1) / SG_ROWS), (unsigned)((std::max(1, cmax) + SG_COLS - 1) / SG_COLS));
+    in_pieces(cj, [&](size_t f0, size_t c) {
+      launch(cls, fl * c / cj, 0.0, [&] {
+        slice_gemm_kernel<<<dim3(grid.x, grid.y, (unsigned)c), 256, 0, s>>>(dst_tasks + set * per_set + f0);
+      });
+    });
+  };
   // Right-hand-side columns per CTA: the batch's largest channel count, rounded up to 1, 2, 4, 8.
   const int cbw = cmax <= 1 ? 1 : cmax <= 2 ? 2 : cmax <= 4 ? 4 : 8;
   const unsigned cchunks = (unsigned)std::max(1, (cmax + cbw - 1) / cbw);
@@ -608,6 +666,7 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
         launch(K_REF_RES, resid_flops * c / cj, 0.0,
                [&] { gm_matvec_kernel<<<dim3((unsigned)c, rows), 256, 0, s>>>(drd + f0, k); });
       });
+      for (int side = 0; side < nsides; ++side) slice_products(set_mv + (size_t)k * nsides + side, K_REF_RES);
       for (int pass = 0; pass < 2; ++pass) {
         in_pieces(cj, [&](size_t f0, size_t c) {
           launch(K_REF_GMRES, 0.0, 0.0,
@@ -642,6 +701,8 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
       launch(K_REF_RES, resid_flops * c / cj, 0.0,
              [&] { refine_residual_kernel<<<dim3((unsigned)c, rows), 256, 0, s>>>(drd + f0); });
     });
+    for (int side = 0; side < nsides; ++side) slice_products(set_res + side, K_REF_RES);
+    slice_products(set_gam, K_REF_CHECK);
     launch(K_REF_CHECK, 0.0, 0.0, [&] {
       refine_check_kernel<<<(unsigned)cj, 256, 0, s>>>(drd, ctx->refine_tol, ctx->max_iters, rt_out, rerr, rdone);
     });

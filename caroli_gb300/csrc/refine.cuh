@@ -70,6 +70,8 @@ struct RefineDesc {
   // left slice, the others by W_R on the right slice; cl = 0 for a transmission.
   const double2* w_l;
   int32_t cl, pad2;
+  // Γ_L x_L of the current x (nl x c, column-major), formed by slice_gemm_kernel for the check.
+  double2* gx;
 };
 
 constexpr int GM_M = 12;  // Arnoldi steps per outer step
@@ -88,13 +90,6 @@ __device__ __forceinline__ double2 rhs_at(const RefineDesc& R, int i, int j) {
   return ri >= 0 ? R.w_r[ri + (int64_t)(j - R.cl) * R.nr] : make_double2(0.0, 0.0);
 }
 
-// Σ[i, a] of an m x m column-major block, or (Σ^†)[i, a] = conj(Σ[a, i]) for the adjoint.
-__device__ __forceinline__ double2 sigma_at(const double2* sg, int i, int a, int m, int adjoint) {
-  if (!adjoint) return sg[i + (int64_t)a * m];
-  const double2 v = sg[a + (int64_t)i * m];
-  return make_double2(v.x, -v.y);
-}
-
 // Forward sweep of the fronts of one level: grid (tasks, column chunks).
 // The sweeps solve M d = v for v = the residual (src < 0) or the Arnoldi vector V_src, and write
 // d to R.d (dst < 0) or to Z_dst.
@@ -105,7 +100,8 @@ __device__ __forceinline__ float2* sweep_dst(const RefineDesc& R, int dst) {
   return dst < 0 ? R.d : R.Z + (int64_t)dst * R.nblk * R.c;
 }
 
-// x += d, then the FP64 residual r = B - A x of every row: grid (jobs, row chunks of 256).
+// x += d, then the FP64 residual r = B - A x of every row: grid (jobs, row chunks of 256). The
+// residual kernel applies B - (z - H) x; the slices' Σ x follow as slice_gemm_kernel launches.
 __global__ void __launch_bounds__(256) refine_update_kernel(RefineDesc* __restrict__ rd) {
   RefineDesc& R = rd[blockIdx.x];
   if (R.done) return;
@@ -124,18 +120,13 @@ __global__ void __launch_bounds__(256) refine_residual_kernel(RefineDesc* __rest
   if (R.done) return;
   const int i = blockIdx.y * 256 + threadIdx.x;
   if (i >= R.nblk) return;
-  const int li = R.slice_l[i], ri = R.slice_r[i];
   for (int j = 0; j < R.c; ++j) {
     const double2* xj = R.x + (int64_t)j * R.nblk;
     double2 acc = rhs_at(R, i, j);
     acc.x -= R.energy * xj[i].x;
     acc.y -= R.energy * xj[i].y;
     for (int q = R.csr_ptr[i]; q < R.csr_ptr[i + 1]; ++q) acc = cfma(acc, R.vals[R.csr_q[q]], xj[R.csr_col[q]]);
-    if (li >= 0)
-      for (int a = 0; a < R.nl; ++a) acc = cfma(acc, sigma_at(R.sigma_l, li, a, R.nl, R.adjoint), xj[R.left_local[a]]);
-    if (ri >= 0)
-      for (int a = 0; a < R.nr; ++a) acc = cfma(acc, sigma_at(R.sigma_r, ri, a, R.nr, R.adjoint), xj[R.right_local[a]]);
-    R.r[i + (int64_t)j * R.nblk] = acc;
+    R.r[i + (int64_t)j * R.nblk] = acc;  // + Σ_L x + Σ_R x on the slices: slice_gemm_kernel
   }
 }
 
@@ -165,8 +156,7 @@ __global__ void __launch_bounds__(256) refine_check_kernel(RefineDesc* __restric
     const int a = idx % R.nl, j = idx / R.nl;
     const double2* xj = R.x + (int64_t)j * R.nblk;
     const int row = R.left_local[a];
-    double2 g = make_double2(0.0, 0.0);
-    for (int b = 0; b < R.nl; ++b) g = cfma(g, R.gamma_l[a + (int64_t)b * R.nl], xj[R.left_local[b]]);
+    const double2 g = R.gx[a + (int64_t)j * R.nl];  // (Γ_L x_L)[a], from slice_gemm_kernel
     const double2 xa = xj[row];
     tl += xa.x * g.x + xa.y * g.y;
     const float2 dv = R.d[row + (int64_t)j * R.nblk];
@@ -273,13 +263,13 @@ __global__ void __launch_bounds__(256) gm_start_kernel(RefineDesc* __restrict__ 
   }
 }
 
-// w = A z_k into V_{k+1}, A = z - H - Σ_L - Σ_R in FP64. grid (jobs, row chunks of 256).
+// w = A z_k into V_{k+1}, A = z - H - Σ_L - Σ_R in FP64: z - H here, grid (jobs, row chunks of
+// 256); the dense Σ blocks of the slices follow as slice_gemm_kernel launches.
 __global__ void __launch_bounds__(256) gm_matvec_kernel(RefineDesc* __restrict__ rd, int k) {
   const RefineDesc& R = rd[blockIdx.x];
   if (R.done || R.inner_done) return;
   const int i = blockIdx.y * 256 + threadIdx.x;
   if (i >= R.nblk) return;
-  const int li = R.slice_l[i], ri = R.slice_r[i];
   const float2* Zk = R.Z + (int64_t)k * R.nblk * R.c;
   double2* W = R.V + (int64_t)(k + 1) * R.nblk * R.c;
   for (int j = 0; j < R.c; ++j) {
@@ -289,11 +279,7 @@ __global__ void __launch_bounds__(256) gm_matvec_kernel(RefineDesc* __restrict__
     acc.x *= R.energy;
     acc.y *= R.energy;
     for (int q = R.csr_ptr[i]; q < R.csr_ptr[i + 1]; ++q) acc = cfms(acc, R.vals[R.csr_q[q]], zd(R.csr_col[q]));
-    if (li >= 0)
-      for (int a = 0; a < R.nl; ++a) acc = cfms(acc, sigma_at(R.sigma_l, li, a, R.nl, R.adjoint), zd(R.left_local[a]));
-    if (ri >= 0)
-      for (int a = 0; a < R.nr; ++a) acc = cfms(acc, sigma_at(R.sigma_r, ri, a, R.nr, R.adjoint), zd(R.right_local[a]));
-    W[i + (int64_t)j * R.nblk] = acc;
+    W[i + (int64_t)j * R.nblk] = acc;  // - Σ_L z - Σ_R z on the slices: slice_gemm_kernel
   }
 }
 
@@ -477,6 +463,104 @@ __global__ void gm_residual_kernel(RefineDesc* __restrict__ rd, int njobs) {
 
 namespace caroli {
 
+// ---- Dense slice products --------------------------------------------------------------------
+// The lead blocks of A (Σ_L, Σ_R: m x m, dense, on the slices' orbitals) and Γ_L of the trace,
+// applied to the c right-hand-side columns of a job at once: for i < m, j < c,
+//     out[orow[i] + j ldo] = (accumulate ? out : 0) + sign Σ_a S(i, a) in[irow[a] + j ldi],
+// S(i, a) = S[i + a m], or conj(S[a + i m]) for the adjoint solve. A batched complex FP64 GEMM:
+// 64 x 32 output tiles, K in steps of 16 staged in shared memory, a 4 x 2 complex tile per thread;
+// with hundreds of channels (a 32 x 32-site lead) these products carry most of the refinement's
+// FP64 work.
+struct SliceTask {
+  const RefineDesc* rd;  // skipped once the job is done (mode 0: or its inner solve is done)
+  const double2* s;
+  const int32_t* irow;   // rows of the input (block-local), m entries
+  const int32_t* orow;   // rows of the output, m entries; null: row i
+  const void* in;        // double2, or float2 with in_f32
+  double2* out;
+  int64_t ldi, ldo;
+  int32_t m, c, adj, in_f32, mode, accumulate;
+  double sign;
+};
+
+constexpr int SG_ROWS = 64, SG_COLS = 32, SG_K = 16;
+
+__global__ void __launch_bounds__(256) slice_gemm_kernel(const SliceTask* __restrict__ tasks) {
+  __shared__ double2 As[SG_K][SG_ROWS];
+  __shared__ double2 Bs[SG_K][SG_COLS];
+  const SliceTask t = tasks[blockIdx.z];
+  const RefineDesc& R = *t.rd;
+  if (R.done || (t.mode == 0 && R.inner_done)) return;
+  const int i0 = blockIdx.x * SG_ROWS, j0 = blockIdx.y * SG_COLS;
+  if (i0 >= t.m || j0 >= t.c) return;
+  const int tid = threadIdx.x, ti = tid & 15, tj = tid >> 4;
+  double2 acc[4][2];
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+#pragma unroll
+    for (int q = 0; q < 2; ++q) acc[r][q] = make_double2(0.0, 0.0);
+  for (int k0 = 0; k0 < t.m; k0 += SG_K) {
+    // S tile: rows i0.., columns k0.. (coalesced along the stored dimension).
+    for (int e = tid; e < SG_ROWS * SG_K; e += 256) {
+      int ii, kk;
+      if (t.adj) { kk = e % SG_K; ii = e / SG_K; }
+      else { ii = e % SG_ROWS; kk = e / SG_ROWS; }
+      const int i = i0 + ii, k = k0 + kk;
+      double2 v = make_double2(0.0, 0.0);
+      if (i < t.m && k < t.m) {
+        if (t.adj) { v = t.s[k + (int64_t)i * t.m]; v.y = -v.y; }
+        else v = t.s[i + (int64_t)k * t.m];
+      }
+      As[kk][ii] = v;
+    }
+    // Input tile: rows irow[k0..], columns j0.. (coalesced along the rows).
+    for (int e = tid; e < SG_K * SG_COLS; e += 256) {
+      const int kk = e % SG_K, jj = e / SG_K;
+      const int k = k0 + kk, j = j0 + jj;
+      double2 v = make_double2(0.0, 0.0);
+      if (k < t.m && j < t.c) {
+        const int64_t q = t.irow[k] + (int64_t)j * t.ldi;
+        if (t.in_f32) {
+          const float2 f = static_cast<const float2*>(t.in)[q];
+          v = make_double2((double)f.x, (double)f.y);
+        } else {
+          v = static_cast<const double2*>(t.in)[q];
+        }
+      }
+      Bs[kk][jj] = v;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int kk = 0; kk < SG_K; ++kk) {
+      double2 a[4], b[2];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) a[r] = As[kk][ti + 16 * r];
+#pragma unroll
+      for (int q = 0; q < 2; ++q) b[q] = Bs[kk][tj + 16 * q];
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int q = 0; q < 2; ++q) acc[r][q] = cfma(acc[r][q], a[r], b[q]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int i = i0 + ti + 16 * r;
+    if (i >= t.m) continue;
+    const int64_t orow = t.orow ? t.orow[i] : i;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int j = j0 + tj + 16 * q;
+      if (j >= t.c) continue;
+      double2& o = t.out[orow + (int64_t)j * t.ldo];
+      const double2 v = make_double2(t.sign * acc[r][q].x, t.sign * acc[r][q].y);
+      if (t.accumulate) { o.x += v.x; o.y += v.y; }
+      else o = v;
+    }
+  }
+}
+
 // Transmission matrix t = W_L^† x_L of each job after its refinement (x = G W_R): t is
 // cl x c column-major, W_L nl x cl. grid (jobs), threads over the entries of t.
 __global__ void tmatrix_kernel(const RefineDesc* __restrict__ rd, const double2* const* __restrict__ wl,
@@ -544,7 +628,8 @@ __global__ void scatter_sources_kernel(double2* __restrict__ B, int nblk, int c0
   dst.y += w.y;
 }
 
-// Right-hand side of the adjoint solve: Γ_L x_j on the left slice (x from the forward solve).
+// Right-hand side of the adjoint solve: Γ_L x_j on the left slice (x from the forward solve, Γ_L x
+// from its last check).
 // grid (jobs, row chunks).
 __global__ void __launch_bounds__(256) grad_rhs_kernel(const RefineDesc* __restrict__ fwd, double2* const* rhs) {
   const RefineDesc& R = fwd[blockIdx.x];
@@ -552,11 +637,8 @@ __global__ void __launch_bounds__(256) grad_rhs_kernel(const RefineDesc* __restr
   if (i >= R.nblk) return;
   const int li = R.slice_l[i];
   for (int j = 0; j < R.c; ++j) {
-    double2 acc = make_double2(0.0, 0.0);
-    if (li >= 0) {
-      const double2* xj = R.x + (int64_t)j * R.nblk;
-      for (int b = 0; b < R.nl; ++b) acc = cfma(acc, R.gamma_l[li + (int64_t)b * R.nl], xj[R.left_local[b]]);
-    }
+    // Γ_L x_L of the converged x: the last check's slice product (x does not change after it).
+    const double2 acc = li >= 0 ? R.gx[li + (int64_t)j * R.nl] : make_double2(0.0, 0.0);
     rhs[blockIdx.x][i + (int64_t)j * R.nblk] = acc;
   }
 }
