@@ -213,6 +213,313 @@ def time_gradient(steps):
             "status_ok": bool((st_g == 0).all() and (st_f == 0).all())}
 
 
+# ---- The many-ribbon workload: 256 graphene zigzag ribbons of uneven sizes x 64 energies ------------
+RIBBONS = ("graphene-ribbons: 256 zigzag ribbons, widths 40-160 x lengths 100-400 cells (xoshiro seed 1), "
+           "Anderson W=1.0 (seed 1000003 s + ribbon), 64 E in [-0.5,0.5]; mixed c64 + f64 refinement")
+
+
+def ribbon_shapes(count, seed):
+    """(width, length) of each ribbon: uniform integers in [40, 160] and [100, 400] cells drawn in
+    that order from xoshiro256** seed_from_u64(seed)."""
+    from caroli_gb300.disorder import Xoshiro256
+
+    rng = Xoshiro256.seed_from_u64(seed)
+    return [(rng.integer(40, 160), rng.integer(100, 400)) for _ in range(count)]
+
+
+def _ribbon_system(args):
+    """Pool worker: the System of ribbon r (graphene zigzag, clean leads, Anderson w (u - 1/2) per
+    site from seed_from_u64(1 000 003 seed + r), the benchmark's convention of
+    caroli-bench/src/main.rs:120-126)."""
+    seed, r, width, length, w = args
+    from caroli_gb300 import Region, graphene
+    from caroli_gb300.disorder import ScalarPotential, bench_disorder
+    from caroli_gb300.system import build_system
+
+    clean = graphene()
+    region = Region.cuboid(clean.lattice, [length, width, 0])
+    pot = bench_disorder(seed, r, length, width, 2, w)
+    return build_system([clean.with_onsite_term(ScalarPotential(pot, width, 2, 1))], clean, region, 0)
+
+
+def _ribbon_sigma(args):
+    """Pool worker: the clean zigzag leads' Σ_L, Σ_R and W_R of a width at every energy."""
+    width, energies = args
+    from caroli_gb300 import NestedTwoTerminal, Region, graphene
+
+    clean = graphene()
+    lead = NestedTwoTerminal.from_model(clean, clean, Region.cuboid(clean.lattice, [3, width, 0]), 0)
+    out = []
+    for e in energies:
+        s = lead.self_energies(e)
+        out.append((s.energy, s.blocks[0][0], s.blocks[0][1], s.w_right()[0]))
+    return width, out
+
+
+def ribbons_workload(count=256, energies=64, seed=1, w=1.0, processes=None):
+    """The ribbons (NestedTwoTerminal each) and, per ribbon width, the LeadSelfEnergies of every
+    energy. Host work (model builds, lead modes) runs on a spawn pool before any GPU call."""
+    import multiprocessing as mp
+
+    from caroli_gb300 import LeadSelfEnergies, NestedTwoTerminal
+
+    shapes = ribbon_shapes(count, seed)
+    es = list(np.linspace(-0.5, 0.5, energies))
+    widths = sorted({wd for wd, _ in shapes})
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+    t0 = time.perf_counter()
+    with mp.get_context("spawn").Pool(processes or os.cpu_count() or 1) as pool:
+        # Largest ribbons first so the pool's tail is short.
+        order = sorted(range(count), key=lambda r: -shapes[r][0] * shapes[r][1])
+        built = pool.map(_ribbon_system, [(seed, r, shapes[r][0], shapes[r][1], w) for r in order], chunksize=1)
+        sig = dict(pool.map(_ribbon_sigma, [(wd, es) for wd in sorted(widths, reverse=True)], chunksize=1))
+    systems = [None] * count
+    for r, s in zip(order, built):
+        systems[r] = s
+    host_s = time.perf_counter() - t0
+    ribbons = [NestedTwoTerminal(s) for s in systems]
+    sigmas = {}
+    for wd in widths:
+        row = []
+        for e, sl, sr, wr in sig[wd]:
+            lse = LeadSelfEnergies(e, [(sl, sr)])
+            lse._w_right = [wr]
+            row.append(lse)
+        sigmas[wd] = row
+    return ribbons, shapes, sigmas, es, host_s
+
+
+def run_ribbons(args):
+    """The many-ribbon workload in one batched launch sequence per step (caroli_solve_multi)."""
+    from caroli_gb300 import Precision, solve_systems
+    from caroli_gb300.nested import context
+
+    ribbons, shapes, sigmas, es, host_s = ribbons_workload(args.ribbons, args.energies)
+    ne = len(es)
+    items = [(ribbons[r], sigmas[shapes[r][0]][k], 0) for r in range(len(ribbons)) for k in range(ne)]
+    ctx = context(0)
+    t0 = time.perf_counter()
+    solve_systems(items, Precision.MIXED)  # plan and Σ uploads, first factorization
+    upload_s = time.perf_counter() - t0
+    for _ in range(max(0, args.warmup - 1)):
+        solve_systems(items, Precision.MIXED)
+    with Clocks(0) as clk:
+        ctx.region_begin()
+        w0 = time.perf_counter()
+        for _ in range(args.steps):
+            t_mixed, st_mixed, _ = solve_systems(items, Precision.MIXED)
+        ms, launches = ctx.region_end()
+        wall = time.perf_counter() - w0
+    plan0 = ribbons[0].plan()
+    fallbacks, max_iters = plan0.last_stats()
+    # FP64 on every 8th energy of every ribbon (the ratio's denominator), and the mixed T there.
+    sub = [i for i in range(len(items)) if (i % ne) % 8 == 0]
+    sub_items = [items[i] for i in sub]
+    solve_systems(sub_items, Precision.DOUBLE)
+    ctx.region_begin()
+    t_dbl, st_dbl, _ = solve_systems(sub_items, Precision.DOUBLE)
+    ms_dbl, _ = ctx.region_end()
+    ctx.region_begin()
+    t_msub, _, _ = solve_systems(sub_items, Precision.MIXED)
+    ms_msub, _ = ctx.region_end()
+    dT = np.abs(t_mixed[sub] - t_dbl)
+    # End to end: every ribbon's H values uploaded from pinned host memory each step (Σ resident:
+    # one copy per ribbon and energy, uploaded once), T read back.
+    import torch as _torch
+
+    def pinned(a):
+        buf = _torch.empty(a.size, dtype=_torch.complex128, pin_memory=True).numpy()
+        buf[...] = a.ravel()
+        return buf.reshape(a.shape)
+
+    host_vals = [pinned(np.stack(rb.system.values)) for rb in ribbons]
+    h2d = sum(v.nbytes for v in host_vals) + 3 * 4 * len(items)
+    d2h = len(items) * (8 + 4 + 8)
+    ctx.region_begin()
+    e0 = time.perf_counter()
+    for _ in range(args.steps):
+        for rb, v in zip(ribbons, host_vals):
+            rb.plan().upload_values(v)
+        solve_systems(items, Precision.MIXED)
+    e2e_ms, _ = ctx.region_end()
+    e2e_wall = time.perf_counter() - e0
+    roof, kernels = roofline_probe(ctx, lambda: solve_systems(items, Precision.MIXED), ms / args.steps,
+                                   traffic_of=lambda name: None)
+    # CPU baseline: the oracle on one energy of 16 ribbons spread over the sizes.
+    cpu = None
+    if args.cpu_sample > 0:
+        from oracle import Oracle
+
+        pick = list(range(0, len(ribbons), max(1, len(ribbons) // args.cpu_sample)))[:args.cpu_sample]
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        tref = []
+        for r in pick:
+            s = sigmas[shapes[r][0]][ne // 2]
+            t, st = Oracle(ribbons[r].system).solve_batch([0], [s.energy], [ribbons[r].system.values[0]],
+                                                          [s.blocks[0][0]], [s.blocks[0][1]], threads=threads)
+            tref.append(t[0])
+        dt = time.perf_counter() - t0
+        idx = [r * ne + ne // 2 for r in pick]
+        cpu = {"value": len(pick) / dt, "unit": "solves/s", "cores": threads, "kind": "port",
+               "sample": f"{len(pick)} ribbons spread over the sizes at E = {es[ne // 2]:.4f} (one solve at a time, "
+                         f"OpenMP inside), {dt:.1f} s wall",
+               "max_abs_dT_vs_gpu_mixed": float(np.abs(np.array(tref) - t_mixed[idx]).max())}
+    n = len(items)
+    line = {
+        "metric": METRIC, "value": n * args.steps / (ms * 1e-3), "unit": "solves/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c64 factors + f64 refinement",
+        "data": "synthetic (seeded shapes and disorder of the reference's benchmark conventions; no dataset)",
+        "config": {"workload": RIBBONS, "solves_per_step": n, "ribbons": len(ribbons),
+                   "unknowns_min_max": [int(min(2 * a * b for a, b in shapes)), int(max(2 * a * b for a, b in shapes))],
+                   "distinct_widths": len(sigmas), "parallelism": "replicas x1",
+                   "l2": "inputs larger than L2 (every ribbon's fronts per step)"},
+        "fp64_gpu": {"value": len(sub) / (ms_dbl * 1e-3), "unit": "solves/s", "ms": ms_dbl,
+                     "sample": f"every 8th energy of every ribbon ({len(sub)} solves)",
+                     "mixed_ms_same_sample": ms_msub},
+        "mixed_over_fp64": ms_dbl / ms_msub,
+        "max_abs_dT_vs_fp64": float(dT.max()), "median_abs_dT_vs_fp64": float(np.median(dT)),
+        "status_ok": bool((st_mixed == 0).all()), "fp64_recomputed_solves": int(fallbacks),
+        "e2e": {"value": n * args.steps / (e2e_ms * 1e-3), "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "wall_s": e2e_wall,
+                "note": "H values of every ribbon uploaded each step; lead self-energies resident"},
+        "gpu_launches": int(launches), "roofline": roof, "kernels_ms_per_step": kernels, "clocks": clk.summary(),
+        "wall_s_timed": wall, "host_setup_s": host_s, "first_solve_with_uploads_s": upload_s, "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---- The cubic workload: 3D Anderson wire 64 x 32 x 32, W = 16.5, mixed plus gradient ---------------
+CUBIC = ("cubic-anderson-64x32x32: 3D cubic 1-orbital t=1, Anderson W=16.5 (CLI seeds), square 32x32 leads, "
+         "32 E in [-1,1] x 16 configurations; mixed c64 + f64 refinement, dT/dV of every site")
+
+
+def cubic_workload(length=64, width=32, depth=32, configs=16):
+    from caroli_gb300 import NestedTwoTerminal, Region, cubic
+    from caroli_gb300.disorder import disordered
+
+    m = cubic()
+    region = Region.cuboid(m.lattice, [length, width, depth])
+    devices = [disordered(m, region, [{"kind": "anderson", "strength": 16.5, "seed": 1}], c) for c in range(configs)]
+    return NestedTwoTerminal.from_models(devices, m, region, 0)
+
+
+def run_cubic(args):
+    """A bounded sample of the cubic workload (its 512 solves take minutes in FP64): the energies
+    `--cubic-energies` of the 32-point grid x `--configs` configurations, mixed and FP64 on the same
+    solves, the gradient (dT/dV of all 65 536 sites) on them, and the oracle on a few."""
+    from caroli_gb300 import Precision
+    from caroli_gb300.nested import context
+
+    sys_ = cubic_workload(configs=args.configs)
+    grid = np.linspace(-1.0, 1.0, 32)
+    pick = [int(k) for k in args.cubic_energies.split(",")]
+    sigmas = [sys_.self_energies_on_device(grid[k]) for k in pick]
+    pairs = [(s, c) for s in sigmas for c in range(args.configs)]
+    S, C = [p[0] for p in pairs], [p[1] for p in pairs]
+    ctx = context(0)
+    ctx.set_mixed_max_channels(args.mixed_max_channels)
+    plan = sys_.plan()
+    for _ in range(args.warmup):
+        sys_.solve_batch(S, C, Precision.MIXED)
+    with Clocks(0) as clk:
+        ctx.region_begin()
+        w0 = time.perf_counter()
+        for _ in range(args.steps):
+            t_mixed, st_mixed, _ = sys_.solve_batch(S, C, Precision.MIXED)
+        ms, launches = ctx.region_end()
+        wall = time.perf_counter() - w0
+    phases = plan.last_phases()
+    fallbacks, max_iters = plan.last_stats()
+    steps_job, steps_batch = plan.last_refine_steps()
+    ctx.region_begin()
+    t_dbl, st_dbl, _ = sys_.solve_batch(S, C, Precision.DOUBLE)
+    ms_dbl, _ = ctx.region_end()
+    dT = np.abs(t_mixed - t_dbl)
+    # Gradient on the same solves (host self-energies: the adjoint needs Σ^† on the device too,
+    # which the slot holds either way).
+    ctx.region_begin()
+    t_g, st_g, dv, dp = sys_.transmissions_with_grad(S, C)
+    ms_grad, _ = ctx.region_end()
+    roof, kernels = roofline_probe(ctx, lambda: sys_.solve_batch(S, C, Precision.MIXED), ms / args.steps,
+                                   traffic_of=lambda name: None)
+    cpu = None
+    if args.cpu_sample > 0:
+        from oracle import Oracle
+
+        hs = sys_.self_energies(grid[pick[0]])
+        threads = os.cpu_count() or 1
+        orc = Oracle(sys_.system)
+        t0 = time.perf_counter()
+        tref, st = orc.solve_batch([0] * args.cpu_sample, [hs.energy] * args.cpu_sample,
+                                   [sys_.system.values[c] for c in range(args.cpu_sample)],
+                                   [hs.blocks[0][0]] * args.cpu_sample, [hs.blocks[0][1]] * args.cpu_sample,
+                                   threads=threads)
+        dt = time.perf_counter() - t0
+        cpu = {"value": args.cpu_sample / dt, "unit": "solves/s", "cores": threads, "kind": "port",
+               "sample": f"{args.cpu_sample} configurations at E = {hs.energy:.4f}, {dt:.1f} s wall",
+               "max_abs_dT_vs_gpu_mixed": float(np.abs(tref - t_mixed[:args.cpu_sample]).max())}
+    n = len(pairs)
+    line = {
+        "metric": METRIC, "value": n * args.steps / (ms * 1e-3), "unit": "solves/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c64 factors + f64 refinement",
+        "data": "synthetic (seeded Anderson disorder of the reference's CLI conventions; no dataset)",
+        "config": {"workload": CUBIC, "solves_per_step": n, "sample": f"energies {pick} of 32 x {args.configs} "
+                   "configurations", "unknowns": sys_.system.n, "lead_channels": [int(len(s.blocks[0][2])) for s in sigmas],
+                   "parallelism": "replicas x1", "l2": "inputs larger than L2 (fronts ~1.3 GB per solve)"},
+        "fp64_gpu": {"value": n / (ms_dbl * 1e-3), "unit": "solves/s", "ms_per_step": ms_dbl},
+        "mixed_over_fp64": ms_dbl / (ms / args.steps),
+        "max_abs_dT_vs_fp64": float(dT.max()), "max_rel_dT_vs_fp64": float((dT / np.maximum(np.abs(t_dbl), 1e-300)).max()),
+        "phases_ms": {"factor": phases[0], "root": phases[1], "refinement": phases[2]},
+        "refinement": {"max_iterations": max_iters, "fp64_recomputed_solves": fallbacks, "gmres_steps": steps_job,
+                       "batch_steps": steps_batch},
+        "gradient": {"grad_ms": ms_grad, "grad_fwd_ratio": ms_grad / (ms / args.steps),
+                     "max_abs_dT_fwd_vs_grad": float(np.abs(t_g - t_mixed).max()),
+                     "status_ok": bool((st_g == 0).all()), "sites": int(sys_.system.n)},
+        "status_ok": bool((st_mixed == 0).all() and (st_dbl == 0).all()),
+        "gpu_launches": int(launches), "roofline": roof, "kernels_ms_per_step": kernels, "clocks": clk.summary(),
+        "wall_s_timed": wall, "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def roofline_probe(ctx, step, step_ms, traffic_of):
+    """Per-kernel-class device time of one untimed step (each class probed launch by launch on its
+    own pass); the dominant class against its roof."""
+    names = ctx.kernel_classes()
+    probe = {}
+    for k, name in enumerate(names):
+        for q in range(len(names)):
+            ctx.kernel_stats(q, reset=True)
+        ctx.probe(k)
+        step()
+        ctx.probe(-1)
+        stt = ctx.kernel_stats(k)
+        probe[name] = {"ms": stt["ms"], "flops": stt["flops"], "bytes": stt["bytes"], "launches": stt["launches"]}
+    dom = max(probe.items(), key=lambda kv: kv[1]["ms"])
+    pk = peaks()
+    d = dom[1]
+    traffic = traffic_of(dom[0])
+    if dom[0] in FLOP_CLASSES:
+        achieved = d["flops"] / (d["ms"] * 1e-3) / 1e12
+        roof = {"kernel": dom[0], "bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+                "frac": achieved / pk["bf16_tflops"], "traffic": traffic, "note": f"peak = {pk['source']} bf16 dense"}
+    else:
+        achieved = d["bytes"] / (d["ms"] * 1e-3) / 1e9
+        roof = {"kernel": dom[0], "bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / pk["hbm_gbs"], "traffic": traffic, "note": f"peak = {pk['source']} HBM copy"}
+    roof["per"] = "step (all launches of the class in one step)"
+    roof["algorithmic"] = d["bytes"] if roof["bound"] == "hbm" else d["flops"]
+    roof["ms_per_step"] = d["ms"]
+    roof["launches_per_step"] = d["launches"]
+    roof["share_of_step"] = d["ms"] / step_ms
+    kernels = {k: {"ms": round(v["ms"], 3), "launches": v["launches"]} for k, v in probe.items() if v["launches"]}
+    return roof, kernels
+
+
 def cpu_baseline(sys_, pairs, sample, threads):
     """The oracle (C++ restatement of the reference's CPU path) on `sample` instances."""
     from oracle import Oracle
@@ -464,8 +771,26 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=264)
     ap.add_argument("--profile-run", action="store_true", help="warm-up steps and one step, no timing (profilers)")
     ap.add_argument("--no-gradient", dest="gradient", action="store_false", help="skip the grad/fwd measurement")
+    ap.add_argument("--workload", default="bhz", choices=["bhz", "ribbons", "cubic"],
+                    help="bhz: the headline BHZ 200x64 magnetic batch; ribbons: 256 graphene ribbons x 64 E; "
+                         "cubic: a sample of the 64x32x32 Anderson wire")
+    ap.add_argument("--ribbons", type=int, default=256)
+    ap.add_argument("--cubic-energies", default="8,16,23", help="indices into the cubic workload's 32 energies")
+    ap.add_argument("--mixed-max-channels", type=int, default=100000)
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.workload == "cubic":
+        if args.configs == 8:
+            args.configs = 2
+        if args.cpu_sample == 264:
+            args.cpu_sample = 2
+        run_cubic(args)
+    elif args.workload == "ribbons":
+        if args.energies == 33:
+            args.energies = 64
+        if args.cpu_sample == 264:
+            args.cpu_sample = 16
+        run_ribbons(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -958,11 +958,21 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
   Launcher launch{ctx, s};
   size_t begin = 0;
   while (begin < nj) {
-    // Chunk of jobs within the memory budget.
+    // Chunk of jobs within the memory budget: the fronts and, in mixed precision, the refinement's
+    // vectors (one column per channel: x, r, d, the FP64 Arnoldi basis and the f32 preconditioned
+    // vectors, the sweeps' buffers; twice with the adjoint solve of a gradient).
     size_t end = begin, bytes = 0;
     while (end < nj) {
       const FrontPlan& P = specs[end].plan->host;
       size_t b = (size_t)P.arena_elems * vb + (size_t)P.fronts[P.root].n * P.fronts[P.root].n * vr;
+      if (mixed) {
+        const SigmaSlot& sg = specs[end].sys->slots[specs[end].slot];
+        const size_t c = states ? (size_t)(states->cl[end] + states->cr[end]) : (size_t)sg.channels[specs[end].block];
+        const size_t nblk = (size_t)specs[end].sys->blocks[specs[end].block].nblk;
+        const size_t per = c * (nblk * (16 * (GM_M + 1) + 8 * GM_M + 16 + 16 + 8) +
+                                (size_t)(P.sum_ne + P.sum_nb) * 8 + (size_t)P.nl * 16);
+        b += per * (grad ? 2 : 1);
+      }
       if (end > begin && bytes + b > ctx->mem_budget) break;
       bytes += b;
       ++end;

@@ -113,18 +113,18 @@ def gradient_bhz(length, width, configs=1, anderson=0.02, concentration=0.1, exc
     return sys_, derivs
 
 
-def graphene_ribbons(count, seed=1, widths=(8, 24), lengths=(12, 40), w=1.0):
+def graphene_ribbons(count, seed=1, widths=(8, 24), lengths=(12, 40), w=1.0, pick=None):
     """Graphene zigzag ribbons of uneven sizes, as the many-ribbon workload draws them (widths and
     lengths from xoshiro seed_from_u64(seed), Anderson w(u - 0.5) per site from
-    seed_from_u64(1 000 003 seed + ribbon), the benchmark's convention of caroli-bench/src/main.rs:124),
-    at test sizes. Returns the NestedTwoTerminal of each ribbon."""
+    seed_from_u64(1 000 003 seed + ribbon), the benchmark's convention of caroli-bench/src/main.rs:124).
+    Returns the NestedTwoTerminal of each ribbon, or of the ribbons `pick` of the `count` drawn."""
     from caroli_gb300.disorder import Xoshiro256
 
     rng = Xoshiro256.seed_from_u64(seed)
+    shapes = [(rng.integer(*widths), rng.integer(*lengths)) for _ in range(count)]
     out = []
-    for r in range(count):
-        width = rng.integer(*widths)
-        length = rng.integer(*lengths)
+    for r in (range(count) if pick is None else pick):
+        width, length = shapes[r]
         clean = graphene()
         region = Region.cuboid(clean.lattice, [length, width, 0])
         subs = len(clean.lattice.sublattices)
