@@ -46,6 +46,9 @@ SIGNATURES = {
     "caroli_set_tensor_cores": (ctypes.c_int, [P, ctypes.c_int]),
     "caroli_set_mixed_max_channels": (ctypes.c_int, [P, ctypes.c_int]),
     "caroli_set_wait_limit": (ctypes.c_int, [P, ctypes.c_int64]),
+    "caroli_set_autotune": (ctypes.c_int, [P, ctypes.c_int]),
+    "caroli_set_graphs": (ctypes.c_int, [P, ctypes.c_int]),
+    "caroli_last_schedule": (ctypes.c_int, [P, P, P, P, P, P, P]),
     "caroli_solve_multi": (ctypes.c_int, [P, ctypes.c_int, P, P, P, ctypes.c_int, P, P, P]),
     "caroli_scattering_states": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P, P, P, P]),
     "caroli_multi_leads": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P]),
@@ -145,6 +148,26 @@ class Context:
     def set_mixed_max_channels(self, channels=96):
         """Mixed-precision block solves with more sources than ``channels`` take the FP64 path."""
         self.check(self.lib.caroli_set_mixed_max_channels(self.h, int(channels)))
+
+    def set_autotune(self, enable=True):
+        """The f32 factorization's schedule picked per plan set by timing trials (default on)."""
+        self.check(self.lib.caroli_set_autotune(self.h, 1 if enable else 0))
+
+    def set_graphs(self, enable=True):
+        """Replay a repeated batch's factorization as a CUDA graph (default on)."""
+        self.check(self.lib.caroli_set_graphs(self.h, 1 if enable else 0))
+
+    def last_schedule(self):
+        """The last batch's schedule: small_max, tensor_cores, tuned, the trial times (ms) of
+        (48, 64, 96) x (tensor cores, CUDA cores), graph replays and captures so far."""
+        sm, tc, tu = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        ms = np.zeros(6)
+        rep, cap = ctypes.c_int64(), ctypes.c_int64()
+        self.check(self.lib.caroli_last_schedule(self.h, ctypes.byref(sm), ctypes.byref(tc), ctypes.byref(tu), ptr(ms),
+                                                 ctypes.byref(rep), ctypes.byref(cap)))
+        return {"small_max": sm.value, "tensor_cores": bool(tc.value), "tuned": bool(tu.value),
+                "trial_ms": [None if np.isnan(x) else float(x) for x in ms], "graph_replays": rep.value,
+                "graph_captures": cap.value}
 
     def set_wait_limit(self, polls=-1):
         """Polls of a tensor-core pipeline wait before it gives up (negative: the default)."""

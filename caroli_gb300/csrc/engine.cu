@@ -12,6 +12,7 @@
 #include <cstdio>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <numeric>
@@ -275,7 +276,7 @@ struct TaskLevel {
 struct TaskCache {
   bool valid = false;
   std::vector<uint64_t> plans;  // identities of the chunk's plans
-  int tsize = 0, trsize = 0, max_levels = 0;
+  int tsize = 0, trsize = 0, max_levels = 0, small_max = 0;
   bool mixed = false;
   const void *arena = nullptr, *rarena = nullptr;
   std::vector<Task> tasks;
@@ -287,6 +288,31 @@ struct TaskCache {
   double root_flops = 0.0, trace_flops = 0.0;
   const void *piv = nullptr, *y = nullptr, *bt = nullptr, *scale = nullptr, *bad = nullptr, *dinv = nullptr,
              *dtasks = nullptr;
+};
+
+// The autotuner's choice for a plan set: the largest f32 front factored by one CTA in shared
+// memory (fronts above it take the panel sweep and the rank-32 updates), whether those updates run
+// on the tensor cores, and the factorization times the trials measured.
+struct TuneChoice {
+  int small_max = SMALL_MAX_F32;
+  bool tensor_cores = true;
+  bool tuned = false;
+  double ms[6] = {0, 0, 0, 0, 0, 0};  // per candidate (small_max 48 / 64 / 96 x tensor cores on / off)
+};
+
+// A captured factorization (every level's launches, the root assembly and inverse) and what it
+// was captured with: a batch with the same key replays it with one graph launch.
+struct FactorGraph {
+  cudaGraphExec_t exec = nullptr;
+  std::vector<uint64_t> key;
+  std::vector<uint64_t> seen;  // the key of the previous batch: a key is captured on its second run
+  int64_t launches = 0;
+  KStat stats[K_COUNT];
+  void reset() {
+    if (exec) cudaGraphExecDestroy(exec);
+    exec = nullptr;
+    key.clear();
+  }
 };
 
 }  // namespace
@@ -336,6 +362,16 @@ struct caroli_ctx {
   int mixed_max_channels = MIXED_MAX_CHANNELS;  // CAROLI_MIXED block solves with more channels run in FP64
   uint32_t tc_wait_limit = TCU_WAIT;            // polls of a pipeline wait in tc_update_kernel
   unsigned char* noalloc_base = nullptr;        // device address of the allocation-free scratch array
+  // Autotuner and graph replay (see run_jobs and tune_jobs).
+  bool autotune = true;                         // pick the f32 factorization's schedule per plan set
+  bool use_graphs = true;                       // replay a repeated batch's factorization as a CUDA graph
+  int small_max_f32 = SMALL_MAX_F32;            // f32 fronts up to this size: one CTA each (else panel + update)
+  bool tc_choice = true;                        // the autotuner's tensor-core choice (with tensor_cores set)
+  bool factor_only = false;                     // run_jobs stops after the root inverse (tuning trials)
+  std::map<std::vector<uint64_t>, TuneChoice> tuned;  // per plan set and precision
+  TuneChoice last_tune;                               // the choice the last batch ran with
+  FactorGraph fgraph;                                 // the factorization of the last repeated batch
+  int64_t graph_replays = 0, graph_captures = 0;
   // Every entry point taking the context holds this for its whole call, so that threads sharing a
   // context are serialised (recursive: an entry point may reach another one's helpers).
   mutable std::recursive_mutex mu;
@@ -362,7 +398,6 @@ System* get_system(caroli_ctx* ctx, int id) {
 }
 
 template <typename T> struct Prec {
-  static constexpr int small_max = sizeof(T) == 8 ? SMALL_MAX_F64 : SMALL_MAX_F32;
   static constexpr double tol = sizeof(T) == 8 ? PIVOT_TOL_F64 : PIVOT_TOL_F32;
 };
 
@@ -1028,15 +1063,15 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
     // kept with its device copies: a repeated batch reuses them without host work.
     using Level = TaskLevel;
     TaskCache& tc = ctx->tcache;
+    const int small_max = sizeof(T) == 8 ? SMALL_MAX_F64 : ctx->small_max_f32;
     std::vector<uint64_t> key_plans(cj);
     for (size_t j = 0; j < cj; ++j) key_plans[j] = specs[begin + j].plan->id;
     const bool hit = tc.valid && tc.plans == key_plans && tc.tsize == (int)sizeof(T) && tc.trsize == (int)sizeof(TR) &&
                      tc.mixed == mixed && tc.arena == (const void*)arena && tc.rarena == (const void*)rarena &&
-                     tc.max_levels == max_levels;
+                     tc.max_levels == max_levels && tc.small_max == small_max;
     std::vector<Task>& tasks = tc.tasks;
     std::vector<Level>& levels = tc.levels;
     std::vector<InvTask>& inv = tc.inv;  // large fronts' pivot blocks per level, then the roots
-    const int small_max = Prec<T>::small_max;
     size_t& inv_piv = tc.inv_piv;  // scratch sizes: pivots (entries) and Y blocks (bytes)
     size_t& inv_y = tc.inv_y;
     size_t& inv_bt = tc.inv_bt;
@@ -1198,6 +1233,7 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
     tc.arena = arena;
     tc.rarena = rarena;
     tc.max_levels = max_levels;
+    tc.small_max = small_max;
     tc.valid = true;
 
     // Batched blocked inverse of `count` matrices starting at dinv + first, largest n.
@@ -1224,7 +1260,7 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
         const unsigned rt = (unsigned)((nmax + 63) / 64);
         in_pieces(count, [&](size_t f0, size_t c) {
           launch(ucls, uper * c / count, ubper * c / count, [&] {
-            if (std::is_same<TT, float>::value && ctx->tensor_cores)
+            if (std::is_same<TT, float>::value && ctx->tensor_cores && ctx->tc_choice)
               tc_update_kernel<<<dim3((unsigned)((nmax + TCU_ROWS - 1) / TCU_ROWS), (unsigned)c,
                                       (unsigned)((nmax + TCU_COLS * TCU_GROUP - 1) / (TCU_COLS * TCU_GROUP))),
                                  TCU_THREADS, TCU_SMEM, s>>>(
@@ -1237,62 +1273,130 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
       launch(cls, 0.0, 0.0, [&] { inv_finish_kernel<TT><<<(unsigned)count, 256, smf, s>>>(dinv + first, djobs, status); });
     };
 
-    CK(cudaEventRecord(ctx->ev0, s));
     const int perturb = mixed ? 1 : 0;
-    // Factorization, level by level.
-    for (int L = 0; L < max_levels; ++L) {
-      const Level& lv = levels[L];
-      if (lv.tiny_n) {
-        const unsigned blocks = (unsigned)((lv.tiny_n + TINY_WARPS - 1) / TINY_WARPS);
-        launch(K_SMALL, lv.tiny_flops, lv.tiny_bytes, [&] {
-          if (mixed)
-            tiny_front_kernel<T, true><<<blocks, 256, tiny_smem<T>(lv.max_tiny_n), s>>>(
-                djobs, dtasks + lv.tiny0, (int)lv.tiny_n, Prec<T>::tol, perturb, pert, lv.max_tiny_n);
-          else
-            tiny_front_kernel<T, false><<<blocks, 256, tiny_smem<T>(lv.max_tiny_n), s>>>(
-                djobs, dtasks + lv.tiny0, (int)lv.tiny_n, Prec<T>::tol, perturb, pert, lv.max_tiny_n);
-        });
-      }
-      for (int b = 0; b < 3; ++b) {
-        if (!lv.sbn[b]) continue;
-        const size_t sm = small_smem_bytes(lv.sb_n[b], lv.sb_ne[b], vb);
-        const unsigned nblk = (unsigned)lv.sbn[b];
-        const Task* st = dtasks + lv.sb0[b];
-        const double share = (double)lv.sbn[b] / (double)lv.small_n;
-        launch(K_SMALL, lv.small_flops * share, lv.small_bytes * share, [&] {
-          if (mixed)
-            small_front_kernel<T, true><<<nblk, 256, sm, s>>>(djobs, st, Prec<T>::tol, perturb, pert);
-          else
-            small_front_kernel<T, false><<<nblk, 256, sm, s>>>(djobs, st, Prec<T>::tol, perturb, pert);
-        });
-      }
-      if (lv.large_n) {
-        const Task* lt = dtasks + lv.large0;
-        const int mt = (lv.max_large_n + 63) / 64;
-        in_pieces(lv.large_n, [&](size_t f0, size_t c) {
-          launch(K_ASSEMBLE, 0.0, lv.asm_bytes * c / lv.large_n, [&] {
-            assemble_kernel<T, T><<<dim3((lv.max_large_n + 31) / 32, (unsigned)c), 256, 0, s>>>(djobs, lt + f0, 0);
+    // Factorization level by level, then the root front and its inverse: a fixed launch sequence
+    // for a given batch (task lists, scratch, schedule).
+    auto factor_all = [&]() {
+      CK(cudaEventRecord(ctx->ev0, s));
+      // Factorization, level by level.
+      for (int L = 0; L < max_levels; ++L) {
+        const Level& lv = levels[L];
+        if (lv.tiny_n) {
+          const unsigned blocks = (unsigned)((lv.tiny_n + TINY_WARPS - 1) / TINY_WARPS);
+          launch(K_SMALL, lv.tiny_flops, lv.tiny_bytes, [&] {
+            if (mixed)
+              tiny_front_kernel<T, true><<<blocks, 256, tiny_smem<T>(lv.max_tiny_n), s>>>(
+                  djobs, dtasks + lv.tiny0, (int)lv.tiny_n, Prec<T>::tol, perturb, pert, lv.max_tiny_n);
+            else
+              tiny_front_kernel<T, false><<<blocks, 256, tiny_smem<T>(lv.max_tiny_n), s>>>(
+                  djobs, dtasks + lv.tiny0, (int)lv.tiny_n, Prec<T>::tol, perturb, pert, lv.max_tiny_n);
           });
-        });
-        const size_t ninv = (L + 1 < max_levels ? levels[L + 1].inv0 : rinv0) - lv.inv0;
-        inverse(T{}, lv.inv0, ninv, lv.max_large_n, lv.max_large_ne, Prec<T>::tol, perturb, K_PANEL, lv.pan_flops,
-                K_UPDATE, lv.upd_flops, lv.upd_bytes);
-        (void)mt;
+        }
+        for (int b = 0; b < 3; ++b) {
+          if (!lv.sbn[b]) continue;
+          const size_t sm = small_smem_bytes(lv.sb_n[b], lv.sb_ne[b], vb);
+          const unsigned nblk = (unsigned)lv.sbn[b];
+          const Task* st = dtasks + lv.sb0[b];
+          const double share = (double)lv.sbn[b] / (double)lv.small_n;
+          launch(K_SMALL, lv.small_flops * share, lv.small_bytes * share, [&] {
+            if (mixed)
+              small_front_kernel<T, true><<<nblk, 256, sm, s>>>(djobs, st, Prec<T>::tol, perturb, pert);
+            else
+              small_front_kernel<T, false><<<nblk, 256, sm, s>>>(djobs, st, Prec<T>::tol, perturb, pert);
+          });
+        }
+        if (lv.large_n) {
+          const Task* lt = dtasks + lv.large0;
+          const int mt = (lv.max_large_n + 63) / 64;
+          in_pieces(lv.large_n, [&](size_t f0, size_t c) {
+            launch(K_ASSEMBLE, 0.0, lv.asm_bytes * c / lv.large_n, [&] {
+              assemble_kernel<T, T><<<dim3((lv.max_large_n + 31) / 32, (unsigned)c), 256, 0, s>>>(djobs, lt + f0, 0);
+            });
+          });
+          const size_t ninv = (L + 1 < max_levels ? levels[L + 1].inv0 : rinv0) - lv.inv0;
+          inverse(T{}, lv.inv0, ninv, lv.max_large_n, lv.max_large_ne, Prec<T>::tol, perturb, K_PANEL, lv.pan_flops,
+                  K_UPDATE, lv.upd_flops, lv.upd_bytes);
+          (void)mt;
+        }
       }
-    }
-    CK(cudaEventRecord(ctx->evf, s));
-    // Root front in TR, then its inverse. The reference's root LU has no stability test (a zero
-    // pivot means a singular root); in mixed precision tiny root pivots are perturbed like the
-    // fronts' (the refinement corrects).
-    const Task* rt = dtasks + root0;
-    in_pieces(cj, [&](size_t f0, size_t c) {
-      launch(K_ROOT_ASM, 0.0, 0.0, [&] {
-        assemble_kernel<T, TR><<<dim3((max_root + 31) / 32, (unsigned)c), 256, 0, s>>>(djobs, rt + f0, 1);
+      CK(cudaEventRecord(ctx->evf, s));
+      // Root front in TR, then its inverse. The reference's root LU has no stability test (a zero
+      // pivot means a singular root); in mixed precision tiny root pivots are perturbed like the
+      // fronts' (the refinement corrects).
+      const Task* rt = dtasks + root0;
+      in_pieces(cj, [&](size_t f0, size_t c) {
+        launch(K_ROOT_ASM, 0.0, 0.0, [&] {
+          assemble_kernel<T, TR><<<dim3((max_root + 31) / 32, (unsigned)c), 256, 0, s>>>(djobs, rt + f0, 1);
+        });
       });
-    });
-    inverse(TR{}, rinv0, cj, max_root, max_root, mixed ? Prec<T>::tol * 1e-2 : 0.0, perturb, K_ROOT_INV, root_flops,
-            K_ROOT_INV, 0.0, 0.0);
-    CK(cudaEventRecord(ctx->evr, s));
+      inverse(TR{}, rinv0, cj, max_root, max_root, mixed ? Prec<T>::tol * 1e-2 : 0.0, perturb, K_ROOT_INV, root_flops,
+              K_ROOT_INV, 0.0, 0.0);
+      CK(cudaEventRecord(ctx->evr, s));
+    };
+    // A batch seen twice in a row (same plans, schedule and scratch) is captured as a CUDA graph
+    // on its second run and replayed afterwards: one launch in place of the level-by-level
+    // sequence. Probed runs (per-launch events) always launch directly.
+    std::vector<uint64_t> gkey(key_plans);
+    for (uint64_t v : {(uint64_t)sizeof(T), (uint64_t)sizeof(TR), (uint64_t)mixed, (uint64_t)small_max,
+                       (uint64_t)(ctx->tensor_cores && ctx->tc_choice), (uint64_t)ctx->tc_wait_limit, (uint64_t)cj,
+                       (uint64_t)(uintptr_t)djobs,
+                       (uint64_t)(uintptr_t)dtasks, (uint64_t)(uintptr_t)dinv, (uint64_t)(uintptr_t)pert,
+                       (uint64_t)(uintptr_t)status, (uint64_t)(uintptr_t)arena, (uint64_t)(uintptr_t)rarena})
+      gkey.push_back(v);
+    FactorGraph& fg = ctx->fgraph;
+    if (!ctx->use_graphs || ctx->probe >= 0) {
+      factor_all();
+    } else if (fg.exec && fg.key == gkey) {
+      CK(cudaGraphLaunch(fg.exec, s));
+      for (int k = 0; k < K_COUNT; ++k) {
+        ctx->kstat[k].launches += fg.stats[k].launches;
+        ctx->kstat[k].flops += fg.stats[k].flops;
+        ctx->kstat[k].bytes += fg.stats[k].bytes;
+      }
+      launch.launches += fg.launches;
+      ctx->graph_replays += 1;
+    } else if (fg.seen == gkey) {
+      fg.reset();
+      KStat before[K_COUNT];
+      for (int k = 0; k < K_COUNT; ++k) before[k] = ctx->kstat[k];
+      const int64_t l0 = launch.launches;
+      cudaGraph_t graph = nullptr;
+      CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      try {
+        factor_all();
+      } catch (...) {
+        cudaStreamEndCapture(s, &graph);
+        if (graph) cudaGraphDestroy(graph);
+        throw;
+      }
+      CK(cudaStreamEndCapture(s, &graph));
+      const cudaError_t ie = cudaGraphInstantiate(&fg.exec, graph, 0);
+      cudaGraphDestroy(graph);
+      CK(ie);
+      fg.key = gkey;
+      fg.launches = launch.launches - l0;
+      for (int k = 0; k < K_COUNT; ++k) {
+        fg.stats[k].launches = ctx->kstat[k].launches - before[k].launches;
+        fg.stats[k].flops = ctx->kstat[k].flops - before[k].flops;
+        fg.stats[k].bytes = ctx->kstat[k].bytes - before[k].bytes;
+      }
+      CK(cudaGraphLaunch(fg.exec, s));
+      ctx->graph_captures += 1;
+    } else {
+      factor_all();
+    }
+    fg.seen = gkey;
+    if (ctx->factor_only) {  // a tuning trial: the factorization time is all it needs
+      CK(cudaStreamSynchronize(s));
+      float mf = 0.f, mr = 0.f;
+      CK(cudaEventElapsedTime(&mf, ctx->ev0, ctx->evf));
+      CK(cudaEventElapsedTime(&mr, ctx->evf, ctx->evr));
+      ctx->factor_ms += mf;
+      ctx->root_ms += mr;
+      launch.collect();
+      begin = end;
+      continue;
+    }
     std::vector<double> th(cj), eh(cj, 0.0);
     std::vector<int32_t> sh(cj, ST_OK), ih(cj, 0);
     if (!mixed) {
@@ -1496,10 +1600,83 @@ void solve_with_delays(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>&
   }
 }
 
+// The autotuner of the f32 factorization: for a plan set not seen before, the factorization (tree
+// and root, device time between CUDA events) of up to 256 of its block solves is run under each
+// candidate schedule, and the fastest is kept for that plan set and precision. Candidates: the
+// largest front factored by one CTA in shared memory (48, 64 or 96 variables; larger fronts take
+// the panel sweep and rank-32 updates) x those updates on the tensor cores or on the CUDA cores.
+// The trials leave the results and the accounting of the call untouched.
+template <typename TR>
+void apply_tuning(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, Mode mode) {
+  ctx->small_max_f32 = SMALL_MAX_F32;
+  ctx->tc_choice = true;
+  if (specs.empty()) return;
+  std::vector<uint64_t> key;
+  for (const JobSpec& sp : specs) key.push_back(sp.plan->id);
+  std::sort(key.begin(), key.end());
+  key.erase(std::unique(key.begin(), key.end()), key.end());
+  key.push_back(0xC0FFEE00u + (uint64_t)mode);
+  key.push_back(ctx->tensor_cores ? 1 : 0);
+  auto it = ctx->tuned.find(key);
+  if (it == ctx->tuned.end()) {
+    if (!ctx->autotune || ctx->probe >= 0) {
+      ctx->last_tune = TuneChoice{};
+      ctx->last_tune.tensor_cores = ctx->tensor_cores;
+      return;
+    }
+    // Saved accounting of the call (the trials must not show in it).
+    KStat saved[K_COUNT];
+    for (int k = 0; k < K_COUNT; ++k) saved[k] = ctx->kstat[k];
+    const double s_last = ctx->last_ms, s_f = ctx->factor_ms, s_r = ctx->root_ms, s_t = ctx->tail_ms;
+    const int64_t s_ll = ctx->last_launches, s_rl = ctx->region_launches;
+    std::vector<JobSpec> sample(specs.begin(), specs.begin() + std::min<size_t>(specs.size(), 256));
+    TuneChoice best;
+    best.tuned = true;
+    double best_ms = INFINITY;
+    const int cand_small[3] = {48, 64, 96};
+    const bool use_graphs = ctx->use_graphs;
+    ctx->use_graphs = false;
+    ctx->factor_only = true;
+    try {
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 2; ++b) {
+          const bool tcv = b == 0;
+          if (tcv && !ctx->tensor_cores) { best.ms[a * 2 + b] = NAN; continue; }
+          ctx->small_max_f32 = cand_small[a];
+          ctx->tc_choice = tcv;
+          ctx->factor_ms = ctx->root_ms = 0.0;
+          std::vector<JobOut> tmp;
+          run_jobs<float, TR>(ctx, sys, sample, mode, tmp);
+          const double ms = ctx->factor_ms + ctx->root_ms;
+          best.ms[a * 2 + b] = ms;
+          if (ms < best_ms) {
+            best_ms = ms;
+            best.small_max = cand_small[a];
+            best.tensor_cores = tcv;
+          }
+        }
+    } catch (...) {
+      ctx->factor_only = false;
+      ctx->use_graphs = use_graphs;
+      throw;
+    }
+    ctx->factor_only = false;
+    ctx->use_graphs = use_graphs;
+    for (int k = 0; k < K_COUNT; ++k) ctx->kstat[k] = saved[k];
+    ctx->last_ms = s_last; ctx->factor_ms = s_f; ctx->root_ms = s_r; ctx->tail_ms = s_t;
+    ctx->last_launches = s_ll; ctx->region_launches = s_rl;
+    it = ctx->tuned.emplace(key, best).first;
+  }
+  ctx->small_max_f32 = it->second.small_max;
+  ctx->tc_choice = it->second.tensor_cores;
+  ctx->last_tune = it->second;
+}
+
 void solve_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, Mode mode, std::vector<JobOut>& out) {
   if (mode == MODE_DOUBLE) {
     solve_with_delays<double, double>(ctx, sys, specs, mode, out);
   } else if (mode == MODE_SINGLE) {
+    apply_tuning<double>(ctx, sys, specs, mode);
     solve_with_delays<float, double>(ctx, sys, specs, mode, out);
   } else {
     // Block solves with many right-lead channels go to the FP64 path directly: the refinement
@@ -1516,6 +1693,7 @@ void solve_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs,
     out.assign(specs.size(), JobOut{});
     if (!few.empty()) {
       std::vector<JobOut> fo;
+      apply_tuning<float>(ctx, sys, few, mode);
       run_jobs<float, float>(ctx, sys, few, mode, fo);
       for (size_t q = 0; q < few_idx.size(); ++q) out[few_idx[q]] = std::move(fo[q]);
     }
@@ -1680,6 +1858,7 @@ void caroli_ctx_destroy(caroli_ctx* ctx) {
     cudaEventDestroy(e.first);
     cudaEventDestroy(e.second);
   }
+  ctx->fgraph.reset();
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -2018,6 +2197,7 @@ int caroli_transmission_with_grad(caroli_ctx* ctx, int plan_id, int count, const
     g.nparams = sys->dvals ? sys->nparams : 0;
     g.nnz = sys->desc.row_ptr[sys->desc.n];
     std::vector<JobOut> jo;
+    apply_tuning<float>(ctx, sys, specs, MODE_MIXED);
     run_jobs<float, float>(ctx, sys, specs, MODE_MIXED, jo, &g);
     const int64_t n = sys->desc.n;
     for (int i = 0; i < count; ++i) {
@@ -2108,6 +2288,7 @@ int caroli_scattering_states(caroli_ctx* ctx, int plan_id, int count, const int3
     std::vector<std::vector<double2>> psi(specs.size());
     rq.psi = &psi;
     std::vector<JobOut> jo;
+    apply_tuning<float>(ctx, sys, specs, MODE_MIXED);
     run_jobs<float, float>(ctx, sys, specs, MODE_MIXED, jo, nullptr, &rq);
     // Block-local columns to the caller's layout: ψ_L of instance i is n x Σ_b cl_b, block b's
     // columns after those of the blocks before it, zero outside the block's orbitals.
@@ -2220,6 +2401,7 @@ void multi_mixed(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs
     std::vector<std::vector<double2>> q(fs.size());
     rq.psi = &q;
     std::vector<JobOut> fo;
+    apply_tuning<float>(ctx, sys, fs, MODE_MIXED);
     run_jobs<float, float>(ctx, sys, fs, MODE_MIXED, fo, nullptr, &rq);
     for (size_t k = 0; k < fs.size(); ++k) {
       const size_t j = few[k];
@@ -2594,6 +2776,7 @@ int caroli_transmission_matrix(caroli_ctx* ctx, int plan_id, int count, const in
     std::vector<std::vector<double2>> tm(specs.size());
     rq.psi = &tm;
     std::vector<JobOut> jo;
+    apply_tuning<float>(ctx, sys, specs, MODE_MIXED);
     run_jobs<float, float>(ctx, sys, specs, MODE_MIXED, jo, nullptr, &rq);
     for (int i = 0; i < count; ++i) {
       int32_t st = ST_OK;
@@ -2819,6 +3002,7 @@ int caroli_multi_scattering_states(caroli_ctx* ctx, int plan_id, int count, cons
     std::vector<std::vector<double2>> x(specs.size());
     rq.psi = &x;
     std::vector<JobOut> jo;
+    apply_tuning<float>(ctx, sys, specs, MODE_MIXED);
     run_jobs<float, float>(ctx, sys, specs, MODE_MIXED, jo, nullptr, &rq);
     const int64_t n = sys->desc.n;
     for (int i = 0; i < count; ++i) {
@@ -3201,6 +3385,38 @@ int caroli_set_mixed_max_channels(caroli_ctx* ctx, int channels) {
   if (!ctx) return CAROLI_EINVAL;
   if (channels < 0) return fail_with(ctx, CAROLI_EINVAL, "caroli_set_mixed_max_channels: negative channel count");
   ctx->mixed_max_channels = channels;
+  return CAROLI_OK;
+}
+
+int caroli_set_autotune(caroli_ctx* ctx, int enable) {
+  CTX_LOCK(ctx);
+  if (!ctx) return CAROLI_EINVAL;
+  ctx->autotune = enable != 0;
+  ctx->tuned.clear();
+  return CAROLI_OK;
+}
+
+int caroli_set_graphs(caroli_ctx* ctx, int enable) {
+  CTX_LOCK(ctx);
+  if (!ctx) return CAROLI_EINVAL;
+  ctx->use_graphs = enable != 0;
+  ctx->fgraph.reset();
+  ctx->fgraph.seen.clear();
+  return CAROLI_OK;
+}
+
+int caroli_last_schedule(const caroli_ctx* ctx, int32_t* small_max, int32_t* tensor_cores, int32_t* tuned,
+                         double* trial_ms, int64_t* graph_replays, int64_t* graph_captures) {
+  CTX_LOCK(ctx);
+  if (!ctx) return CAROLI_EINVAL;
+  const TuneChoice& t = ctx->last_tune;
+  if (small_max) *small_max = t.small_max;
+  if (tensor_cores) *tensor_cores = t.tensor_cores ? 1 : 0;
+  if (tuned) *tuned = t.tuned ? 1 : 0;
+  if (trial_ms)
+    for (int k = 0; k < 6; ++k) trial_ms[k] = t.ms[k];
+  if (graph_replays) *graph_replays = ctx->graph_replays;
+  if (graph_captures) *graph_captures = ctx->graph_captures;
   return CAROLI_OK;
 }
 

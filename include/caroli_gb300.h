@@ -367,6 +367,27 @@ int caroli_set_mixed_max_channels(caroli_ctx* ctx, int channels);
  * testing that path. No reference counterpart. */
 int caroli_set_wait_limit(caroli_ctx* ctx, int64_t polls);
 
+/* The autotuner (default on; no reference counterpart): the first time a set of plans is solved in
+ * reduced precision, the f32 factorization of up to 256 of its block solves is timed under each
+ * candidate schedule (the largest front factored by one CTA in shared memory: 48, 64 or 96
+ * variables, larger ones taking the panel sweep and rank-32 updates; those updates on the tensor
+ * cores or the CUDA cores) and the fastest is kept for that plan set and precision. Off: the
+ * default schedule (96, tensor cores as caroli_set_tensor_cores). Changing it forgets the choices. */
+int caroli_set_autotune(caroli_ctx* ctx, int enable);
+
+/* CUDA graph replay (default on; no reference counterpart): a batch run twice in a row with the
+ * same plans, schedule and device buffers has its factorization (every tree level's launches, the
+ * root assembly and inverse) captured as a CUDA graph on its second run and replayed with one
+ * launch afterwards. */
+int caroli_set_graphs(caroli_ctx* ctx, int enable);
+
+/* The schedule the last batch ran with: small_max and tensor_cores as above, tuned = 1 when the
+ * autotuner chose them, trial_ms[6] (may be NULL) the trials' factorization times in ms for
+ * (48, 64, 96) x (tensor cores, CUDA cores) (NaN: not tried), and the factorization graphs replayed
+ * and captured so far. */
+int caroli_last_schedule(const caroli_ctx* ctx, int32_t* small_max, int32_t* tensor_cores, int32_t* tuned,
+                         double* trial_ms, int64_t* graph_replays, int64_t* graph_captures);
+
 /* Device time of the last caroli_solve_batch split into the tree factorization, the root
  * inverse, and the rest (trace, or refinement and double-precision recomputations), in ms. */
 int caroli_last_phases(const caroli_ctx* ctx, double* factor_ms, double* root_ms, double* tail_ms);

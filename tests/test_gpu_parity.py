@@ -158,6 +158,7 @@ def test_tensor_core_updates_match_cuda_cores():
     S, C = [p[0] for p in pairs], [p[1] for p in pairs]
     ctx = context(0)
     out = {}
+    ctx.set_autotune(False)  # the schedule as set here, not the tuner's choice
     try:
         for tc in (True, False):
             ctx.set_tensor_cores(tc)
@@ -167,6 +168,7 @@ def test_tensor_core_updates_match_cuda_cores():
             out[tc] = (t32, tm, sys_.plan().last_refine_steps()[0])
     finally:
         ctx.set_tensor_cores(True)
+        ctx.set_autotune(True)
     for k, (s, c) in enumerate(pairs):
         ref = oracle_T(sys_, s, config=c)
         e_tc, e_cc = abs(out[True][0][k] - ref), abs(out[False][0][k] - ref)

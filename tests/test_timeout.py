@@ -23,6 +23,7 @@ def test_wait_limit_timeout_reaches_caller_and_context_recovers():
     plan = sys_.plan()
     ctx = plan.ctx
     ctx.set_tensor_cores(True)
+    ctx.set_autotune(False)  # the default schedule: fronts above 96 variables on the tensor cores
     try:
         ctx.set_wait_limit(0)
         t, st, _ = sys_.solve_batch(sigmas, [0, 0], Precision.SINGLE)
@@ -35,7 +36,10 @@ def test_wait_limit_timeout_reaches_caller_and_context_recovers():
             assert abs(tm - r) <= 1e-10 * (1 + abs(r)), (tm, r)
     finally:
         ctx.set_wait_limit(-1)
+        ctx.set_autotune(True)
+    ctx.set_autotune(False)
     t, st, _ = sys_.solve_batch(sigmas, [0, 0], Precision.SINGLE)
+    ctx.set_autotune(True)
     assert (st == _native.OK).all(), st
     for ts, r in zip(t, ref):
         assert abs(ts - r) < 1e-2, (ts, r)
