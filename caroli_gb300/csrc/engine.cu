@@ -191,6 +191,11 @@ struct Buf {
     }
     return p;
   }
+  void release() {
+    cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
   ~Buf() { cudaFree(p); }
 };
 
@@ -231,6 +236,10 @@ struct RefineBufs {
   Buf rdesc, rx, rr, rd, rtb, rhb, rt, rerr, rdone, rgx, stasks;
   Buf gV, gZ, gH, gg, gcs, gsn, gy, gbeta, gcol, gflags;
   Buf segs, ctasks, ccount, cjobs;  // task lists compacted to the solves still iterating
+  // The vectors (one column per channel; the bulk of a mixed batch's memory besides the fronts).
+  void release_vectors() {
+    for (Buf* b : {&rx, &rr, &rd, &rtb, &rhb, &rgx, &gV, &gZ}) b->release();
+  }
 };
 
 // A gradient request: d H / d p values of every configuration, and the per-job outputs.
@@ -991,6 +1000,10 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
   const bool mixed = mode == MODE_MIXED;
   out.assign(nj, JobOut{});
   Launcher launch{ctx, s};
+  // The memory budget of a batch covers its fronts and, in mixed precision, its refinement vectors;
+  // a batch without refinement gives the idle vectors of an earlier mixed batch back first.
+  if (!mixed)
+    for (RefineBufs& b : ctx->rb) b.release_vectors();
   size_t begin = 0;
   while (begin < nj) {
     // Chunk of jobs within the memory budget: the fronts and, in mixed precision, the refinement's
