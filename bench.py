@@ -312,6 +312,7 @@ def run_ribbons(args):
         ms, launches = ctx.region_end()
         wall = time.perf_counter() - w0
     plan0 = ribbons[0].plan()
+    schedule = ctx.last_schedule()
     fallbacks, max_iters = plan0.last_stats()
     # FP64 on every 8th energy of every ribbon (the ratio's denominator), and the mixed T there.
     sub = [i for i in range(len(items)) if (i % ne) % 8 == 0]
@@ -385,8 +386,8 @@ def run_ribbons(args):
         "e2e": {"value": n * args.steps / (e2e_ms * 1e-3), "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "wall_s": e2e_wall,
                 "note": "H values of every ribbon uploaded each step; lead self-energies resident"},
-        "gpu_launches": int(launches), "roofline": roof, "kernels_ms_per_step": kernels, "clocks": clk.summary(),
-        "wall_s_timed": wall, "host_setup_s": host_s, "first_solve_with_uploads_s": upload_s, "cpu_baseline": cpu,
+        "gpu_launches": int(launches), "schedule": schedule, "roofline": roof, "kernels_ms_per_step": kernels,
+        "clocks": clk.summary(), "wall_s_timed": wall, "host_setup_s": host_s, "first_solve_with_uploads_s": upload_s, "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)
 
@@ -432,6 +433,7 @@ def run_cubic(args):
         ms, launches = ctx.region_end()
         wall = time.perf_counter() - w0
     phases = plan.last_phases()
+    schedule = ctx.last_schedule()
     fallbacks, max_iters = plan.last_stats()
     steps_job, steps_batch = plan.last_refine_steps()
     ctx.region_begin()
@@ -480,7 +482,7 @@ def run_cubic(args):
                      "max_abs_dT_fwd_vs_grad": float(np.abs(t_g - t_mixed).max()),
                      "status_ok": bool((st_g == 0).all()), "sites": int(sys_.system.n)},
         "status_ok": bool((st_mixed == 0).all() and (st_dbl == 0).all()),
-        "gpu_launches": int(launches), "roofline": roof, "kernels_ms_per_step": kernels, "clocks": clk.summary(),
+        "gpu_launches": int(launches), "schedule": schedule, "roofline": roof, "kernels_ms_per_step": kernels, "clocks": clk.summary(),
         "wall_s_timed": wall, "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)
@@ -599,6 +601,7 @@ def run_ours(args):
         wall = time.perf_counter() - w0
     barrier(dist, torch)
     ms_max = reduce_max(ms, dist, torch)
+    schedule = ctx.last_schedule()  # the autotuner's choice for this batch, graph replays so far
     fallbacks, max_iters = plan.last_stats()
     iters, perturbed, jstat = plan.last_job_info()
     # Plain FP64 GPU path on the same batch (one step after one warm-up).
@@ -714,6 +717,7 @@ def run_ours(args):
         "e2e": {"value": nsolve * args.steps / (e2e_ms * 1e-3), "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "wall_s": e2e_wall},
         "gpu_launches": int(launches),
+        "schedule": schedule,
         "inputs_on_device": gen,
         "roofline": roof,
         "kernels_ms_per_step": kernels,
