@@ -29,6 +29,7 @@
 #include "sweep.cuh"
 #include "disorder.cuh"
 #include "leadsig.cuh"
+#include "tcgemm.cuh"
 
 using namespace caroli;
 
@@ -236,9 +237,10 @@ struct RefineBufs {
   Buf rdesc, rx, rr, rd, rtb, rhb, rt, rerr, rdone, rgx, stasks;
   Buf gV, gZ, gH, gg, gcs, gsn, gy, gbeta, gcol, gflags;
   Buf segs, ctasks, ccount, cjobs;  // task lists compacted to the solves still iterating
+  Buf tg_fr, tg_tasks, tg_stage;    // tensor-core sweeps of many-column solves (tcgemm.cuh)
   // The vectors (one column per channel; the bulk of a mixed batch's memory besides the fronts).
   void release_vectors() {
-    for (Buf* b : {&rx, &rr, &rd, &rtb, &rhb, &rgx, &gV, &gZ}) b->release();
+    for (Buf* b : {&rx, &rr, &rd, &rtb, &rhb, &rgx, &gV, &gZ, &tg_stage}) b->release();
   }
 };
 
@@ -581,6 +583,144 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
   }
   SliceTask* dst_tasks = static_cast<SliceTask*>(rb.stasks.get(sth.size() * sizeof(SliceTask)));
   CK(cudaMemcpyAsync(dst_tasks, sth.data(), sth.size() * sizeof(SliceTask), cudaMemcpyHostToDevice, s));
+  // Solves with many columns (TG_MIN_COLS or more channels) sweep their large fronts and the root
+  // as tensor-core GEMMs (tcgemm.cuh): per level, the fronts' right-hand sides are gathered into a
+  // staging block, then one GEMM task per output block. The lists hold every large front of every
+  // such job; tasks of finished solves exit at once.
+  const bool wide = cmax >= TG_MIN_COLS;
+  const int nlev_w = (int)lr.size();
+  struct WideLevel { size_t fr0 = 0, nfr = 0, fw0 = 0, nfw = 0, bw0 = 0, nbw = 0; int max_m = 1; };
+  std::vector<WideLevel> wl(nlev_w);
+  TGFront* dtg_fr = nullptr;
+  TGTask* dtg_tasks = nullptr;
+  size_t root_fr0 = 0, root_nfr = 0, root_t0 = 0;
+  int root_m = 1;
+  if (wide) {
+    const std::vector<Task>& htasks = ctx->tcache.tasks;
+    std::vector<TGFront> frs;
+    std::vector<TGTask> tgs;
+    std::vector<size_t> stage_off_f, stage_off_b;  // per entry of frs (forward and backward stages)
+    size_t stage_need = 1;
+    // Fronts first (forward gathers, then backward gathers), then tasks (forward, backward, root).
+        for (int L = 0; L < nlev_w; ++L) {
+      size_t off = 0;
+      WideLevel& W = wl[L];
+      W.fr0 = frs.size();
+      for (size_t q = lr[L].first; q < lr[L].first + lr[L].count; ++q) {
+        const Task& tk = htasks[q];
+        const RefineDesc& R = rdh[tk.job];
+        if (R.c == 0) continue;
+        const FrontDesc& f = specs[begin + tk.job].plan->host.fronts[tk.front];
+        frs.push_back({drd + tk.job, tk.fd, nullptr});
+        stage_off_f.push_back(off);
+        off += (size_t)f.n * R.c;
+        W.max_m = std::max(W.max_m, f.n);
+      }
+      W.nfr = frs.size() - W.fr0;
+      stage_need = std::max(stage_need, off);
+    }
+    for (size_t j = 0; j < cj; ++j) {
+      const RefineDesc& R = rdh[j];
+      if (R.c == 0) continue;
+      root_m = std::max(root_m, specs[begin + j].plan->host.fronts[R.root_front].n);
+    }
+    // Root gathers: one per wide job, stage m x c each.
+    root_fr0 = frs.size();
+    size_t roff = 0;
+    for (size_t j = 0; j < cj; ++j) {
+      const RefineDesc& R = rdh[j];
+      if (R.c == 0) continue;
+      const FrontPlan& P = specs[begin + j].plan->host;
+      frs.push_back({drd + j, specs[begin + j].plan->fronts + P.root, nullptr});
+      stage_off_f.push_back(roff);
+      roff += (size_t)P.fronts[P.root].n * R.c;
+    }
+    root_nfr = frs.size() - root_fr0;
+    stage_need = std::max(stage_need, roff);
+    float2* stage = static_cast<float2*>(rb.tg_stage.get(stage_need * sizeof(float2)));
+    for (size_t e = 0; e < frs.size(); ++e) frs[e].stage = stage + stage_off_f[e];
+    for (int L = 0; L < nlev_w; ++L) {
+      WideLevel& W = wl[L];
+      W.fw0 = tgs.size();
+      size_t e = W.fr0;
+      for (size_t q = lr[L].first; q < lr[L].first + lr[L].count; ++q) {
+        const Task& tk = htasks[q];
+        const RefineDesc& R = rdh[tk.job];
+        if (R.c == 0) continue;
+        const FrontDesc& f = specs[begin + tk.job].plan->host.fronts[tk.front];
+        const float2* F = R.arena + f.arena_off;
+        const int ne = f.ne, nb = f.n - f.ne;
+        TGTask a{};
+        a.rd = drd + tk.job; a.b = frs[e].stage; a.ldb = f.n; a.n = R.c; a.k = ne; a.sign = 1.f;
+        if (ne > 0) {  // t = F11^-1 z_e
+          TGTask t1 = a;
+          t1.a = F; t1.lda = f.n; t1.c = R.tb + f.toff; t1.ldc = R.sum_ne; t1.m = ne;
+          tgs.push_back(t1);
+        }
+        if (nb > 0) {  // h = z_b + W z_e
+          TGTask t2 = a;
+          t2.a = F + ne; t2.lda = f.n; t2.add = frs[e].stage + ne; t2.ldadd = f.n;
+          t2.c = R.hb + f.hoff; t2.ldc = R.sum_nb; t2.m = nb;
+          tgs.push_back(t2);
+        }
+        ++e;
+      }
+      W.nfw = tgs.size() - W.fw0;
+      W.bw0 = tgs.size();
+      e = W.fr0;
+      for (size_t q = lr[L].first; q < lr[L].first + lr[L].count; ++q) {
+        const Task& tk = htasks[q];
+        const RefineDesc& R = rdh[tk.job];
+        if (R.c == 0) continue;
+        const FrontDesc& f = specs[begin + tk.job].plan->host.fronts[tk.front];
+        const int ne = f.ne, nb = f.n - f.ne;
+        if (ne > 0) {  // x_e = t - X x_b (x_b staged with leading dimension nb)
+          TGTask t3{};
+          t3.rd = drd + tk.job; t3.a = R.arena + f.arena_off + (size_t)ne * f.n; t3.lda = f.n;
+          t3.b = frs[e].stage; t3.ldb = std::max(nb, 1); t3.add = R.tb + f.toff; t3.ldadd = R.sum_ne;
+          t3.c = nullptr; t3.crow = R.srows + f.var_off; t3.ldc = R.nblk; t3.m = ne; t3.n = R.c; t3.k = nb;
+          t3.sign = -1.f;
+          tgs.push_back(t3);
+        }
+        ++e;
+      }
+      W.nbw = tgs.size() - W.bw0;
+    }
+    root_t0 = tgs.size();
+    for (size_t e = root_fr0; e < root_fr0 + root_nfr; ++e) {
+      const size_t j = (size_t)(frs[e].rd - drd);
+      const RefineDesc& R = rdh[j];
+      const FrontPlan& P = specs[begin + j].plan->host;
+      const int m = P.fronts[P.root].n;
+      TGTask t4{};
+      t4.rd = drd + j; t4.a = R.root; t4.lda = m; t4.adj = R.adjoint; t4.b = frs[e].stage; t4.ldb = m;
+      t4.c = nullptr; t4.crow = R.srows + P.fronts[P.root].var_off; t4.ldc = R.nblk; t4.m = m; t4.n = R.c; t4.k = m;
+      t4.sign = 1.f;
+      tgs.push_back(t4);
+    }
+    dtg_fr = static_cast<TGFront*>(rb.tg_fr.get(std::max<size_t>(frs.size(), 1) * sizeof(TGFront)));
+    dtg_tasks = static_cast<TGTask*>(rb.tg_tasks.get(std::max<size_t>(tgs.size(), 1) * sizeof(TGTask)));
+    if (!frs.empty()) CK(cudaMemcpyAsync(dtg_fr, frs.data(), frs.size() * sizeof(TGFront), cudaMemcpyHostToDevice, s));
+    if (!tgs.empty()) CK(cudaMemcpyAsync(dtg_tasks, tgs.data(), tgs.size() * sizeof(TGTask), cudaMemcpyHostToDevice, s));
+  }
+  // GEMM launches of a task range: grid (column tiles, row tiles of the largest m, tasks).
+  auto tg_gemm = [&](size_t t0, size_t nt, int max_m, int src, int dst, KClass cls) {
+    const unsigned gx = (unsigned)((cmax + TG_COLS - 1) / TG_COLS), gy = (unsigned)((max_m + TG_ROWS - 1) / TG_ROWS);
+    in_pieces(nt, [&](size_t f0, size_t c) {
+      launch(cls, 0.0, 0.0, [&] {
+        tc_sweep_gemm_kernel<<<dim3(gx, gy, (unsigned)c), TG_THREADS, TG_SMEM, s>>>(dtg_tasks + t0 + f0, src, dst,
+                                                                                   ctx->tc_wait_limit);
+      });
+    });
+  };
+  auto tg_gather = [&](bool fwd, size_t f0r, size_t nf, int src, int dst, KClass cls) {
+    in_pieces(nf, [&](size_t f0, size_t c) {
+      launch(cls, 0.0, 0.0, [&] {
+        if (fwd) tg_gather_fwd_kernel<<<dim3(64, (unsigned)c), 256, 0, s>>>(dtg_fr + f0r + f0, src);
+        else tg_gather_bwd_kernel<<<dim3(64, (unsigned)c), 256, 0, s>>>(dtg_fr + f0r + f0, src, dst);
+      });
+    });
+  };
   // Launches the slice products of one set (all jobs); flops for the accounting.
   auto slice_products = [&](size_t set, KClass cls) {
     double fl = 0.0;
@@ -659,6 +799,13 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
       const int nt = hcount[3 * L], nm = hcount[3 * L + 1], nr = hcount[3 * L + 2];
       if (nt) warp_fwd(std::integral_constant<int, 1>{}, lr[L].tiny0, nt);
       if (nm) warp_fwd(std::integral_constant<int, 3>{}, lr[L].mid0, nm);
+      if (wide) {
+        if (wl[L].nfr) {
+          tg_gather(true, wl[L].fr0, wl[L].nfr, src, dst, K_REF_FWD);
+          tg_gemm(wl[L].fw0, wl[L].nfw, wl[L].max_m, src, dst, K_REF_FWD);
+        }
+        continue;
+      }
       if (!nr) continue;
       const size_t sm = (size_t)std::max(1, lr[L].max_ne) * CB * sizeof(float2);
       const unsigned tiles = (unsigned)((lr[L].max_n + SW_ROWS - 1) / SW_ROWS);
@@ -670,16 +817,28 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
       });
     }
     const int nj = hcount[nseg];
-    in_pieces((size_t)nj, [&](size_t f0, size_t c) {
-      launch(K_REF_ROOT, 0.0, 0.0, [&] {
-        sweep_root_kernel<CB><<<dim3(cchunks, (unsigned)c), 256, (size_t)max_root * CB * sizeof(float2), s>>>(
-            drd, cjobs + f0, src, dst);
+    if (wide) {
+      tg_gather(true, root_fr0, root_nfr, src, dst, K_REF_ROOT);
+      tg_gemm(root_t0, root_nfr, root_m, src, dst, K_REF_ROOT);
+    } else {
+      in_pieces((size_t)nj, [&](size_t f0, size_t c) {
+        launch(K_REF_ROOT, 0.0, 0.0, [&] {
+          sweep_root_kernel<CB><<<dim3(cchunks, (unsigned)c), 256, (size_t)max_root * CB * sizeof(float2), s>>>(
+              drd, cjobs + f0, src, dst);
+        });
       });
-    });
+    }
     for (int L = nlev - 1; L >= 0; --L) {
       const int nt = hcount[3 * L], nm = hcount[3 * L + 1], nr = hcount[3 * L + 2];
       if (nt) warp_bwd(std::integral_constant<int, 1>{}, lr[L].tiny0, nt);
       if (nm) warp_bwd(std::integral_constant<int, 3>{}, lr[L].mid0, nm);
+      if (wide) {
+        if (wl[L].nfr) {
+          tg_gather(false, wl[L].fr0, wl[L].nfr, src, dst, K_REF_BWD);
+          tg_gemm(wl[L].bw0, wl[L].nbw, wl[L].max_m, src, dst, K_REF_BWD);
+        }
+        continue;
+      }
       if (!nr) continue;
       const size_t sm = (size_t)std::max(1, lr[L].max_n) * CB * sizeof(float2);
       const unsigned tiles = (unsigned)((std::max(1, lr[L].max_ne) + SW_ROWS - 1) / SW_ROWS);
@@ -1824,7 +1983,7 @@ int caroli_ctx_create(int device_ordinal, caroli_ctx** out) {
     ctx->mem_budget = free_b / 2;
     int optin = 0;
     CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_ordinal));
-    for (auto* k : {(const void*)tc_update_kernel,
+    for (auto* k : {(const void*)tc_update_kernel, (const void*)tc_sweep_gemm_kernel,
                     (const void*)small_front_kernel<double, false>, (const void*)small_front_kernel<float, false>,
                     (const void*)small_front_kernel<double, true>, (const void*)small_front_kernel<float, true>,
                     (const void*)inv_finish_kernel<double>, (const void*)inv_finish_kernel<float>,

@@ -79,3 +79,50 @@ def test_cubic_64x32x32_mixed_and_gradient():
     for i, a in enumerate(sites):
         fd = (tf[2 * i] - tf[2 * i + 1]) / (2 * h)
         assert abs(dv[0, a] - fd) <= 1e-4 * scale + 1e-9, (a, dv[0, a], fd)
+
+
+def test_tensor_core_sweeps_many_channels():
+    """Solves with many lead channels sweep their large fronts and the root as tensor-core GEMMs
+    (tcgemm.cuh; from 32 columns on). A 24 x 12 x 12 cubic wire (about 90 channels) in mixed
+    precision, forward T and the adjoint gradient, against the oracle and the FP64 path."""
+    from caroli_gb300.nested import context
+
+    sys_ = cubic_wire(24, 12, 12, configs=2)
+    sigmas = [sys_.self_energies(e) for e in (-0.7, 0.4)]
+    S, C = [s for s in sigmas for _ in range(2)], [0, 1, 0, 1]
+    assert min(s.w_right()[0].shape[1] for s in sigmas) >= 32
+    ctx = context(0)
+    try:
+        ctx.set_mixed_max_channels(100000)
+        tm, st, _ = sys_.solve_batch(S, C, Precision.MIXED)
+        assert (st == 0).all() and sys_.plan().last_stats()[0] == 0
+        tg, stg, dv, _ = sys_.transmissions_with_grad(S, C)
+        assert (stg == 0).all()
+    finally:
+        ctx.set_mixed_max_channels(96)
+    t64, st64, _ = sys_.solve_batch(S, C, Precision.DOUBLE)
+    for k, (s, c) in enumerate(zip(S, C)):
+        ref = oracle_T(sys_, s, config=c)
+        assert abs(tm[k] - ref) <= 1e-8 * (1 + abs(ref)), (k, tm[k], ref)
+        assert abs(tg[k] - tm[k]) <= 1e-12 * (1 + abs(ref))
+        assert abs(t64[k] - ref) <= 1e-10 * (1 + abs(ref))
+    # The uniform-shift sum rule of the gradient: Σ_a dT/dV_a = -dT/dE at fixed self-energies.
+    h = 1e-6
+    plan = sys_.plan()
+    vals = []
+    for c in (0, 1):
+        base = sys_.system.values[c]
+        for sgn in (1, -1):
+            v = base.copy()
+            for a in range(sys_.system.n):
+                lo, hi = sys_.system.row_ptr[a], sys_.system.row_ptr[a + 1]
+                v[lo + int(np.nonzero(sys_.system.cols[lo:hi] == a)[0][0])] += sgn * h
+            vals.append(v)
+    plan.upload_values(np.stack(vals))
+    try:
+        tf, stf, _ = sys_.solve_batch([sigmas[0]] * 4, [0, 1, 2, 3], Precision.DOUBLE)
+    finally:
+        plan.upload_values(np.stack(sys_.system.values))
+    for c in (0, 1):
+        fd = (tf[2 * c] - tf[2 * c + 1]) / (2 * h)
+        assert abs(dv[c].sum() - fd) <= 1e-4 * abs(fd) + 1e-8, (c, dv[c].sum(), fd)
