@@ -197,6 +197,12 @@ struct Buf {
     p = nullptr;
     bytes = 0;
   }
+  // As get, but also gives back most of an allocation far larger than needed (a batch in another
+  // precision left it), so that buffers grown by different batches do not add up.
+  void* fit(size_t need) {
+    if (bytes > 2 * need + (size_t(64) << 20)) release();
+    return get(need);
+  }
   ~Buf() { cudaFree(p); }
 };
 
@@ -1201,8 +1207,8 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
       max_levels = std::max(max_levels, P.levels);
       parts_per_job = std::max(parts_per_job, (size_t)(P.nr + 7) / 8);
     }
-    V* arena = static_cast<V*>(ctx->arena.get(std::max<size_t>(aoff, 1) * vb));
-    VR* rarena = static_cast<VR*>(ctx->root_arena.get(std::max<size_t>(roff, 1) * vr));
+    V* arena = static_cast<V*>(ctx->arena.fit(std::max<size_t>(aoff, 1) * vb));
+    VR* rarena = static_cast<VR*>(ctx->root_arena.fit(std::max<size_t>(roff, 1) * vr));
     uint8_t* fail = static_cast<uint8_t*>(ctx->fail.get(std::max<size_t>(foff, 1)));
     int32_t* status = static_cast<int32_t*>(ctx->status.get(cj * sizeof(int32_t)));
     int* pert = static_cast<int*>(ctx->pert.get(cj * sizeof(int)));
@@ -1449,7 +1455,7 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
     // Factorization level by level, then the root front and its inverse: a fixed launch sequence
     // for a given batch (task lists, scratch, schedule).
     auto factor_all = [&]() {
-      CK(cudaEventRecord(ctx->ev0, s));
+      CK(cudaEventRecordWithFlags(ctx->ev0, s, cudaEventRecordExternal));
       // Factorization, level by level.
       for (int L = 0; L < max_levels; ++L) {
         const Level& lv = levels[L];
@@ -1491,7 +1497,7 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
           (void)mt;
         }
       }
-      CK(cudaEventRecord(ctx->evf, s));
+      CK(cudaEventRecordWithFlags(ctx->evf, s, cudaEventRecordExternal));
       // Root front in TR, then its inverse. The reference's root LU has no stability test (a zero
       // pivot means a singular root); in mixed precision tiny root pivots are perturbed like the
       // fronts' (the refinement corrects).
@@ -1503,7 +1509,7 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
       });
       inverse(TR{}, rinv0, cj, max_root, max_root, mixed ? Prec<T>::tol * 1e-2 : 0.0, perturb, K_ROOT_INV, root_flops,
               K_ROOT_INV, 0.0, 0.0);
-      CK(cudaEventRecord(ctx->evr, s));
+      CK(cudaEventRecordWithFlags(ctx->evr, s, cudaEventRecordExternal));
     };
     // A batch seen twice in a row (same plans, schedule and scratch) is captured as a CUDA graph
     // on its second run and replayed afterwards: one launch in place of the level-by-level
