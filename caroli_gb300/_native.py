@@ -158,14 +158,15 @@ class Context:
         self.check(self.lib.caroli_set_graphs(self.h, 1 if enable else 0))
 
     def last_schedule(self):
-        """The last batch's schedule: small_max, tensor_cores, tuned, the trial times (ms) of
-        (48, 64, 96) x (tensor cores, CUDA cores), graph replays and captures so far."""
+        """The last batch's schedule: small_max, the update mode (2: tensor cores with the split
+        Schur GEMM, 1: tensor-core rank-32 updates, 0: CUDA cores), tuned, the trial times (ms) of
+        (48, 64, 96) x (2, 1, 0), graph replays and captures so far."""
         sm, tc, tu = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
-        ms = np.zeros(6)
+        ms = np.zeros(9)
         rep, cap = ctypes.c_int64(), ctypes.c_int64()
         self.check(self.lib.caroli_last_schedule(self.h, ctypes.byref(sm), ctypes.byref(tc), ctypes.byref(tu), ptr(ms),
                                                  ctypes.byref(rep), ctypes.byref(cap)))
-        return {"small_max": sm.value, "tensor_cores": bool(tc.value), "tuned": bool(tu.value),
+        return {"small_max": sm.value, "update_mode": tc.value, "tuned": bool(tu.value),
                 "trial_ms": [None if np.isnan(x) else float(x) for x in ms], "graph_replays": rep.value,
                 "graph_captures": cap.value}
 

@@ -34,6 +34,9 @@ struct InvTask {
   void* bt;         // f32 matrices: the same rows as the tensor-core operand B' (see tc_update_kernel)
   double* scale2;   // max |a_ij|^2 of the input
   int32_t* bad;     // set when a pivot is refused
+  int32_t ncol;     // columns the sweep transforms (n; npiv when the rest columns are formed by one
+                    // GEMM afterwards, see schur_split in the engine)
+  int32_t pad;
 };
 
 constexpr int GJ_KB = 32;
@@ -190,7 +193,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) inv_panel_kernel(
   // 3. Pivot rows of the rest columns into Y; displaced rows into place. A warp per column.
   V* Y = static_cast<V*>(t.y);
   const int nd = ndisp;
-  for (int j = w; j < n; j += nw) {
+  for (int j = w; j < t.ncol; j += nw) {
     if (j >= k0 && j < k0 + kb) continue;
     V* Aj = A + (int64_t)j * ld;
     V yv = cx<V>(0.0, 0.0), dv = cx<V>(0.0, 0.0);
@@ -225,7 +228,7 @@ __global__ void __launch_bounds__(256) inv_update_kernel(const InvTask* __restri
   if (k0 >= t.npiv) return;
   if (*t.bad) return;
   const int kb = min(GJ_KB, t.npiv - k0);
-  const int rest = n - kb;
+  const int rest = t.ncol - kb;
   const int i0 = blockIdx.x * 64, r0 = blockIdx.y * 64;
   if (i0 >= n || r0 >= rest) return;
   V* A = static_cast<V*>(t.a);
@@ -312,7 +315,7 @@ __global__ void __launch_bounds__(TCU_THREADS, 2) tc_update_kernel(const InvTask
   if (k0 >= t.npiv || t.bt == nullptr) return;
   if (*t.bad) return;
   const int kb = min(GJ_KB, t.npiv - k0);
-  const int rest = n - kb;
+  const int rest = t.ncol - kb;
   const int i0 = blockIdx.x * TCU_ROWS;
   if (i0 >= n || rest <= 0) return;
   const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;

@@ -287,6 +287,10 @@ struct TaskLevel {
   int max_tiny_n = 0;
   double upd_flops = 0, upd_bytes = 0;  // the rank-kb updates of the blocked sweep
   double pan_flops = 0;                 // its panel sweeps (kb steps over n rows of kb columns)
+  // Split Schur update (f32 on the tensor cores): F12 copies and the [X; S] GEMM tasks of the level.
+  size_t f12_0 = 0, f12_n = 0, sg0 = 0, sg_n = 0;
+  int sg_max_m = 1, sg_max_cols = 1;
+  double sg_flops = 0;
 };
 
 // The task lists of the last batch (see run_jobs).
@@ -294,7 +298,14 @@ struct TaskCache {
   bool valid = false;
   std::vector<uint64_t> plans;  // identities of the chunk's plans
   int tsize = 0, trsize = 0, max_levels = 0, small_max = 0;
-  bool mixed = false;
+  bool mixed = false, split = false;
+  std::vector<F12Copy> f12;      // split Schur update: F12 copies, stage offsets (elements)
+  std::vector<size_t> f12_off;
+  std::vector<size_t> f12_inv;   // the InvTask (its bad flag) of each copy
+  std::vector<TGTask> sgt;       // and the GEMM tasks (pointers into the arena and the stage)
+  std::vector<std::pair<size_t, int>> sgt_stage;  // per task: copy index, 0 (X) or 1 (S)
+  size_t f12_elems = 0;
+  const void *f12_stage = nullptr, *f12_dev = nullptr, *sgt_dev = nullptr, *status_dev = nullptr;
   const void *arena = nullptr, *rarena = nullptr;
   std::vector<Task> tasks;
   std::vector<TaskLevel> levels;
@@ -309,12 +320,17 @@ struct TaskCache {
 
 // The autotuner's choice for a plan set: the largest f32 front factored by one CTA in shared
 // memory (fronts above it take the panel sweep and the rank-32 updates), whether those updates run
-// on the tensor cores, and the factorization times the trials measured.
+// on the tensor cores, whether the Schur complement of those fronts is one tensor-core GEMM after
+// panels restricted to the pivot columns, and the factorization times the trials measured.
+constexpr int TUNE_CANDIDATES = 9;
 struct TuneChoice {
   int small_max = SMALL_MAX_F32;
   bool tensor_cores = true;
+  bool split = true;
   bool tuned = false;
-  double ms[6] = {0, 0, 0, 0, 0, 0};  // per candidate (small_max 48 / 64 / 96 x tensor cores on / off)
+  // Per candidate: small_max 48 / 64 / 96 x (tensor cores with the split Schur GEMM, tensor cores
+  // rank-32 updates only, CUDA cores).
+  double ms[TUNE_CANDIDATES] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
 };
 
 // A captured factorization (every level's launches, the root assembly and inverse) and what it
@@ -384,6 +400,8 @@ struct caroli_ctx {
   bool use_graphs = true;                       // replay a repeated batch's factorization as a CUDA graph
   int small_max_f32 = SMALL_MAX_F32;            // f32 fronts up to this size: one CTA each (else panel + update)
   bool tc_choice = true;                        // the autotuner's tensor-core choice (with tensor_cores set)
+  bool split_choice = true;                     // f32 Schur complements as one tensor-core GEMM per front
+  Buf f12_stage, f12_list, sgt_list;            // its F12 copies and task lists
   bool factor_only = false;                     // run_jobs stops after the root inverse (tuning trials)
   std::map<std::vector<uint64_t>, TuneChoice> tuned;  // per plan set and precision
   TuneChoice last_tune;                               // the choice the last batch ran with
@@ -1242,11 +1260,14 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
     using Level = TaskLevel;
     TaskCache& tc = ctx->tcache;
     const int small_max = sizeof(T) == 8 ? SMALL_MAX_F64 : ctx->small_max_f32;
+    // Split Schur update: the panel sweeps transform only the pivot columns, then one tensor-core
+    // GEMM per front forms [X; S] = [F11^-1; W] F12 + [0; F22] (f32 fronts below the root).
+    const bool split = std::is_same<T, float>::value && ctx->tensor_cores && ctx->tc_choice && ctx->split_choice;
     std::vector<uint64_t> key_plans(cj);
     for (size_t j = 0; j < cj; ++j) key_plans[j] = specs[begin + j].plan->id;
     const bool hit = tc.valid && tc.plans == key_plans && tc.tsize == (int)sizeof(T) && tc.trsize == (int)sizeof(TR) &&
                      tc.mixed == mixed && tc.arena == (const void*)arena && tc.rarena == (const void*)rarena &&
-                     tc.max_levels == max_levels && tc.small_max == small_max;
+                     tc.max_levels == max_levels && tc.small_max == small_max && tc.split == split;
     std::vector<Task>& tasks = tc.tasks;
     std::vector<Level>& levels = tc.levels;
     std::vector<InvTask>& inv = tc.inv;  // large fronts' pivot blocks per level, then the roots
@@ -1263,6 +1284,8 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
     double& trace_flops = tc.trace_flops;
     if (!hit) {
     tc.valid = false;
+    tc.f12.clear(); tc.f12_off.clear(); tc.f12_inv.clear(); tc.sgt.clear(); tc.sgt_stage.clear();
+    tc.f12_elems = 0;
     tasks.clear();
     levels.assign(max_levels, Level{});
     inv.clear();
@@ -1314,6 +1337,8 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
       lv.small_n = tasks.size() - lv.small0;
       lv.large0 = tasks.size();
       lv.inv0 = inv.size();
+      lv.f12_0 = tc.f12.size();
+      lv.sg0 = tc.sgt.size();
       for (size_t j = 0; j < cj; ++j) {
         const auto& fr = specs[begin + j].plan->host.fronts;
         const FrontDesc* dfr = specs[begin + j].plan->fronts;
@@ -1326,11 +1351,16 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
             lv.inv_flops += 8.0 / 3 * ne * ne * ne;
             lv.gemm0_flops += 8 * ne * ne * nb;
             lv.gemm1_flops += 8 * nb * nb * ne;
+            const double ncol = split ? ne : (double)fr[k].n;  // columns the sweep transforms
             for (int k0 = 0; k0 < fr[k].ne; k0 += GJ_KB) {
               const double kb = std::min(GJ_KB, fr[k].ne - k0), nn = fr[k].n;
-              lv.upd_flops += 8.0 * nn * (nn - kb) * kb;  // complex n x kb times kb x (n - kb)
-              lv.upd_bytes += 2.0 * nn * (nn - kb) * vb;  // the rest columns read and written
+              lv.upd_flops += 8.0 * nn * (ncol - kb) * kb;  // complex n x kb times kb x (ncol - kb)
+              lv.upd_bytes += 2.0 * nn * (ncol - kb) * vb;  // the rest columns read and written
               lv.pan_flops += 8.0 * nn * kb * kb;
+            }
+            if (split) {
+              lv.upd_flops += 8.0 * fr[k].n * ne * nb;                           // [X; S] = [F11^-1; W] F12
+              lv.upd_bytes += ((double)fr[k].n * ne + 3.0 * ne * nb + 2.0 * nb * nb) * vb;  // A, F12 twice, X, F22
             }
             lv.asm_bytes += (double)fr[k].n * fr[k].n * vb;
             if (fr[k].ne > 0) {
@@ -1339,8 +1369,31 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
               it.ld = fr[k].n;
               it.n = fr[k].n;
               it.npiv = fr[k].ne;
+              it.ncol = split ? fr[k].ne : fr[k].n;
               it.job = (int32_t)j;
               it.front = (int32_t)k;
+              if (split && fr[k].n > fr[k].ne) {
+                const int fne = fr[k].ne, fnb = fr[k].n - fr[k].ne;
+                float2* fa = reinterpret_cast<float2*>(arena + arena_off[j] + fr[k].arena_off);
+                const size_t ci = tc.f12.size();
+                tc.f12.push_back({fa, nullptr, fr[k].n, fne, nullptr});
+                tc.f12_off.push_back(tc.f12_elems);
+                tc.f12_inv.push_back(inv.size());
+                tc.f12_elems += (size_t)fne * fnb;
+                TGTask tx{};
+                tx.a = fa; tx.lda = fr[k].n; tx.ldb = fne; tx.c = fa + (size_t)fne * fr[k].n; tx.ldc = fr[k].n;
+                tx.m = fne; tx.n = fnb; tx.k = fne; tx.sign = 1.f; tx.job = (int32_t)j;
+                TGTask ts = tx;
+                ts.a = fa + fne; ts.add = fa + fne + (size_t)fne * fr[k].n; ts.ldadd = fr[k].n;
+                ts.c = fa + fne + (size_t)fne * fr[k].n; ts.m = fnb;
+                tc.sgt.push_back(tx);
+                tc.sgt_stage.push_back({ci, 0});
+                tc.sgt.push_back(ts);
+                tc.sgt_stage.push_back({ci, 1});
+                lv.sg_max_m = std::max(lv.sg_max_m, std::max(fne, fnb));
+                lv.sg_max_cols = std::max(lv.sg_max_cols, fnb);
+                lv.sg_flops += 8.0 * fr[k].n * (double)fne * fnb;
+              }
               inv_piv_off.push_back(inv_piv);
               inv_y_off.push_back(inv_y);
               inv_bt_off.push_back(vb == sizeof(float2) ? inv_bt : SIZE_MAX);
@@ -1352,6 +1405,8 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
           }
       }
       lv.large_n = tasks.size() - lv.large0;
+      lv.f12_n = tc.f12.size() - lv.f12_0;
+      lv.sg_n = tc.sgt.size() - lv.sg0;
       lv.max_n = std::max(std::max(lv.max_small_n, lv.max_large_n), lv.tiny_n ? TINY_MAX : 0);
     }
     root0 = tasks.size();
@@ -1370,6 +1425,7 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
       it.ld = m;
       it.n = m;
       it.npiv = m;
+      it.ncol = m;
       it.job = (int32_t)j;
       it.front = -1;
       inv_piv_off.push_back(inv_piv);
@@ -1389,8 +1445,12 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
     int32_t* dbad = static_cast<int32_t*>(ctx->ibad.get(std::max<size_t>(inv.size(), 1) * sizeof(int32_t)));
     InvTask* dinv = static_cast<InvTask*>(ctx->inv.get(std::max<size_t>(inv.size(), 1) * sizeof(InvTask)));
     Task* dtasks = static_cast<Task*>(ctx->tasks.get(tasks.size() * sizeof(Task)));
+    float2* f12_stage = static_cast<float2*>(ctx->f12_stage.get(std::max<size_t>(tc.f12_elems, 1) * sizeof(float2)));
+    F12Copy* df12 = static_cast<F12Copy*>(ctx->f12_list.get(std::max<size_t>(tc.f12.size(), 1) * sizeof(F12Copy)));
+    TGTask* dsgt = static_cast<TGTask*>(ctx->sgt_list.get(std::max<size_t>(tc.sgt.size(), 1) * sizeof(TGTask)));
     const bool same_scratch = hit && tc.piv == dpiv && tc.y == dy && tc.bt == dbt && tc.scale == dscale &&
-                              tc.bad == dbad && tc.dinv == dinv && tc.dtasks == dtasks;
+                              tc.bad == dbad && tc.dinv == dinv && tc.dtasks == dtasks && tc.f12_stage == f12_stage &&
+                              tc.f12_dev == df12 && tc.sgt_dev == dsgt && tc.status_dev == status;
     if (!same_scratch) {
       for (size_t q = 0; q < inv.size(); ++q) {
         inv[q].piv = dpiv + inv_piv_off[q];
@@ -1402,7 +1462,20 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
       if (!inv.empty())
         CK(cudaMemcpyAsync(dinv, inv.data(), inv.size() * sizeof(InvTask), cudaMemcpyHostToDevice, s));
       CK(cudaMemcpyAsync(dtasks, tasks.data(), tasks.size() * sizeof(Task), cudaMemcpyHostToDevice, s));
+      for (size_t q = 0; q < tc.f12.size(); ++q) {
+        tc.f12[q].stage = f12_stage + tc.f12_off[q];
+        tc.f12[q].bad = dbad + tc.f12_inv[q];
+      }
+      for (size_t q = 0; q < tc.sgt.size(); ++q) {
+        tc.sgt[q].b = f12_stage + tc.f12_off[tc.sgt_stage[q].first];
+        tc.sgt[q].status = status;
+      }
+      if (!tc.f12.empty())
+        CK(cudaMemcpyAsync(df12, tc.f12.data(), tc.f12.size() * sizeof(F12Copy), cudaMemcpyHostToDevice, s));
+      if (!tc.sgt.empty())
+        CK(cudaMemcpyAsync(dsgt, tc.sgt.data(), tc.sgt.size() * sizeof(TGTask), cudaMemcpyHostToDevice, s));
       tc.piv = dpiv; tc.y = dy; tc.bt = dbt; tc.scale = dscale; tc.bad = dbad; tc.dinv = dinv; tc.dtasks = dtasks;
+      tc.f12_stage = f12_stage; tc.f12_dev = df12; tc.sgt_dev = dsgt; tc.status_dev = status;
     }
     tc.plans = key_plans;
     tc.tsize = (int)sizeof(T);
@@ -1412,6 +1485,7 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
     tc.rarena = rarena;
     tc.max_levels = max_levels;
     tc.small_max = small_max;
+    tc.split = split;
     tc.valid = true;
 
     // Batched blocked inverse of `count` matrices starting at dinv + first, largest n.
@@ -1494,6 +1568,22 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
           const size_t ninv = (L + 1 < max_levels ? levels[L + 1].inv0 : rinv0) - lv.inv0;
           inverse(T{}, lv.inv0, ninv, lv.max_large_n, lv.max_large_ne, Prec<T>::tol, perturb, K_PANEL, lv.pan_flops,
                   K_UPDATE, lv.upd_flops, lv.upd_bytes);
+          if (split && lv.f12_n) {
+            // [X; S] = [F11^-1; W] F12 + [0; F22] of every front of the level on the tensor cores
+            // (its flops and bytes are counted with the level's updates above).
+            in_pieces(lv.f12_n, [&](size_t f0, size_t c) {
+              launch(K_UPDATE, 0.0, 0.0, [&] {
+                f12_copy_kernel<<<dim3(32, (unsigned)c), 256, 0, s>>>(df12 + lv.f12_0 + f0);
+              });
+            });
+            in_pieces(lv.sg_n, [&](size_t f0, size_t c) {
+              launch(K_UPDATE, 0.0, 0.0, [&] {
+                tc_sweep_gemm_kernel<<<dim3((unsigned)((lv.sg_max_cols + TG_COLS - 1) / TG_COLS),
+                                            (unsigned)((lv.sg_max_m + TG_ROWS - 1) / TG_ROWS), (unsigned)c),
+                                       TG_THREADS, TG_SMEM, s>>>(dsgt + lv.sg0 + f0, 0, 0, ctx->tc_wait_limit);
+              });
+            });
+          }
           (void)mt;
         }
       }
@@ -1519,7 +1609,9 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
                        (uint64_t)(ctx->tensor_cores && ctx->tc_choice), (uint64_t)ctx->tc_wait_limit, (uint64_t)cj,
                        (uint64_t)(uintptr_t)djobs,
                        (uint64_t)(uintptr_t)dtasks, (uint64_t)(uintptr_t)dinv, (uint64_t)(uintptr_t)pert,
-                       (uint64_t)(uintptr_t)status, (uint64_t)(uintptr_t)arena, (uint64_t)(uintptr_t)rarena})
+                       (uint64_t)(uintptr_t)status, (uint64_t)(uintptr_t)arena, (uint64_t)(uintptr_t)rarena,
+                       (uint64_t)split, (uint64_t)(uintptr_t)df12, (uint64_t)(uintptr_t)dsgt,
+                       (uint64_t)(uintptr_t)f12_stage})
       gkey.push_back(v);
     FactorGraph& fg = ctx->fgraph;
     if (!ctx->use_graphs || ctx->probe >= 0) {
@@ -1788,6 +1880,7 @@ template <typename TR>
 void apply_tuning(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, Mode mode) {
   ctx->small_max_f32 = SMALL_MAX_F32;
   ctx->tc_choice = true;
+  ctx->split_choice = true;
   if (specs.empty()) return;
   std::vector<uint64_t> key;
   for (const JobSpec& sp : specs) key.push_back(sp.plan->id);
@@ -1800,6 +1893,7 @@ void apply_tuning(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spec
     if (!ctx->autotune || ctx->probe >= 0) {
       ctx->last_tune = TuneChoice{};
       ctx->last_tune.tensor_cores = ctx->tensor_cores;
+      ctx->last_tune.split = ctx->tensor_cores;
       return;
     }
     // Saved accounting of the call (the trials must not show in it).
@@ -1817,20 +1911,22 @@ void apply_tuning(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spec
     ctx->factor_only = true;
     try {
       for (int a = 0; a < 3; ++a)
-        for (int b = 0; b < 2; ++b) {
-          const bool tcv = b == 0;
-          if (tcv && !ctx->tensor_cores) { best.ms[a * 2 + b] = NAN; continue; }
+        for (int b = 0; b < 3; ++b) {
+          const bool tcv = b < 2, spl = b == 0;
+          if (tcv && !ctx->tensor_cores) { best.ms[a * 3 + b] = NAN; continue; }
           ctx->small_max_f32 = cand_small[a];
           ctx->tc_choice = tcv;
+          ctx->split_choice = spl;
           ctx->factor_ms = ctx->root_ms = 0.0;
           std::vector<JobOut> tmp;
           run_jobs<float, TR>(ctx, sys, sample, mode, tmp);
           const double ms = ctx->factor_ms + ctx->root_ms;
-          best.ms[a * 2 + b] = ms;
+          best.ms[a * 3 + b] = ms;
           if (ms < best_ms) {
             best_ms = ms;
             best.small_max = cand_small[a];
             best.tensor_cores = tcv;
+            best.split = spl;
           }
         }
     } catch (...) {
@@ -1847,6 +1943,7 @@ void apply_tuning(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spec
   }
   ctx->small_max_f32 = it->second.small_max;
   ctx->tc_choice = it->second.tensor_cores;
+  ctx->split_choice = it->second.split;
   ctx->last_tune = it->second;
 }
 
@@ -3589,10 +3686,10 @@ int caroli_last_schedule(const caroli_ctx* ctx, int32_t* small_max, int32_t* ten
   if (!ctx) return CAROLI_EINVAL;
   const TuneChoice& t = ctx->last_tune;
   if (small_max) *small_max = t.small_max;
-  if (tensor_cores) *tensor_cores = t.tensor_cores ? 1 : 0;
+  if (tensor_cores) *tensor_cores = !t.tensor_cores ? 0 : (t.split ? 2 : 1);
   if (tuned) *tuned = t.tuned ? 1 : 0;
   if (trial_ms)
-    for (int k = 0; k < 6; ++k) trial_ms[k] = t.ms[k];
+    for (int k = 0; k < TUNE_CANDIDATES; ++k) trial_ms[k] = t.ms[k];
   if (graph_replays) *graph_replays = ctx->graph_replays;
   if (graph_captures) *graph_captures = ctx->graph_captures;
   return CAROLI_OK;
@@ -3798,7 +3895,7 @@ extern "C" int caroli_solve_batch_noalloc(caroli_ctx* ctx, int plan_id, int coun
     size_t po = 0, yo = 0;
     auto add_inv = [&](void* a, int n, int np, int32_t job, int32_t front) {
       InvTask it{};
-      it.a = a; it.ld = n; it.n = n; it.npiv = np; it.job = job; it.front = front;
+      it.a = a; it.ld = n; it.n = n; it.npiv = np; it.ncol = n; it.job = job; it.front = front;
       it.piv = reinterpret_cast<int32_t*>(base + o_piv) + po;
       it.y = reinterpret_cast<double2*>(base + o_y) + yo;
       it.scale2 = reinterpret_cast<double*>(base + o_scale) + inv.size();

@@ -1,11 +1,14 @@
-// Refinement sweeps with many right-hand-side columns on the tcgen05 tensor cores.
+// Complex f32 GEMMs on the tcgen05 tensor cores: the refinement sweeps of solves with many
+// right-hand-side columns, and the Schur complements of large fronts (schur_split in the engine).
 //
 // A solve whose right lead has hundreds of open channels (a 32 x 32-site cubic lead) carries one
 // right-hand side per channel through every sweep, so each large front's sweep is a complex GEMM:
 //   forward   [t; h - z_b] = [F11^-1; W] z_e        (n x ne times ne x c)
 //   backward  x_e = t - X x_b                       (ne x nb times nb x c)
 //   root      x = F_root^-1 z  (or its conjugate transpose for the adjoint)
-// with the right-hand sides gathered into dense staging blocks first (gather kernels below). The
+// with the right-hand sides gathered into dense staging blocks first (gather kernels below); and
+//   Schur     [X; S] = [F11^-1; W] F12 + [0; F22]    (n x ne times ne x nb, F12 staged aside)
+// after the panel sweeps have formed the pivot columns [F11^-1; W]. The
 // product runs as the real GEMM of the 2 x 2 expansion used by tc_update_kernel:
 //     D = A' B'^T,  A'[2i][2k] = Re a, A'[2i][2k+1] = -Im a, A'[2i+1][2k] = Im a, A'[2i+1][2k+1] = Re a,
 //                   B'[j][2k] = Re b[k, j], B'[j][2k+1] = Im b[k, j]
@@ -45,7 +48,8 @@ struct TGTask {
   int64_t lda, ldb, ldadd, ldc;
   int32_t m, n, k, adj;
   float sign;
-  int32_t pad;
+  int32_t job;            // without rd (a factorization product): the solve whose status a timeout sets
+  int32_t* status;
 };
 
 // grid (column tiles, row tiles, tasks), TG_THREADS threads, TG_SMEM dynamic shared memory.
@@ -56,8 +60,8 @@ __global__ void __launch_bounds__(TG_THREADS, 2) tc_sweep_gemm_kernel(const TGTa
   __shared__ __align__(8) uint64_t mma_done;
   __shared__ int abort_flag;
   const TGTask t = tasks[blockIdx.z];
-  RefineDesc& R = *const_cast<RefineDesc*>(t.rd);
-  if (sweep_idle(R, src)) return;
+  RefineDesc* Rp = const_cast<RefineDesc*>(t.rd);
+  if (Rp && sweep_idle(*Rp, src)) return;
   const int i0 = blockIdx.y * TG_ROWS, j0 = blockIdx.x * TG_COLS;
   if (i0 >= t.m || j0 >= t.n) return;
   const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
@@ -143,8 +147,12 @@ __global__ void __launch_bounds__(TG_THREADS, 2) tc_sweep_gemm_kernel(const TGTa
     // the FP64 recomputation.
     if (issued > 0) tc::mbar_wait(&mma_done, (uint32_t)((issued - 1) & 1), TCU_WAIT);
     if (tid == 0) {
-      R.stalled = 1;
-      R.done = 1;
+      if (Rp) {
+        Rp->stalled = 1;
+        Rp->done = 1;
+      } else if (t.status) {
+        t.status[t.job] = ST_TIMEOUT;
+      }
     }
   } else {
     // Epilogue: warp w reads TMEM lane quarter w & 3 (real rows 32 (w & 3) + lane) and column half
@@ -162,7 +170,7 @@ __global__ void __launch_bounds__(TG_THREADS, 2) tc_sweep_gemm_kernel(const TGTa
     }
     tc::tmem_ld_wait();
     if (gi < t.m) {
-      float* cbase = reinterpret_cast<float*>(t.c ? t.c : sweep_dst(R, dst));
+      float* cbase = reinterpret_cast<float*>(t.c ? t.c : sweep_dst(*Rp, dst));
       const int64_t orow = t.crow ? t.crow[gi].var : gi;
       const float* abase = reinterpret_cast<const float*>(t.add);
 #pragma unroll
@@ -216,6 +224,27 @@ __global__ void __launch_bounds__(256) tg_gather_bwd_kernel(const TGFront* __res
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
     const int p = (int)(e % nb), j = (int)(e / nb);
     g.stage[e] = dout[R.srows[f.var_off + f.ne + p].var + (int64_t)j * R.nblk];
+  }
+}
+
+// F12 (the rows of the pivot block, columns ne..n) of every front of a list copied aside, column-
+// major ne x nb: the B operand of the Schur GEMM, whose output X overwrites F12. grid (element
+// chunks, fronts).
+struct F12Copy {
+  const float2* a;  // the front, column-major n x n
+  float2* stage;    // ne x nb
+  int32_t n, ne;
+  const int32_t* bad;  // the front's pivot block was refused: nothing to form
+};
+
+__global__ void __launch_bounds__(256) f12_copy_kernel(const F12Copy* __restrict__ list) {
+  const F12Copy g = list[blockIdx.y];
+  if (g.bad && *g.bad) return;
+  const int nb = g.n - g.ne;
+  const int64_t total = (int64_t)g.ne * nb;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e % g.ne), j = (int)(e / g.ne);
+    g.stage[e] = g.a[i + (int64_t)(g.ne + j) * g.n];
   }
 }
 

@@ -369,10 +369,13 @@ int caroli_set_wait_limit(caroli_ctx* ctx, int64_t polls);
 
 /* The autotuner (default on; no reference counterpart): the first time a set of plans is solved in
  * reduced precision, the f32 factorization of up to 256 of its block solves is timed under each
- * candidate schedule (the largest front factored by one CTA in shared memory: 48, 64 or 96
- * variables, larger ones taking the panel sweep and rank-32 updates; those updates on the tensor
- * cores or the CUDA cores) and the fastest is kept for that plan set and precision. Off: the
- * default schedule (96, tensor cores as caroli_set_tensor_cores). Changing it forgets the choices. */
+ * candidate schedule and the fastest is kept for that plan set and precision. Candidates: the
+ * largest front factored by one CTA in shared memory (48, 64 or 96 variables; larger ones take
+ * the panel sweep and rank-32 updates) x how those larger fronts are updated: (2) on the tensor
+ * cores with the panels restricted to the pivot columns and the Schur complement [X; S] formed by
+ * one GEMM per front, (1) on the tensor cores with rank-32 updates of every column, (0) on the CUDA
+ * cores. Off: the default schedule (96, mode 2 when caroli_set_tensor_cores is on). Changing it
+ * forgets the choices. */
 int caroli_set_autotune(caroli_ctx* ctx, int enable);
 
 /* CUDA graph replay (default on; no reference counterpart): a batch run twice in a row with the
@@ -381,10 +384,10 @@ int caroli_set_autotune(caroli_ctx* ctx, int enable);
  * launch afterwards. */
 int caroli_set_graphs(caroli_ctx* ctx, int enable);
 
-/* The schedule the last batch ran with: small_max and tensor_cores as above, tuned = 1 when the
- * autotuner chose them, trial_ms[6] (may be NULL) the trials' factorization times in ms for
- * (48, 64, 96) x (tensor cores, CUDA cores) (NaN: not tried), and the factorization graphs replayed
- * and captured so far. */
+/* The schedule the last batch ran with: small_max, the update mode as above (tensor_cores = 2, 1
+ * or 0), tuned = 1 when the autotuner chose them, trial_ms[9] (may be NULL) the trials'
+ * factorization times in ms for small_max (48, 64, 96) x mode (2, 1, 0) (NaN: not tried), and the
+ * factorization graphs replayed and captured so far. */
 int caroli_last_schedule(const caroli_ctx* ctx, int32_t* small_max, int32_t* tensor_cores, int32_t* tuned,
                          double* trial_ms, int64_t* graph_replays, int64_t* graph_captures);
 

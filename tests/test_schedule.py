@@ -1,8 +1,9 @@
 """The autotuned factorization schedule and CUDA graph replay of repeated batches.
 
 The autotuner times the f32 factorization of a plan set under each candidate schedule (fronts up
-to 48, 64 or 96 variables in one CTA; rank-32 updates on the tensor cores or the CUDA cores) and
-keeps the fastest; every schedule must give the oracle's T in mixed precision. A batch solved
+to 48, 64 or 96 variables in one CTA; larger fronts' Schur complements as one tensor-core GEMM,
+as rank-32 tensor-core updates, or on the CUDA cores) and keeps the fastest; every schedule must
+give the oracle's T in mixed precision. A batch solved
 again with the same plans and buffers replays its factorization as one CUDA graph; the replay must
 give the same bits as the direct launches.
 """
@@ -27,8 +28,8 @@ def test_autotuner_picks_the_fastest_trial_and_keeps_parity():
     sch = ctx.last_schedule()
     assert sch["tuned"]
     trials = [x for x in sch["trial_ms"] if x is not None]
-    assert len(trials) == 6 and min(trials) > 0
-    idx = [48, 64, 96].index(sch["small_max"]) * 2 + (0 if sch["tensor_cores"] else 1)
+    assert len(trials) == 9 and min(trials) > 0
+    idx = [48, 64, 96].index(sch["small_max"]) * 3 + (2 - sch["update_mode"])
     assert sch["trial_ms"][idx] == min(trials)
     for (s, c), tv in zip(zip(S, C), t):
         assert abs(tv - oracle_T(sys_, s, config=c)) <= 1e-8
