@@ -46,10 +46,15 @@ struct CudaError {
   cudaError_t e;
   const char* what;
 };
+// A failed call's error is also taken out of the runtime's last-error slot (it is not sticky
+// unless the context is lost), so that the next call's launch checks do not report it again.
 #define CK(x)                                             \
   do {                                                    \
     cudaError_t _e = (x);                                 \
-    if (_e != cudaSuccess) throw CudaError{_e, #x};       \
+    if (_e != cudaSuccess) {                              \
+      (void)cudaGetLastError();                           \
+      throw CudaError{_e, #x};                            \
+    }                                                     \
   } while (0)
 
 template <typename T> T* dalloc(size_t count) {
@@ -1528,8 +1533,16 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
     const int perturb = mixed ? 1 : 0;
     // Factorization level by level, then the root front and its inverse: a fixed launch sequence
     // for a given batch (task lists, scratch, schedule).
+    // Phase events: recorded as event nodes when the factorization is captured into a graph (the
+    // external flag is only valid during a capture), so that every replay records them.
+    bool capturing = false;
+    auto record = [&](cudaEvent_t ev) {
+      if (capturing) CK(cudaEventRecordWithFlags(ev, s, cudaEventRecordExternal));
+      else CK(cudaEventRecord(ev, s));
+    };
+    cudaEvent_t ev0 = ctx->ev0, evf = ctx->evf, evr = ctx->evr;
     auto factor_all = [&]() {
-      CK(cudaEventRecordWithFlags(ctx->ev0, s, cudaEventRecordExternal));
+      record(ev0);
       // Factorization, level by level.
       for (int L = 0; L < max_levels; ++L) {
         const Level& lv = levels[L];
@@ -1587,7 +1600,7 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
           (void)mt;
         }
       }
-      CK(cudaEventRecordWithFlags(ctx->evf, s, cudaEventRecordExternal));
+      record(evf);
       // Root front in TR, then its inverse. The reference's root LU has no stability test (a zero
       // pivot means a singular root); in mixed precision tiny root pivots are perturbed like the
       // fronts' (the refinement corrects).
@@ -1599,7 +1612,7 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
       });
       inverse(TR{}, rinv0, cj, max_root, max_root, mixed ? Prec<T>::tol * 1e-2 : 0.0, perturb, K_ROOT_INV, root_flops,
               K_ROOT_INV, 0.0, 0.0);
-      CK(cudaEventRecordWithFlags(ctx->evr, s, cudaEventRecordExternal));
+      record(evr);
     };
     // A batch seen twice in a row (same plans, schedule and scratch) is captured as a CUDA graph
     // on its second run and replayed afterwards: one launch in place of the level-by-level
@@ -1632,13 +1645,17 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
       const int64_t l0 = launch.launches;
       cudaGraph_t graph = nullptr;
       CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      capturing = true;
       try {
         factor_all();
       } catch (...) {
+        capturing = false;
         cudaStreamEndCapture(s, &graph);
         if (graph) cudaGraphDestroy(graph);
+        (void)cudaGetLastError();
         throw;
       }
+      capturing = false;
       CK(cudaStreamEndCapture(s, &graph));
       const cudaError_t ie = cudaGraphInstantiate(&fg.exec, graph, 0);
       cudaGraphDestroy(graph);
