@@ -48,6 +48,7 @@ SIGNATURES = {
     "caroli_set_wait_limit": (ctypes.c_int, [P, ctypes.c_int64]),
     "caroli_set_autotune": (ctypes.c_int, [P, ctypes.c_int]),
     "caroli_set_graphs": (ctypes.c_int, [P, ctypes.c_int]),
+    "caroli_set_schedule": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int]),
     "caroli_last_schedule": (ctypes.c_int, [P, P, P, P, P, P, P]),
     "caroli_solve_multi": (ctypes.c_int, [P, ctypes.c_int, P, P, P, ctypes.c_int, P, P, P]),
     "caroli_scattering_states": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P, P, P, P]),
@@ -152,6 +153,10 @@ class Context:
     def set_autotune(self, enable=True):
         """The f32 factorization's schedule picked per plan set by timing trials (default on)."""
         self.check(self.lib.caroli_set_autotune(self.h, 1 if enable else 0))
+
+    def set_schedule(self, small_max=96, update_mode=1):
+        """The schedule used while the autotuner is off (see caroli_set_schedule)."""
+        self.check(self.lib.caroli_set_schedule(self.h, int(small_max), int(update_mode)))
 
     def set_graphs(self, enable=True):
         """Replay a repeated batch's factorization as a CUDA graph (default on)."""

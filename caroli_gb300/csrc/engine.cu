@@ -331,7 +331,7 @@ constexpr int TUNE_CANDIDATES = 9;
 struct TuneChoice {
   int small_max = SMALL_MAX_F32;
   bool tensor_cores = true;
-  bool split = true;
+  bool split = false;
   bool tuned = false;
   // Per candidate: small_max 48 / 64 / 96 x (tensor cores with the split Schur GEMM, tensor cores
   // rank-32 updates only, CUDA cores).
@@ -405,7 +405,8 @@ struct caroli_ctx {
   bool use_graphs = true;                       // replay a repeated batch's factorization as a CUDA graph
   int small_max_f32 = SMALL_MAX_F32;            // f32 fronts up to this size: one CTA each (else panel + update)
   bool tc_choice = true;                        // the autotuner's tensor-core choice (with tensor_cores set)
-  bool split_choice = true;                     // f32 Schur complements as one tensor-core GEMM per front
+  bool split_choice = false;                    // f32 Schur complements as one tensor-core GEMM per front
+  int fixed_small_max = SMALL_MAX_F32, fixed_mode = 1;  // the schedule without the autotuner
   Buf f12_stage, f12_list, sgt_list;            // its F12 copies and task lists
   bool factor_only = false;                     // run_jobs stops after the root inverse (tuning trials)
   std::map<std::vector<uint64_t>, TuneChoice> tuned;  // per plan set and precision
@@ -756,9 +757,15 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
     for (size_t j = 0; j < cj; ++j) fl += 8.0 * sth[set * per_set + j].m * (double)sth[set * per_set + j].m * sth[set * per_set + j].c;
     if (fl == 0.0) return;
     const dim3 grid((unsigned)((slice_m + SG_ROWS - 1) / SG_ROWS), (unsigned)((std::max(1, cmax) + SG_COLS - 1) / SG_COLS));
+    const unsigned rchunks = (unsigned)((slice_m + 127) / 128);
     in_pieces(cj, [&](size_t f0, size_t c) {
       launch(cls, fl * c / cj, 0.0, [&] {
-        slice_gemm_kernel<<<dim3(grid.x, grid.y, (unsigned)c), 256, 0, s>>>(dst_tasks + set * per_set + f0);
+        const SliceTask* tk = dst_tasks + set * per_set + f0;
+        if (cmax <= 1) slice_rows_kernel<1><<<dim3(rchunks, (unsigned)c), 128, 0, s>>>(tk);
+        else if (cmax <= 2) slice_rows_kernel<2><<<dim3(rchunks, (unsigned)c), 128, 0, s>>>(tk);
+        else if (cmax <= 4) slice_rows_kernel<4><<<dim3(rchunks, (unsigned)c), 128, 0, s>>>(tk);
+        else if (cmax <= 8) slice_rows_kernel<8><<<dim3(rchunks, (unsigned)c), 128, 0, s>>>(tk);
+        else slice_gemm_kernel<<<dim3(grid.x, grid.y, (unsigned)c), 256, 0, s>>>(tk);
       });
     });
   };
@@ -1897,7 +1904,7 @@ template <typename TR>
 void apply_tuning(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, Mode mode) {
   ctx->small_max_f32 = SMALL_MAX_F32;
   ctx->tc_choice = true;
-  ctx->split_choice = true;
+  ctx->split_choice = false;
   if (specs.empty()) return;
   std::vector<uint64_t> key;
   for (const JobSpec& sp : specs) key.push_back(sp.plan->id);
@@ -1908,9 +1915,14 @@ void apply_tuning(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spec
   auto it = ctx->tuned.find(key);
   if (it == ctx->tuned.end()) {
     if (!ctx->autotune || ctx->probe >= 0) {
+      // The fixed schedule (caroli_set_schedule; by default the tuner's default).
+      ctx->small_max_f32 = ctx->fixed_small_max;
+      ctx->tc_choice = ctx->fixed_mode >= 1;
+      ctx->split_choice = ctx->fixed_mode == 2;
       ctx->last_tune = TuneChoice{};
-      ctx->last_tune.tensor_cores = ctx->tensor_cores;
-      ctx->last_tune.split = ctx->tensor_cores;
+      ctx->last_tune.small_max = ctx->fixed_small_max;
+      ctx->last_tune.tensor_cores = ctx->tensor_cores && ctx->fixed_mode >= 1;
+      ctx->last_tune.split = ctx->fixed_mode == 2;
       return;
     }
     // Saved accounting of the call (the trials must not show in it).
@@ -1919,9 +1931,15 @@ void apply_tuning(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spec
     const double s_last = ctx->last_ms, s_f = ctx->factor_ms, s_r = ctx->root_ms, s_t = ctx->tail_ms;
     const int64_t s_ll = ctx->last_launches, s_rl = ctx->region_launches;
     std::vector<JobSpec> sample(specs.begin(), specs.begin() + std::min<size_t>(specs.size(), 256));
+    // The default schedule (fronts up to 96 variables in one CTA, rank-32 updates on the tensor
+    // cores, or the CUDA cores when they are off) is kept unless a candidate is more than 5 %
+    // faster: the schedule also shapes the refinement's preconditioner, which the trials do not
+    // time, so a difference within the trials' noise is not worth a change.
     TuneChoice best;
     best.tuned = true;
-    double best_ms = INFINITY;
+    best.split = false;
+    best.tensor_cores = ctx->tensor_cores;
+    double best_ms = INFINITY, default_ms = INFINITY;
     const int cand_small[3] = {48, 64, 96};
     const bool use_graphs = ctx->use_graphs;
     ctx->use_graphs = false;
@@ -1939,6 +1957,7 @@ void apply_tuning(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spec
           run_jobs<float, TR>(ctx, sys, sample, mode, tmp);
           const double ms = ctx->factor_ms + ctx->root_ms;
           best.ms[a * 3 + b] = ms;
+          if (cand_small[a] == SMALL_MAX_F32 && !spl && tcv == ctx->tensor_cores) default_ms = ms;
           if (ms < best_ms) {
             best_ms = ms;
             best.small_max = cand_small[a];
@@ -1946,6 +1965,11 @@ void apply_tuning(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spec
             best.split = spl;
           }
         }
+      if (!(best_ms < 0.95 * default_ms)) {
+        best.small_max = SMALL_MAX_F32;
+        best.tensor_cores = ctx->tensor_cores;
+        best.split = false;
+      }
     } catch (...) {
       ctx->factor_only = false;
       ctx->use_graphs = use_graphs;
@@ -3685,6 +3709,16 @@ int caroli_set_autotune(caroli_ctx* ctx, int enable) {
   if (!ctx) return CAROLI_EINVAL;
   ctx->autotune = enable != 0;
   ctx->tuned.clear();
+  return CAROLI_OK;
+}
+
+int caroli_set_schedule(caroli_ctx* ctx, int small_max, int update_mode) {
+  CTX_LOCK(ctx);
+  if (!ctx) return CAROLI_EINVAL;
+  if ((small_max != 48 && small_max != 64 && small_max != 96) || update_mode < 0 || update_mode > 2)
+    return fail_with(ctx, CAROLI_EINVAL, "caroli_set_schedule: small_max 48, 64 or 96 and update_mode 0, 1 or 2");
+  ctx->fixed_small_max = small_max;
+  ctx->fixed_mode = update_mode;
   return CAROLI_OK;
 }
 

@@ -561,6 +561,62 @@ __global__ void __launch_bounds__(256) slice_gemm_kernel(const SliceTask* __rest
   }
 }
 
+// The same products for jobs with few columns (at most CB, the ribbons' few channels): a thread per
+// output row holding its CB sums, the input rows of a K step staged in shared memory. A 64 x 32
+// tile would leave most of its columns empty there. grid (row chunks of 128, tasks), 128 threads.
+template <int CB>
+__global__ void __launch_bounds__(128) slice_rows_kernel(const SliceTask* __restrict__ tasks) {
+  constexpr int KS = 64;
+  __shared__ double2 Xs[KS][CB];
+  const SliceTask t = tasks[blockIdx.y];
+  const RefineDesc& R = *t.rd;
+  if (R.done || (t.mode == 0 && R.inner_done)) return;
+  const int i0 = blockIdx.x * 128;
+  if (i0 >= t.m) return;
+  const int i = i0 + threadIdx.x;
+  double2 acc[CB];
+#pragma unroll
+  for (int j = 0; j < CB; ++j) acc[j] = make_double2(0.0, 0.0);
+  for (int k0 = 0; k0 < t.m; k0 += KS) {
+    for (int e = threadIdx.x; e < KS * CB; e += 128) {
+      const int kk = e % KS, j = e / KS, k = k0 + kk;
+      double2 v = make_double2(0.0, 0.0);
+      if (k < t.m && j < t.c) {
+        const int64_t q = t.irow[k] + (int64_t)j * t.ldi;
+        if (t.in_f32) {
+          const float2 f = static_cast<const float2*>(t.in)[q];
+          v = make_double2((double)f.x, (double)f.y);
+        } else {
+          v = static_cast<const double2*>(t.in)[q];
+        }
+      }
+      Xs[kk][j] = v;
+    }
+    __syncthreads();
+    if (i < t.m) {
+      const int k1 = min(KS, t.m - k0);
+      for (int kk = 0; kk < k1; ++kk) {
+        double2 a;
+        if (t.adj) { a = t.s[(k0 + kk) + (int64_t)i * t.m]; a.y = -a.y; }
+        else a = t.s[i + (int64_t)(k0 + kk) * t.m];
+#pragma unroll
+        for (int j = 0; j < CB; ++j) acc[j] = cfma(acc[j], a, Xs[kk][j]);
+      }
+    }
+    __syncthreads();
+  }
+  if (i >= t.m) return;
+  const int64_t orow = t.orow ? t.orow[i] : i;
+#pragma unroll
+  for (int j = 0; j < CB; ++j) {
+    if (j >= t.c) break;
+    double2& o = t.out[orow + (int64_t)j * t.ldo];
+    const double2 v = make_double2(t.sign * acc[j].x, t.sign * acc[j].y);
+    if (t.accumulate) { o.x += v.x; o.y += v.y; }
+    else o = v;
+  }
+}
+
 // Transmission matrix t = W_L^† x_L of each job after its refinement (x = G W_R): t is
 // cl x c column-major, W_L nl x cl. grid (jobs), threads over the entries of t.
 __global__ void tmatrix_kernel(const RefineDesc* __restrict__ rd, const double2* const* __restrict__ wl,

@@ -374,9 +374,14 @@ int caroli_set_wait_limit(caroli_ctx* ctx, int64_t polls);
  * the panel sweep and rank-32 updates) x how those larger fronts are updated: (2) on the tensor
  * cores with the panels restricted to the pivot columns and the Schur complement [X; S] formed by
  * one GEMM per front, (1) on the tensor cores with rank-32 updates of every column, (0) on the CUDA
- * cores. Off: the default schedule (96, mode 2 when caroli_set_tensor_cores is on). Changing it
- * forgets the choices. */
+ * cores. A candidate replaces the default schedule (96, mode 1 when caroli_set_tensor_cores is on,
+ * else 0) only when it is more than 5 % faster: the schedule also shapes the refinement, which the
+ * trials do not time. Off: the default schedule. Changing it forgets the choices. */
 int caroli_set_autotune(caroli_ctx* ctx, int enable);
+
+/* The schedule used while the autotuner is off: small_max 48, 64 or 96 and the update mode 2, 1
+ * or 0 as above (mode 1 or 2 also needs caroli_set_tensor_cores on). Default (96, 1). */
+int caroli_set_schedule(caroli_ctx* ctx, int small_max, int update_mode);
 
 /* CUDA graph replay (default on; no reference counterpart): a batch run twice in a row with the
  * same plans, schedule and device buffers has its factorization (every tree level's launches, the

@@ -30,15 +30,33 @@ def test_autotuner_picks_the_fastest_trial_and_keeps_parity():
     trials = [x for x in sch["trial_ms"] if x is not None]
     assert len(trials) == 9 and min(trials) > 0
     idx = [48, 64, 96].index(sch["small_max"]) * 3 + (2 - sch["update_mode"])
-    assert sch["trial_ms"][idx] == min(trials)
-    for (s, c), tv in zip(zip(S, C), t):
-        assert abs(tv - oracle_T(sys_, s, config=c)) <= 1e-8
-    # Every candidate schedule reaches the oracle too (the tuner may pick any of them).
+    default = sch["trial_ms"][2 * 3 + 1]  # (96, rank-32 tensor-core updates)
+    # The default unless a candidate is more than 5 % faster; then the fastest.
+    if min(trials) < 0.95 * default:
+        assert sch["trial_ms"][idx] == min(trials)
+    else:
+        assert (sch["small_max"], sch["update_mode"]) == (96, 1)
+    refs = [oracle_T(sys_, s, config=c) for s, c in zip(S, C)]
+    for tv, r in zip(t, refs):
+        assert abs(tv - r) <= 1e-8
+    # Every candidate schedule reaches the oracle too (the tuner may pick any of them), in mixed
+    # precision, and single precision stays within its f32 accuracy.
     ctx.set_autotune(False)
     try:
-        t0, st0, _ = sys_.solve_batch(S, C, Precision.MIXED)
-        assert (st0 == 0).all() and np.abs(t0 - t).max() <= 2e-8
+        for small_max in (48, 64, 96):
+            for mode in (2, 1, 0):
+                ctx.set_schedule(small_max, mode)
+                tm, stm, _ = sys_.solve_batch(S, C, Precision.MIXED)
+                assert (stm == 0).all(), (small_max, mode, stm)
+                assert ctx.last_schedule()["update_mode"] == mode
+                for tv, r in zip(tm, refs):
+                    assert abs(tv - r) <= 1e-8, (small_max, mode, tv, r)
+                t32, st32, _ = sys_.solve_batch(S, C, Precision.SINGLE)
+                assert (st32 == 0).all()
+                for tv, r in zip(t32, refs):
+                    assert abs(tv - r) <= 1e-2, (small_max, mode, tv, r)
     finally:
+        ctx.set_schedule(96, 1)
         ctx.set_autotune(True)
 
 
