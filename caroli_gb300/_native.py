@@ -49,6 +49,7 @@ SIGNATURES = {
     "caroli_set_autotune": (ctypes.c_int, [P, ctypes.c_int]),
     "caroli_set_graphs": (ctypes.c_int, [P, ctypes.c_int]),
     "caroli_set_schedule": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int]),
+    "caroli_set_sweep_columns": (ctypes.c_int, [P, ctypes.c_int]),
     "caroli_last_schedule": (ctypes.c_int, [P, P, P, P, P, P, P]),
     "caroli_solve_multi": (ctypes.c_int, [P, ctypes.c_int, P, P, P, ctypes.c_int, P, P, P]),
     "caroli_scattering_states": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P, P, P, P]),
@@ -157,6 +158,10 @@ class Context:
     def set_schedule(self, small_max=96, update_mode=1):
         """The schedule used while the autotuner is off (see caroli_set_schedule)."""
         self.check(self.lib.caroli_set_schedule(self.h, int(small_max), int(update_mode)))
+
+    def set_sweep_columns(self, min_columns=32):
+        """Batches with this many right-hand-side columns sweep on the tensor cores."""
+        self.check(self.lib.caroli_set_sweep_columns(self.h, int(min_columns)))
 
     def set_graphs(self, enable=True):
         """Replay a repeated batch's factorization as a CUDA graph (default on)."""

@@ -407,6 +407,7 @@ struct caroli_ctx {
   bool tc_choice = true;                        // the autotuner's tensor-core choice (with tensor_cores set)
   bool split_choice = false;                    // f32 Schur complements as one tensor-core GEMM per front
   int fixed_small_max = SMALL_MAX_F32, fixed_mode = 1;  // the schedule without the autotuner
+  int tg_min_cols = TG_MIN_COLS;  // batches with this many right-hand-side columns sweep on the tensor cores
   Buf f12_stage, f12_list, sgt_list;            // its F12 copies and task lists
   bool factor_only = false;                     // run_jobs stops after the root inverse (tuning trials)
   std::map<std::vector<uint64_t>, TuneChoice> tuned;  // per plan set and precision
@@ -617,7 +618,7 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
   // as tensor-core GEMMs (tcgemm.cuh): per level, the fronts' right-hand sides are gathered into a
   // staging block, then one GEMM task per output block. The lists hold every large front of every
   // such job; tasks of finished solves exit at once.
-  const bool wide = cmax >= TG_MIN_COLS;
+  const bool wide = cmax >= ctx->tg_min_cols;
   const int nlev_w = (int)lr.size();
   struct WideLevel { size_t fr0 = 0, nfr = 0, fw0 = 0, nfw = 0, bw0 = 0, nbw = 0; int max_m = 1; };
   std::vector<WideLevel> wl(nlev_w);
@@ -3719,6 +3720,14 @@ int caroli_set_schedule(caroli_ctx* ctx, int small_max, int update_mode) {
     return fail_with(ctx, CAROLI_EINVAL, "caroli_set_schedule: small_max 48, 64 or 96 and update_mode 0, 1 or 2");
   ctx->fixed_small_max = small_max;
   ctx->fixed_mode = update_mode;
+  return CAROLI_OK;
+}
+
+int caroli_set_sweep_columns(caroli_ctx* ctx, int min_columns) {
+  CTX_LOCK(ctx);
+  if (!ctx) return CAROLI_EINVAL;
+  if (min_columns < 1) return fail_with(ctx, CAROLI_EINVAL, "caroli_set_sweep_columns: at least 1 column");
+  ctx->tg_min_cols = min_columns;
   return CAROLI_OK;
 }
 

@@ -383,6 +383,11 @@ int caroli_set_autotune(caroli_ctx* ctx, int enable);
  * or 0 as above (mode 1 or 2 also needs caroli_set_tensor_cores on). Default (96, 1). */
 int caroli_set_schedule(caroli_ctx* ctx, int small_max, int update_mode);
 
+/* Mixed-precision batches whose largest block solve carries at least `min_columns` right-hand-side
+ * columns (channels) sweep their large fronts and roots as tensor-core GEMMs; others use the row
+ * kernels. Default 32. No reference counterpart. */
+int caroli_set_sweep_columns(caroli_ctx* ctx, int min_columns);
+
 /* CUDA graph replay (default on; no reference counterpart): a batch run twice in a row with the
  * same plans, schedule and device buffers has its factorization (every tree level's launches, the
  * root assembly and inverse) captured as a CUDA graph on its second run and replayed with one
