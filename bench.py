@@ -299,6 +299,7 @@ def run_ribbons(args):
     ne = len(es)
     items = [(ribbons[r], sigmas[shapes[r][0]][k], 0) for r in range(len(ribbons)) for k in range(ne)]
     ctx = context(0)
+    ctx.set_refine_options(args.refine_max_iters, 1e-10, 1e-10)
     t0 = time.perf_counter()
     solve_systems(items, Precision.MIXED)  # plan and Σ uploads, first factorization
     upload_s = time.perf_counter() - t0
@@ -314,6 +315,22 @@ def run_ribbons(args):
     plan0 = ribbons[0].plan()
     schedule = ctx.last_schedule()
     fallbacks, max_iters = plan0.last_stats()
+    # Per block solve of the last step: GMRES steps, outer iterations, perturbed pivots, status.
+    j_iters, j_pert, j_stat = plan0.last_job_info()
+    j_steps = plan0.last_job_steps()
+    job_steps, batch_steps = plan0.last_refine_steps()
+
+    def hist(a, cap):
+        a = np.minimum(np.asarray(a), cap)
+        vals, cnt = np.unique(a, return_counts=True)
+        return {int(v): int(c) for v, c in zip(vals, cnt)}
+
+    refinement = {"max_outer_iterations": int(max_iters), "fp64_recomputed_solves": int(fallbacks),
+                  "gmres_steps_total": int(job_steps), "batch_steps": int(batch_steps),
+                  "gmres_steps_hist": hist(j_steps, 80), "outer_iterations_hist": hist(j_iters, 10),
+                  "perturbed_pivots_hist": hist(j_pert, 32),
+                  "mean_steps_unperturbed": float(np.mean(j_steps[j_pert == 0])) if (j_pert == 0).any() else None,
+                  "mean_steps_perturbed": float(np.mean(j_steps[j_pert > 0])) if (j_pert > 0).any() else None}
     # FP64 on every 8th energy of every ribbon (the ratio's denominator), and the mixed T there.
     sub = [i for i in range(len(items)) if (i % ne) % 8 == 0]
     sub_items = [items[i] for i in sub]
@@ -345,8 +362,8 @@ def run_ribbons(args):
         solve_systems(items, Precision.MIXED)
     e2e_ms, _ = ctx.region_end()
     e2e_wall = time.perf_counter() - e0
-    roof, kernels = roofline_probe(ctx, lambda: solve_systems(items, Precision.MIXED), ms / args.steps,
-                                   traffic_of=lambda name: None)
+    roof, kernels = (roofline_probe(ctx, lambda: solve_systems(items, Precision.MIXED), ms / args.steps,
+                                    traffic_of=lambda name: None) if args.probe else (None, None))
     # CPU baseline: the oracle on one energy of 16 ribbons spread over the sizes.
     cpu = None
     if args.cpu_sample > 0:
@@ -383,6 +400,7 @@ def run_ribbons(args):
         "mixed_over_fp64": ms_dbl / ms_msub,
         "max_abs_dT_vs_fp64": float(dT.max()), "median_abs_dT_vs_fp64": float(np.median(dT)),
         "status_ok": bool((st_mixed == 0).all()), "fp64_recomputed_solves": int(fallbacks),
+        "refinement": refinement,
         "e2e": {"value": n * args.steps / (e2e_ms * 1e-3), "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "wall_s": e2e_wall,
                 "note": "H values of every ribbon uploaded each step; lead self-energies resident"},
@@ -781,6 +799,8 @@ def main():
     ap.add_argument("--ribbons", type=int, default=256)
     ap.add_argument("--cubic-energies", default="8,16,23", help="indices into the cubic workload's 32 energies")
     ap.add_argument("--mixed-max-channels", type=int, default=100000)
+    ap.add_argument("--refine-max-iters", type=int, default=6, help="outer refinement steps (caroli_set_refine_options)")
+    ap.add_argument("--no-probe", dest="probe", action="store_false", help="skip the per-kernel-class probe passes")
     args = ap.parse_args()
     if args.workload == "cubic":
         if args.configs == 8:
