@@ -475,7 +475,8 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
                    const float2* arena, const std::vector<size_t>& arena_off, const float2* rarena,
                    const std::vector<size_t>& root_off, LaunchT& launch, std::vector<double>& th,
                    std::vector<double>& eh, std::vector<int32_t>& sh, std::vector<int32_t>& ih, RefineBufs& rb,
-                   int adjoint, const std::vector<const double2*>& rhs, const StatesRequest* states = nullptr) {
+                   int adjoint, const std::vector<const double2*>& rhs, const StatesRequest* states = nullptr,
+                   bool allow_giveup = false) {
   cudaStream_t s = ctx->stream;
   std::vector<RefineDesc> rdh(cj);
   size_t xo = 0, to = 0, ho = 0;
@@ -949,9 +950,18 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
     compact(0);
     CK(cudaMemcpyAsync(dh.data(), rdone, cj * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    bool all = true;
-    for (size_t j = 0; j < cj; ++j) all &= dh[j] != 0 || rdh[j].c == 0;
-    if (all) break;
+    size_t active = 0;
+    for (size_t j = 0; j < cj; ++j) active += (dh[j] == 0 && rdh[j].c != 0) ? 1 : 0;
+    if (active == 0) break;
+    // The batch's tail: after two outer steps, when at most 1/32 of the solves still iterate, every
+    // further step would run the whole launch sequence for those few; they are recomputed in FP64
+    // instead (as failed points, precision.rs:102-115).
+    if (allow_giveup && it >= 1 && it + 1 < ctx->max_iters && active * 32 <= cj) {
+      launch(K_REF_CHECK, 0.0, 0.0, [&] {
+        refine_giveup_kernel<<<(unsigned)((cj + 127) / 128), 128, 0, s>>>(drd, (int)cj);
+      });
+      break;
+    }
   }
   CK(cudaEventRecord(ctx->ev1, s));
   if (!adjoint && !states) {
@@ -1795,8 +1805,10 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
           lr.push_back({lv.tiny0, lv.tiny_n, lv.small0, mid, lv.small0 + mid, lv.small_n - mid + lv.large_n, lv.max_n,
                         std::max(lv.max_large_ne, lv.max_small_n)});
         }
+        // Transmissions only: a stalled solve is recomputed in FP64 there (not so for gradients and
+        // states, whose callers receive the stalled status).
         RefineDesc* fwd = refine(ctx, sys, specs, begin, cj, lr, max_root, dtasks, jd, arena, arena_off, rarena,
-                                 root_off, launch, th, eh, sh, ih, ctx->rb[0], 0, {}, states);
+                                 root_off, launch, th, eh, sh, ih, ctx->rb[0], 0, {}, states, !grad && !states);
         for (size_t j = 0; j < cj && j < ctx->steps_tmp.size(); ++j) out[begin + j].steps = ctx->steps_tmp[j];
         if (grad) gradient(ctx, sys, specs, begin, cj, lr, max_root, dtasks, jd, arena, arena_off, rarena, root_off,
                            launch, th, eh, sh, ih, fwd, *grad, out);

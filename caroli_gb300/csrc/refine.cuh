@@ -197,6 +197,17 @@ __global__ void __launch_bounds__(256) refine_check_kernel(RefineDesc* __restric
   }
 }
 
+// Gives up the solves still iterating: marked stalled, they are recomputed in FP64 (a batch's
+// last few slow solves, see refine in the engine).
+__global__ void refine_giveup_kernel(RefineDesc* __restrict__ rd, int njobs) {
+  const int job = blockIdx.x * blockDim.x + threadIdx.x;
+  if (job >= njobs) return;
+  RefineDesc& R = rd[job];
+  if (R.done) return;
+  R.done = 1;
+  R.stalled = 1;
+}
+
 __global__ void refine_init_kernel(RefineDesc* __restrict__ rd, int njobs) {
   const int job = blockIdx.y;
   if (job >= njobs) return;
