@@ -432,7 +432,8 @@ def run_cubic(args):
     from caroli_gb300 import Precision
     from caroli_gb300.nested import context
 
-    sys_ = cubic_workload(configs=args.configs)
+    shape = [int(x) for x in args.cubic_shape.split(",")]
+    sys_ = cubic_workload(*shape, configs=args.configs)
     grid = np.linspace(-1.0, 1.0, 32)
     pick = [int(k) for k in args.cubic_energies.split(",")]
     sigmas = [sys_.self_energies_on_device(grid[k]) for k in pick]
@@ -798,6 +799,8 @@ def main():
                          "cubic: a sample of the 64x32x32 Anderson wire")
     ap.add_argument("--ribbons", type=int, default=256)
     ap.add_argument("--cubic-energies", default="8,16,23", help="indices into the cubic workload's 32 energies")
+    ap.add_argument("--cubic-shape", default="64,32,32", help="length, width, depth of the cubic wire (a smaller "
+                    "one for profiler captures)")
     ap.add_argument("--mixed-max-channels", type=int, default=100000)
     ap.add_argument("--refine-max-iters", type=int, default=6, help="outer refinement steps (caroli_set_refine_options)")
     ap.add_argument("--no-probe", dest="probe", action="store_false", help="skip the per-kernel-class probe passes")

@@ -50,6 +50,7 @@ SIGNATURES = {
     "caroli_set_graphs": (ctypes.c_int, [P, ctypes.c_int]),
     "caroli_set_schedule": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int]),
     "caroli_set_sweep_columns": (ctypes.c_int, [P, ctypes.c_int]),
+    "caroli_set_small_threads": (ctypes.c_int, [P, ctypes.c_int]),
     "caroli_last_schedule": (ctypes.c_int, [P, P, P, P, P, P, P]),
     "caroli_solve_multi": (ctypes.c_int, [P, ctypes.c_int, P, P, P, ctypes.c_int, P, P, P]),
     "caroli_scattering_states": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P, P, P, P]),
@@ -162,6 +163,10 @@ class Context:
     def set_sweep_columns(self, min_columns=32):
         """Batches with this many right-hand-side columns sweep on the tensor cores."""
         self.check(self.lib.caroli_set_sweep_columns(self.h, int(min_columns)))
+
+    def set_small_threads(self, threads=512):
+        """Threads of a CTA factoring a front of 64 to 96 variables (256 or 512)."""
+        self.check(self.lib.caroli_set_small_threads(self.h, int(threads)))
 
     def set_graphs(self, enable=True):
         """Replay a repeated batch's factorization as a CUDA graph (default on)."""

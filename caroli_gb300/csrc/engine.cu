@@ -408,6 +408,7 @@ struct caroli_ctx {
   bool split_choice = false;                    // f32 Schur complements as one tensor-core GEMM per front
   int fixed_small_max = SMALL_MAX_F32, fixed_mode = 1;  // the schedule without the autotuner
   int tg_min_cols = TG_MIN_COLS;  // batches with this many right-hand-side columns sweep on the tensor cores
+  int small_threads = 512;        // threads of a CTA factoring a front of 64 to 96 variables
   Buf f12_stage, f12_list, sgt_list;            // its F12 copies and task lists
   bool factor_only = false;                     // run_jobs stops after the root inverse (tuning trials)
   std::map<std::vector<uint64_t>, TuneChoice> tuned;  // per plan set and precision
@@ -1581,9 +1582,14 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
           const unsigned nblk = (unsigned)lv.sbn[b];
           const Task* st = dtasks + lv.sb0[b];
           const double share = (double)lv.sbn[b] / (double)lv.small_n;
+          const bool wide_cta = ctx->small_threads == 512 && lv.sb_n[b] > 64;
           launch(K_SMALL, lv.small_flops * share, lv.small_bytes * share, [&] {
-            if (mixed)
+            if (mixed && wide_cta)
+              small_front_wide_kernel<T, true><<<nblk, 512, sm, s>>>(djobs, st, Prec<T>::tol, perturb, pert);
+            else if (mixed)
               small_front_kernel<T, true><<<nblk, 256, sm, s>>>(djobs, st, Prec<T>::tol, perturb, pert);
+            else if (wide_cta)
+              small_front_wide_kernel<T, false><<<nblk, 512, sm, s>>>(djobs, st, Prec<T>::tol, perturb, pert);
             else
               small_front_kernel<T, false><<<nblk, 256, sm, s>>>(djobs, st, Prec<T>::tol, perturb, pert);
           });
@@ -1641,7 +1647,8 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
                        (uint64_t)(uintptr_t)djobs,
                        (uint64_t)(uintptr_t)dtasks, (uint64_t)(uintptr_t)dinv, (uint64_t)(uintptr_t)pert,
                        (uint64_t)(uintptr_t)status, (uint64_t)(uintptr_t)arena, (uint64_t)(uintptr_t)rarena,
-                       (uint64_t)split, (uint64_t)(uintptr_t)df12, (uint64_t)(uintptr_t)dsgt,
+                       (uint64_t)split, (uint64_t)ctx->small_threads, (uint64_t)(uintptr_t)df12,
+                       (uint64_t)(uintptr_t)dsgt,
                        (uint64_t)(uintptr_t)f12_stage})
       gkey.push_back(v);
     FactorGraph& fg = ctx->fgraph;
@@ -2143,6 +2150,8 @@ int caroli_ctx_create(int device_ordinal, caroli_ctx** out) {
     for (auto* k : {(const void*)tc_update_kernel, (const void*)tc_sweep_gemm_kernel,
                     (const void*)small_front_kernel<double, false>, (const void*)small_front_kernel<float, false>,
                     (const void*)small_front_kernel<double, true>, (const void*)small_front_kernel<float, true>,
+                    (const void*)small_front_wide_kernel<double, false>, (const void*)small_front_wide_kernel<float, false>,
+                    (const void*)small_front_wide_kernel<double, true>, (const void*)small_front_wide_kernel<float, true>,
                     (const void*)inv_finish_kernel<double>, (const void*)inv_finish_kernel<float>,
                     (const void*)inv_panel_kernel<double>, (const void*)inv_panel_kernel<float>,
                     (const void*)tiny_front_kernel<double, false>, (const void*)tiny_front_kernel<double, true>,
@@ -3732,6 +3741,14 @@ int caroli_set_schedule(caroli_ctx* ctx, int small_max, int update_mode) {
     return fail_with(ctx, CAROLI_EINVAL, "caroli_set_schedule: small_max 48, 64 or 96 and update_mode 0, 1 or 2");
   ctx->fixed_small_max = small_max;
   ctx->fixed_mode = update_mode;
+  return CAROLI_OK;
+}
+
+int caroli_set_small_threads(caroli_ctx* ctx, int threads) {
+  CTX_LOCK(ctx);
+  if (!ctx) return CAROLI_EINVAL;
+  if (threads != 256 && threads != 512) return fail_with(ctx, CAROLI_EINVAL, "caroli_set_small_threads: 256 or 512");
+  ctx->small_threads = threads;
   return CAROLI_OK;
 }
 

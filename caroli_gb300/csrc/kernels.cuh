@@ -415,9 +415,8 @@ __host__ __device__ inline size_t small_smem_bytes(int n, int ne, size_t vbytes)
 }
 
 template <typename T, bool KEEP>
-__global__ void __launch_bounds__(256) small_front_kernel(const JobDesc* __restrict__ jobs,
-                                                          const Task* __restrict__ tasks, double tol, int perturb,
-                                                          int* __restrict__ perturbed) {
+__device__ __forceinline__ void small_front_body(const JobDesc* __restrict__ jobs, const Task* __restrict__ tasks,
+                                                 double tol, int perturb, int* __restrict__ perturbed) {
   using V = typename Cx<T>::V;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const Task t = tasks[blockIdx.x];
@@ -514,6 +513,22 @@ __global__ void __launch_bounds__(256) small_front_kernel(const JobDesc* __restr
       out[i + (int64_t)j * n] = Fj[i];
     }
   }
+}
+
+// One CTA of 256 threads per front; small_front_wide_kernel: 512 threads, for the largest bucket
+// (fronts of 64 to 96 variables, two CTAs per SM by their shared memory), where twice the warps
+// replay the boundary rows.
+template <typename T, bool KEEP>
+__global__ void __launch_bounds__(256) small_front_kernel(const JobDesc* __restrict__ jobs,
+                                                          const Task* __restrict__ tasks, double tol, int perturb,
+                                                          int* __restrict__ perturbed) {
+  small_front_body<T, KEEP>(jobs, tasks, tol, perturb, perturbed);
+}
+template <typename T, bool KEEP>
+__global__ void __launch_bounds__(512, 2) small_front_wide_kernel(const JobDesc* __restrict__ jobs,
+                                                                  const Task* __restrict__ tasks, double tol,
+                                                                  int perturb, int* __restrict__ perturbed) {
+  small_front_body<T, KEEP>(jobs, tasks, tol, perturb, perturbed);
 }
 
 // ---- large fronts -------------------------------------------------------------------------------

@@ -388,6 +388,10 @@ int caroli_set_schedule(caroli_ctx* ctx, int small_max, int update_mode);
  * kernels. Default 32. No reference counterpart. */
 int caroli_set_sweep_columns(caroli_ctx* ctx, int min_columns);
 
+/* Threads of a CTA factoring a front of 64 to 96 variables in shared memory: 512 (default; twice
+ * the warps replay the boundary rows) or 256. No reference counterpart. */
+int caroli_set_small_threads(caroli_ctx* ctx, int threads);
+
 /* CUDA graph replay (default on; no reference counterpart): a batch run twice in a row with the
  * same plans, schedule and device buffers has its factorization (every tree level's launches, the
  * root assembly and inverse) captured as a CUDA graph on its second run and replayed with one
