@@ -17,9 +17,10 @@
 // accuracy of an f32 product), K-major no-swizzle shared-memory operands (tc.cuh).
 //
 // A CTA computes a 64 x 64 complex tile of one task: K in chunks of 32 complex (64 real, 8 MMA
-// slices), every warp stages the chunk's A' and B' (hi and lo) from global memory, one thread
-// issues the 24 MMAs and commits them to an mbarrier that all threads wait on (bounded) before the
-// next chunk reuses the buffers; two CTAs per SM overlap each other's staging and MMAs. The
+// slices), every warp stages the chunk's A' and B' (hi and lo) into shared memory from registers
+// loaded one chunk ahead, one thread issues the 24 MMAs and commits them to an mbarrier that all
+// threads wait on (bounded) before the next chunk reuses the buffers, while the next chunk's global
+// loads are in flight; two CTAs per SM overlap each other's staging and MMAs. The
 // epilogue reads the accumulator from tensor memory and writes C = add + sign A B, rows optionally
 // scattered through the fronts' SweepRow table. A wait that runs out marks the solve stalled (the
 // refinement then recomputes it in FP64) after the MMAs it issued have drained.
@@ -83,13 +84,25 @@ __global__ void __launch_bounds__(TG_THREADS, 2) tc_sweep_gemm_kernel(const TGTa
   const uint32_t idesc = tc::idesc_tf32(M, TG_COLS);
   const int chunks = (t.k + TG_KC - 1) / TG_KC;
   int issued = 0;  // chunks whose MMAs were committed
-  for (int ch = 0; ch < chunks; ++ch) {
-    const int k0 = ch * TG_KC;
-    // A' chunk: complex rows i0.., columns k0.. (two complex columns per item).
-    for (int idx = tid; idx < TG_ROWS * (TG_KC / 2); idx += TG_THREADS) {
+  // The raw operands of a chunk are loaded into registers one chunk ahead: the next chunk's global
+  // loads are in flight while the current chunk's MMAs run.
+  constexpr int AI = TG_ROWS * (TG_KC / 2) / TG_THREADS, BI = TG_COLS * (TG_KC / 2) / TG_THREADS;
+  float2 ra[AI][2], rb[BI][2];
+  auto a_item = [&](int q, int& i, int& c) {
+    const int idx = tid + q * TG_THREADS;
+    if (t.adj) { c = 2 * (idx % (TG_KC / 2)); i = idx / (TG_KC / 2); }
+    else { i = idx % TG_ROWS; c = 2 * (idx / TG_ROWS); }
+  };
+  auto b_item = [&](int q, int& j, int& c) {
+    const int idx = tid + q * TG_THREADS;
+    c = 2 * (idx % (TG_KC / 2));
+    j = idx / (TG_KC / 2);
+  };
+  auto load_chunk = [&](int k0) {
+#pragma unroll
+    for (int q = 0; q < AI; ++q) {
       int i, c;
-      if (t.adj) { c = 2 * (idx % (TG_KC / 2)); i = idx / (TG_KC / 2); }
-      else { i = idx % TG_ROWS; c = 2 * (idx / TG_ROWS); }
+      a_item(q, i, c);
       float2 p0 = make_float2(0.f, 0.f), p1 = make_float2(0.f, 0.f);
       const int gi = i0 + i, gk = k0 + c;
       if (gi < t.m) {
@@ -101,21 +114,41 @@ __global__ void __launch_bounds__(TG_THREADS, 2) tc_sweep_gemm_kernel(const TGTa
           if (gk + 1 < t.k) p1 = t.a[gi + (int64_t)(gk + 1) * t.lda];
         }
       }
-      const uint32_t o0 = tc::kmajor_offset(2 * i, 2 * c, M), o1 = tc::kmajor_offset(2 * i + 1, 2 * c, M);
-      tc::store_split(a_hi + o0, a_lo + o0, make_float4(p0.x, -p0.y, p1.x, -p1.y));
-      tc::store_split(a_hi + o1, a_lo + o1, make_float4(p0.y, p0.x, p1.y, p1.x));
+      ra[q][0] = p0;
+      ra[q][1] = p1;
     }
-    // B' chunk: rows k0.. of columns j0.. (coalesced along k).
-    for (int idx = tid; idx < TG_COLS * (TG_KC / 2); idx += TG_THREADS) {
-      const int c = 2 * (idx % (TG_KC / 2)), j = idx / (TG_KC / 2);
+#pragma unroll
+    for (int q = 0; q < BI; ++q) {
+      int j, c;
+      b_item(q, j, c);
       const int gk = k0 + c, gj = j0 + j;
       float2 q0 = make_float2(0.f, 0.f), q1 = make_float2(0.f, 0.f);
       if (gj < t.n) {
         if (gk < t.k) q0 = t.b[gk + (int64_t)gj * t.ldb];
         if (gk + 1 < t.k) q1 = t.b[gk + 1 + (int64_t)gj * t.ldb];
       }
+      rb[q][0] = q0;
+      rb[q][1] = q1;
+    }
+  };
+  if (chunks > 0) load_chunk(0);
+  for (int ch = 0; ch < chunks; ++ch) {
+    // A' (two complex columns per item, the 2 x 2 expansion) and B' of this chunk into shared memory.
+#pragma unroll
+    for (int q = 0; q < AI; ++q) {
+      int i, c;
+      a_item(q, i, c);
+      const float2 p0 = ra[q][0], p1 = ra[q][1];
+      const uint32_t o0 = tc::kmajor_offset(2 * i, 2 * c, M), o1 = tc::kmajor_offset(2 * i + 1, 2 * c, M);
+      tc::store_split(a_hi + o0, a_lo + o0, make_float4(p0.x, -p0.y, p1.x, -p1.y));
+      tc::store_split(a_hi + o1, a_lo + o1, make_float4(p0.y, p0.x, p1.y, p1.x));
+    }
+#pragma unroll
+    for (int q = 0; q < BI; ++q) {
+      int j, c;
+      b_item(q, j, c);
       const uint32_t o = tc::kmajor_offset(j, 2 * c, TG_COLS);
-      tc::store_split(b_hi + o, b_lo + o, make_float4(q0.x, q0.y, q1.x, q1.y));
+      tc::store_split(b_hi + o, b_lo + o, make_float4(rb[q][0].x, rb[q][0].y, rb[q][1].x, rb[q][1].y));
     }
     tc::fence_smem_async();
     tc::fence_before_sync();
@@ -134,6 +167,7 @@ __global__ void __launch_bounds__(TG_THREADS, 2) tc_sweep_gemm_kernel(const TGTa
       tc::mma_commit(&mma_done);
     }
     issued = ch + 1;
+    if (ch + 1 < chunks) load_chunk((ch + 1) * TG_KC);
     // The chunk's MMAs must finish before the operands are overwritten (and before the epilogue).
     const bool ok = tc::mbar_wait(&mma_done, (uint32_t)(ch & 1), wait_limit);
     if (!__all_sync(0xffffffffu, ok) && lane == 0) abort_flag = 1;
