@@ -331,15 +331,21 @@ __device__ __forceinline__ void column_order(const int* piv, int npiv, int* cper
 
 // Gauss-Jordan sweep of the leading rows x cols block of F (the pivot candidates of a small front)
 // by the first ceil(cols / 32) warps, a lane per column, synchronised by named barrier 1: same
-// pivots, operations and results as gj_sweep(F, ld, rows, cols, rows, rows, ...). The pivot of
-// step k is the largest |F[i, k]| over i in [k, rows), row k receives the pivot row and row p the
-// old row k, and the scaled pivot row of every step goes to prows (rows x cols). Column k is read
-// from the double buffer cb (2 x rows; cb[0:rows] must hold column 0), which the owner of column
-// k + 1 fills while it updates it. The calling warps must be exactly the first ceil(cols / 32).
+// pivots and operations as gj_sweep(F, ld, rows, cols, rows, rows, ...). The pivot of step k is the
+// largest |F[i, k]| over i in [k, rows), row k receives the pivot row and row p the old row k, and
+// the scaled pivot row of every step goes to prows (rows x cols). Column k is read from the double
+// buffer cb (2 x rows; cb[0:rows] must hold column 0), which the owner of column k + 1 fills while
+// it updates it. The calling warps must be exactly the first ceil(cols / 32).
+//
+// Every lane runs the same loop each step, so the warp holding the pivot column does not execute
+// two divergent loops: a column j != k becomes F[i, j] - c_i pr_j (pr_j = F[p, j] / pivot), the
+// pivot column -c_i / pivot, which is the same update from a zero column (`zeros`, rows zeros in
+// shared memory) with pr = 1 / pivot. Rows k and p, which the interchange treats apart, are
+// rewritten after the loop.
 template <typename T>
 __device__ bool gj_sweep_cols(typename Cx<T>::V* F, int ld, int rows, int cols, double scale2, double tol,
                               typename Cx<T>::V* cb, int* piv, bool perturb, int* perturbed,
-                              typename Cx<T>::V* prows) {
+                              typename Cx<T>::V* prows, const typename Cx<T>::V* zeros) {
   using V = typename Cx<T>::V;
   const int lane = threadIdx.x & 31;
   const int j = threadIdx.x;  // this lane's column
@@ -372,33 +378,81 @@ __device__ bool gj_sweep_cols(typename Cx<T>::V* F, int ld, int rows, int cols, 
     const V inv = cinv(d);
     const V ckk = ck[k];
     if (j < cols) {
-      if (j == k) {
-        prows[k * cols + j] = inv;
-        for (int i = 0; i < rows; ++i) {
-          const V c = (i == p) ? ckk : ck[i];
-          Fj[i] = (i == k) ? inv : cmul(cx<V>(-c.x, -c.y), inv);
-        }
-      } else {
-        const V pr = cmul(Fj[p], inv);
-        const V rk = Fj[k];
-        prows[k * cols + j] = pr;
-        const bool fill = j == k + 1;
-        for (int i = 0; i < rows; ++i) {
-          V nv;
-          if (i == k) {
-            nv = pr;
-          } else {
-            const V c = (i == p) ? ckk : ck[i];
-            nv = cfms_pk((i == p) ? rk : Fj[i], c, pr);
-          }
-          Fj[i] = nv;
-          if (fill) cn[i] = nv;
-        }
+      const bool pc = j == k;
+      const V* src = pc ? zeros : Fj;
+      const V rk = pc ? cx<V>(0.0, 0.0) : Fj[k];
+      const V pr = pc ? inv : cmul(Fj[p], inv);
+      prows[k * cols + j] = pr;
+      const bool fill = j == k + 1;
+#pragma unroll 4
+      for (int i = 0; i < rows; ++i) {
+        const V nv = cfms(src[i], ck[i], pr);
+        Fj[i] = nv;
+        if (fill) cn[i] = nv;
       }
+      if (p != k) {
+        const V nv = cfms(rk, ckk, pr);
+        Fj[p] = nv;
+        if (fill) cn[p] = nv;
+      }
+      Fj[k] = pr;
+      if (fill) cn[k] = pr;
     }
     asm volatile("bar.sync 1, %0;" ::"r"(nthreads) : "memory");
   }
   return true;
+}
+
+// Boundary rows of a small front: the recorded steps replayed, a warp per NR rows (two in f32, one
+// in FP64 for registers), lane l holding columns l + 32 q (q < RQ, RQ = ceil(n / 32)). Step k
+// leaves a row r as r - a prows[k] with a = r[k], and -a prows[k][k] in column k (r[k] is cleared
+// before the subtraction), the operations of the sweep itself. The step's entry a comes from lane
+// k % 32 of register k / 32, a compile-time register in each 32-step segment. Loads of prows past
+// column n run into the buffers after it in shared memory (at most 31 entries past the last row)
+// and are never stored.
+template <typename T, int RQ>
+__device__ __forceinline__ void replay_boundary(typename Cx<T>::V* F, int ld, int n, int ne,
+                                                const typename Cx<T>::V* prows) {
+  using V = typename Cx<T>::V;
+  constexpr int NR = sizeof(T) == 4 ? 2 : 1;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int i0 = ne + NR * w; i0 < n; i0 += NR * nw) {
+    V r[NR][RQ];
+#pragma unroll
+    for (int u = 0; u < NR; ++u)
+#pragma unroll
+      for (int q = 0; q < RQ; ++q) {
+        const int col = lane + 32 * q;
+        r[u][q] = (i0 + u < n && col < n) ? F[i0 + u + col * ld] : cx<V>(0.0, 0.0);
+      }
+#pragma unroll
+    for (int qk = 0; qk < RQ; ++qk) {
+      const int k1 = min(ne, 32 * qk + 32);
+      for (int k = 32 * qk; k < k1; ++k) {
+        const int kl = k & 31;
+        V a[NR];
+#pragma unroll
+        for (int u = 0; u < NR; ++u) {
+          a[u] = cx<V>(__shfl_sync(0xffffffffu, r[u][qk].x, kl), __shfl_sync(0xffffffffu, r[u][qk].y, kl));
+          if (lane == kl) r[u][qk] = cx<V>(0.0, 0.0);
+        }
+        const V* pk = prows + (int64_t)k * n + lane;
+#pragma unroll
+        for (int q = 0; q < RQ; ++q) {
+          const V b = pk[32 * q];
+#pragma unroll
+          for (int u = 0; u < NR; ++u) r[u][q] = cfms(r[u][q], a[u], b);
+        }
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < NR; ++u)
+#pragma unroll
+      for (int q = 0; q < RQ; ++q) {
+        const int col = lane + 32 * q;
+        if (i0 + u < n && col < n) F[i0 + u + col * ld] = r[u][q];
+      }
+  }
 }
 
 // ---- small fronts: assembly and elimination in shared memory, one CTA per front ---------------
@@ -407,11 +461,11 @@ __device__ bool gj_sweep_cols(typename Cx<T>::V* F, int ld, int rows, int cols, 
 // nb boundary rows never pivot and never interchange, so each of them then replays the ne steps
 // on its own from prows, a warp per row, without barriers: the same operations in the same order
 // as a sweep of the whole front.
-// Shared memory: the front (n x (n | 1)), prows (ne x n), the column buffer (2n), 32 doubles,
-// piv and cperm (n).
+// Shared memory: the front (n x (n | 1)), prows (ne x n), the column buffer (2n), n zeros, 32
+// doubles, piv and cperm (n).
 __host__ __device__ inline size_t small_smem_bytes(int n, int ne, size_t vbytes) {
   const int ld = n | 1;
-  return ((size_t)ld * n + (size_t)ne * n + 2 * (size_t)n) * vbytes + 32 * 8 + 2 * (size_t)n * 4 + 16;
+  return ((size_t)ld * n + (size_t)ne * n + 3 * (size_t)n) * vbytes + 32 * 8 + 2 * (size_t)n * 4 + 16;
 }
 
 template <typename T, bool KEEP>
@@ -428,7 +482,8 @@ __device__ __forceinline__ void small_front_body(const JobDesc* __restrict__ job
   V* F = reinterpret_cast<V*>(smem_raw);
   V* prows = F + (int64_t)ld * n;
   V* cb = prows + (int64_t)ne * n;
-  double* red = reinterpret_cast<double*>(cb + 2 * n);
+  V* zeros = cb + 2 * n;
+  double* red = reinterpret_cast<double*>(zeros + n);
   int* piv = reinterpret_cast<int*>(red + 32);
   int* cperm = piv + n;
   {
@@ -460,6 +515,7 @@ __device__ __forceinline__ void small_front_body(const JobDesc* __restrict__ job
     for (int i = lane; i < ne; i += 32) local = fmax(local, cnorm(F[i + j * ld]));
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     if (i < ne) cb[i] = F[i];
+    zeros[i] = cx<V>(0.0, 0.0);
     cperm[i] = i;
   }
   const double scale2 = block_max((double)local, red);  // also publishes cb
@@ -468,7 +524,7 @@ __device__ __forceinline__ void small_front_body(const JobDesc* __restrict__ job
   __shared__ int ok_flag;
   if (w < (n + 31) / 32) {
     const bool okc = gj_sweep_cols<T>(F, ld, ne, n, scale2, tol, cb, piv, perturb != 0,
-                                      perturbed ? perturbed + t.job : nullptr, prows);
+                                      perturbed ? perturbed + t.job : nullptr, prows, zeros);
     if (threadIdx.x == 0) ok_flag = okc ? 1 : 0;
   }
   __syncthreads();
@@ -477,33 +533,10 @@ __device__ __forceinline__ void small_front_body(const JobDesc* __restrict__ job
     if (threadIdx.x == 0) J.fail[t.front] = 1;
     return;
   }
-  // Boundary rows: the recorded steps replayed, a warp per row (columns lane, lane + 32, lane + 64).
-  constexpr int RQ = 3;
-  for (int i = ne + w; i < n; i += nw) {
-    V r[RQ];
-#pragma unroll
-    for (int q = 0; q < RQ; ++q) {
-      const int col = lane + 32 * q;
-      r[q] = col < n ? F[i + col * ld] : cx<V>(0.0, 0.0);
-    }
-    for (int k = 0; k < ne; ++k) {
-      const int qk = k >> 5;
-      const V src = qk == 0 ? r[0] : (qk == 1 ? r[1] : r[2]);
-      const V a = cx<V>(__shfl_sync(0xffffffffu, src.x, k & 31), __shfl_sync(0xffffffffu, src.y, k & 31));
-      const V* pk = prows + (int64_t)k * n;
-#pragma unroll
-      for (int q = 0; q < RQ; ++q) {
-        const int col = lane + 32 * q;
-        if (col >= n) continue;
-        r[q] = (col == k) ? cmul(cx<V>(-a.x, -a.y), pk[col]) : cfms(r[q], a, pk[col]);
-      }
-    }
-#pragma unroll
-    for (int q = 0; q < RQ; ++q) {
-      const int col = lane + 32 * q;
-      if (col < n) F[i + col * ld] = r[q];
-    }
-  }
+  // Boundary rows: the recorded steps replayed.
+  if (n <= 32) replay_boundary<T, 1>(F, ld, n, ne, prows);
+  else if (n <= 64) replay_boundary<T, 2>(F, ld, n, ne, prows);
+  else replay_boundary<T, 3>(F, ld, n, ne, prows);
   if (threadIdx.x == 0) column_order(piv, ne, cperm);
   __syncthreads();
   for (int j = w; j < n; j += nw) {

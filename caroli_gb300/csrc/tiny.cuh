@@ -103,15 +103,17 @@ __global__ void __launch_bounds__(256) tiny_front_kernel(const JobDesc* __restri
       const V inv = cinv(F[k + k * LD]);
       if (lane < n) prow[lane] = (lane == k) ? inv : cmul(F[k + lane * LD], inv);
       __syncwarp();
+      // Every lane runs the same loop: row i becomes row i - c_i prow with c_i its entry in column
+      // k, which is cleared first so that column k receives -c_i / pivot (prow[k] = 1 / pivot).
+      // Row k, the pivot row, is then overwritten with prow by the lanes of its columns.
       if (lane < n) {
         const V ck = F[lane + k * LD];
-        for (int j = 0; j < n; ++j) {
-          V* d = &F[lane + j * LD];
-          if (lane == k) *d = prow[j];
-          else if (j == k) *d = cmul(cx<V>(-ck.x, -ck.y), inv);
-          else *d = cfms(*d, ck, prow[j]);
-        }
+        F[lane + k * LD] = cx<V>(0.0, 0.0);
+#pragma unroll 4
+        for (int j = 0; j < n; ++j) F[lane + j * LD] = cfms(F[lane + j * LD], ck, prow[j]);
       }
+      __syncwarp();
+      if (lane < n) F[k + lane * LD] = prow[lane];
       __syncwarp();
     }
     // Undo the interchanges on the columns, last first (lane i moves its own row's entries).
