@@ -357,11 +357,25 @@ __device__ bool gj_sweep_cols(typename Cx<T>::V* F, int ld, int rows, int cols, 
     V* cn = cb + ((k + 1) & 1) * rows;
     T best = -1;
     int p = 0x7fffffff;
-    for (int i = k + lane; i < rows; i += 32) {
-      const T m = cnorm(ck[i]);
-      if (m > best) { best = m; p = i; }
+    if (sizeof(T) == 4 && rows - k <= 32) {
+      // One candidate per lane: the largest |c|^2 by a warp max of its bits (non-negative floats
+      // order as unsigned integers; +1 so that 0 means no candidate or NaN), the smallest row
+      // among equal maxima by a ballot. Same result as the shuffle reduction below.
+      const int i = k + lane;
+      const float m = i < rows ? (float)cnorm(ck[i]) : -1.f;
+      const unsigned key = (i < rows && m == m) ? __float_as_uint(m) + 1u : 0u;
+      const unsigned top = __reduce_max_sync(0xffffffffu, key);
+      if (top != 0u) {
+        p = k + __ffs(__ballot_sync(0xffffffffu, key == top)) - 1;
+        best = (T)__uint_as_float(top - 1u);
+      }
+    } else {
+      for (int i = k + lane; i < rows; i += 32) {
+        const T m = cnorm(ck[i]);
+        if (m > best) { best = m; p = i; }
+      }
+      warp_argmax(best, p);
     }
-    warp_argmax(best, p);
     const double big = (double)best;
     V d;
     if (!(big > thresh) || p >= rows) {
@@ -462,10 +476,10 @@ __device__ __forceinline__ void replay_boundary(typename Cx<T>::V* F, int ld, in
 // on its own from prows, a warp per row, without barriers: the same operations in the same order
 // as a sweep of the whole front.
 // Shared memory: the front (n x (n | 1)), prows (ne x n), the column buffer (2n), n zeros, 32
-// doubles, piv and cperm (n).
+// doubles, piv and cperm (n), the children's index maps (2n).
 __host__ __device__ inline size_t small_smem_bytes(int n, int ne, size_t vbytes) {
   const int ld = n | 1;
-  return ((size_t)ld * n + (size_t)ne * n + 3 * (size_t)n) * vbytes + 32 * 8 + 2 * (size_t)n * 4 + 16;
+  return ((size_t)ld * n + (size_t)ne * n + 3 * (size_t)n) * vbytes + 32 * 8 + 4 * (size_t)n * 4 + 16;
 }
 
 template <typename T, bool KEEP>
@@ -486,21 +500,46 @@ __device__ __forceinline__ void small_front_body(const JobDesc* __restrict__ job
   double* red = reinterpret_cast<double*>(zeros + n);
   int* piv = reinterpret_cast<int*>(red + 32);
   int* cperm = piv + n;
+  int* cmap = cperm + n;  // 2 x n: child c's position of variable i, -1 where it has none
   {
+    // The children's index maps are read once into shared memory; a lane keeps those of its rows
+    // (lane + 32 q) in registers, so the value loads of all its rows of a column issue together
+    // instead of each waiting for its own index load.
     const ChildBlocks<T> kids(J, f);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      int a[2];
+      kids.index(i, a);
+      cmap[i] = a[0];
+      cmap[n + i] = a[1];
+    }
+    int ar[3][2];
+    bool own[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      const int i = lane + 32 * q;
+      own[q] = i < n && J.own[f.own_off + i];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      const int i = lane + 32 * q;
+      ar[q][0] = i < n ? cmap[i] : -1;
+      ar[q][1] = i < n ? cmap[n + i] : -1;
+    }
     for (int j = w; j < n; j += nw) {
-      int bj[2];
-      kids.index(j, bj);
-      for (int i = lane; i < n; i += 32) {
-        int ai[2];
-        kids.index(i, ai);
-        F[i + j * ld] = kids.template at<T>(ai, bj);
+      const int bj[2] = {cmap[j], cmap[n + j]};
+      V v[3];
+#pragma unroll
+      for (int q = 0; q < 3; ++q) v[q] = kids.template at<T>(ar[q], bj);
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        const int i = lane + 32 * q;
+        if (i >= n) continue;
+        if (i == j && own[q]) v[q].x += (T)J.energy;
+        F[i + j * ld] = v[q];
       }
     }
   }
-  __syncthreads();
-  for (int i = threadIdx.x; i < n; i += blockDim.x)
-    if (J.own[f.own_off + i]) F[i + i * ld].x += (T)J.energy;
   __syncthreads();
   apply_entries<T>(J, f, F, ld, 0, n);
   __syncthreads();
@@ -516,7 +555,6 @@ __device__ __forceinline__ void small_front_body(const JobDesc* __restrict__ job
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     if (i < ne) cb[i] = F[i];
     zeros[i] = cx<V>(0.0, 0.0);
-    cperm[i] = i;
   }
   const double scale2 = block_max((double)local, red);  // also publishes cb
   // Pivot rows: a lane per column in the first ceil(n / 32) warps (named barrier per pivot); the
@@ -537,7 +575,17 @@ __device__ __forceinline__ void small_front_body(const JobDesc* __restrict__ job
   if (n <= 32) replay_boundary<T, 1>(F, ld, n, ne, prows);
   else if (n <= 64) replay_boundary<T, 2>(F, ld, n, ne, prows);
   else replay_boundary<T, 3>(F, ld, n, ne, prows);
-  if (threadIdx.x == 0) column_order(piv, ne, cperm);
+  // Column order, a column per thread of the last warps (the replay gives them the fewest rows):
+  // the interchanges undone on the columns, last first, leave in column j the swept column
+  // sigma_{ne-1}(... sigma_0(j)), sigma_k the transposition (k piv[k]) (as column_order).
+  for (int j = (int)blockDim.x - 1 - (int)threadIdx.x; j < n; j += blockDim.x) {
+    int pos = j;
+    for (int k = 0; k < ne; ++k) {
+      const int p = piv[k];
+      pos = pos == k ? p : (pos == p ? k : pos);
+    }
+    cperm[j] = pos;
+  }
   __syncthreads();
   for (int j = w; j < n; j += nw) {
     const V* Fj = F + cperm[j] * ld;
@@ -548,13 +596,14 @@ __device__ __forceinline__ void small_front_body(const JobDesc* __restrict__ job
   }
 }
 
-// One CTA of 256 threads per front; small_front_wide_kernel: 512 threads, for the largest bucket
-// (fronts of 64 to 96 variables, two CTAs per SM by their shared memory), where twice the warps
-// replay the boundary rows.
+// One CTA of 256 threads per front (f32: registers for five CTAs per SM, as many as their shared
+// memory allows for fronts of up to 64 variables); small_front_wide_kernel: 512 threads, for the
+// largest bucket (fronts of 64 to 96 variables, two CTAs per SM by their shared memory), where
+// twice the warps replay the boundary rows.
 template <typename T, bool KEEP>
-__global__ void __launch_bounds__(256) small_front_kernel(const JobDesc* __restrict__ jobs,
-                                                          const Task* __restrict__ tasks, double tol, int perturb,
-                                                          int* __restrict__ perturbed) {
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 5 : 2)
+    small_front_kernel(const JobDesc* __restrict__ jobs, const Task* __restrict__ tasks, double tol, int perturb,
+                       int* __restrict__ perturbed) {
   small_front_body<T, KEEP>(jobs, tasks, tol, perturb, perturbed);
 }
 template <typename T, bool KEEP>

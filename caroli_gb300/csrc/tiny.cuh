@@ -37,19 +37,20 @@ __global__ void __launch_bounds__(256) tiny_front_kernel(const JobDesc* __restri
   const int n = f.n, ne = f.ne;
   V* F = reinterpret_cast<V*>(smem_raw) + (size_t)w * ((size_t)nmax * LD + nmax);
   V* prow = F + (size_t)nmax * LD;
-  // Assembly: lane i builds row i.
+  // Assembly: lane i builds row i. Column j's child positions are row j's, taken from lane j by a
+  // shuffle, so the value loads of consecutive columns do not wait for index loads.
   {
     const ChildBlocks<T> kids(J, f);
     int ai[2];
     kids.index(lane < n ? lane : 0, ai);
-    if (lane < n)
-      for (int j = 0; j < n; ++j) {
-        int bj[2];
-        kids.index(j, bj);
-        V v = kids.template at<T>(ai, bj);
-        if (j == lane && J.own[f.own_off + lane]) v.x += (T)J.energy;
-        F[lane + j * LD] = v;
-      }
+    const bool own = lane < n && J.own[f.own_off + lane];
+#pragma unroll 4
+    for (int j = 0; j < n; ++j) {
+      const int bj[2] = {__shfl_sync(0xffffffffu, ai[0], j), __shfl_sync(0xffffffffu, ai[1], j)};
+      V v = kids.template at<T>(ai, bj);
+      if (j == lane && own) v.x += (T)J.energy;
+      if (lane < n) F[lane + j * LD] = v;
+    }
   }
   __syncwarp();
   for (int64_t e = lane; e < f.ent_cnt; e += 32) {
