@@ -1334,6 +1334,14 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
           }
       }
       lv.tiny_n = tasks.size() - lv.tiny0;
+      // Largest fronts first: the eight warps of a tiny-front CTA get fronts of about one size (a
+      // CTA lasts as long as its largest front), and the longest CTAs start first.
+      auto by_size = [&](size_t a0, size_t a1) {
+        std::stable_sort(tasks.begin() + a0, tasks.begin() + a1, [&](const Task& x, const Task& y) {
+          return specs[begin + x.job].plan->host.fronts[x.front].n > specs[begin + y.job].plan->host.fronts[y.front].n;
+        });
+      };
+      by_size(lv.tiny0, tasks.size());
       lv.small0 = tasks.size();
       const int bucket_hi[3] = {48, 64, small_max};
       for (int b = 0; b < 3; ++b) {
@@ -1356,6 +1364,7 @@ void run_jobs(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& specs, M
             }
         }
         lv.sbn[b] = tasks.size() - lv.sb0[b];
+        by_size(lv.sb0[b], tasks.size());
         if (hi >= small_max) break;
       }
       lv.small_n = tasks.size() - lv.small0;

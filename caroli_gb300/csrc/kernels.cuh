@@ -482,14 +482,14 @@ __host__ __device__ inline size_t small_smem_bytes(int n, int ne, size_t vbytes)
   return ((size_t)ld * n + (size_t)ne * n + 3 * (size_t)n) * vbytes + 32 * 8 + 4 * (size_t)n * 4 + 16;
 }
 
-template <typename T, bool KEEP>
+template <typename T, bool KEEP, bool PREFETCH>
 __device__ __forceinline__ void small_front_body(const JobDesc* __restrict__ jobs, const Task* __restrict__ tasks,
                                                  double tol, int perturb, int* __restrict__ perturbed) {
   using V = typename Cx<T>::V;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const Task t = tasks[blockIdx.x];
   const JobDesc& J = jobs[t.job];
-  const FrontDesc& f = *t.fd;
+  const FrontDesc f = *t.fd;  // copied at once: its fields load together, not on first use
   const int n = f.n, ne = f.ne;
   const int ld = n | 1;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -501,6 +501,15 @@ __device__ __forceinline__ void small_front_body(const JobDesc* __restrict__ job
   int* piv = reinterpret_cast<int*>(red + 32);
   int* cperm = piv + n;
   int* cmap = cperm + n;  // 2 x n: child c's position of variable i, -1 where it has none
+  // With PREFETCH, the first blockDim.x H entries and their values are requested before the
+  // assembly, so that their loads overlap its loads (where registers allow).
+  const bool has0 = PREFETCH && threadIdx.x < f.ent_cnt;
+  Entry en0{};
+  double2 h0 = make_double2(0.0, 0.0);
+  if (has0) {
+    en0 = J.entries[f.ent_off + threadIdx.x];
+    h0 = J.vals[en0.q];
+  }
   {
     // The children's index maps are read once into shared memory; a lane keeps those of its rows
     // (lane + 32 q) in registers, so the value loads of all its rows of a column issue together
@@ -541,7 +550,18 @@ __device__ __forceinline__ void small_front_body(const JobDesc* __restrict__ job
     }
   }
   __syncthreads();
-  apply_entries<T>(J, f, F, ld, 0, n);
+  if (has0) {
+    if (en0.conj) h0.y = -h0.y;
+    V& d = F[en0.a + (int64_t)en0.b * ld];
+    d = csub(d, from64<V>(h0));
+  }
+  for (int64_t e = threadIdx.x + (PREFETCH ? blockDim.x : 0); e < f.ent_cnt; e += blockDim.x) {
+    const Entry en = J.entries[f.ent_off + e];
+    double2 h = J.vals[en.q];
+    if (en.conj) h.y = -h.y;
+    V& d = F[en.a + (int64_t)en.b * ld];
+    d = csub(d, from64<V>(h));
+  }
   __syncthreads();
   V* out = static_cast<V*>(J.arena) + f.arena_off;
   if (ne == 0) {
@@ -604,13 +624,13 @@ template <typename T, bool KEEP>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 5 : 2)
     small_front_kernel(const JobDesc* __restrict__ jobs, const Task* __restrict__ tasks, double tol, int perturb,
                        int* __restrict__ perturbed) {
-  small_front_body<T, KEEP>(jobs, tasks, tol, perturb, perturbed);
+  small_front_body<T, KEEP, false>(jobs, tasks, tol, perturb, perturbed);
 }
 template <typename T, bool KEEP>
 __global__ void __launch_bounds__(512, 2) small_front_wide_kernel(const JobDesc* __restrict__ jobs,
                                                                   const Task* __restrict__ tasks, double tol,
                                                                   int perturb, int* __restrict__ perturbed) {
-  small_front_body<T, KEEP>(jobs, tasks, tol, perturb, perturbed);
+  small_front_body<T, KEEP, true>(jobs, tasks, tol, perturb, perturbed);
 }
 
 // ---- large fronts -------------------------------------------------------------------------------

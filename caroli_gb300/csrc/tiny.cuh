@@ -33,18 +33,28 @@ __global__ void __launch_bounds__(256) tiny_front_kernel(const JobDesc* __restri
   if (ti >= ntasks) return;
   const Task t = tasks[ti];
   const JobDesc& J = jobs[t.job];
-  const FrontDesc& f = *t.fd;
+  const FrontDesc f = *t.fd;  // copied at once: its fields load together, not on first use
   const int n = f.n, ne = f.ne;
   V* F = reinterpret_cast<V*>(smem_raw) + (size_t)w * ((size_t)nmax * LD + nmax);
   V* prow = F + (size_t)nmax * LD;
+  // The front's first 32 H entries and their values are requested before the assembly, so that
+  // their loads overlap its loads.
+  const bool has0 = lane < f.ent_cnt;
+  Entry en0{};
+  double2 h0 = make_double2(0.0, 0.0);
+  if (has0) {
+    en0 = J.entries[f.ent_off + lane];
+    h0 = J.vals[en0.q];
+  }
   // Assembly: lane i builds row i. Column j's child positions are row j's, taken from lane j by a
-  // shuffle, so the value loads of consecutive columns do not wait for index loads.
+  // shuffle, so the value loads of consecutive columns do not wait for index loads; eight columns
+  // at a time keep sixteen loads in flight per lane.
   {
     const ChildBlocks<T> kids(J, f);
     int ai[2];
     kids.index(lane < n ? lane : 0, ai);
     const bool own = lane < n && J.own[f.own_off + lane];
-#pragma unroll 4
+#pragma unroll 8
     for (int j = 0; j < n; ++j) {
       const int bj[2] = {__shfl_sync(0xffffffffu, ai[0], j), __shfl_sync(0xffffffffu, ai[1], j)};
       V v = kids.template at<T>(ai, bj);
@@ -53,7 +63,12 @@ __global__ void __launch_bounds__(256) tiny_front_kernel(const JobDesc* __restri
     }
   }
   __syncwarp();
-  for (int64_t e = lane; e < f.ent_cnt; e += 32) {
+  if (has0) {
+    if (en0.conj) h0.y = -h0.y;
+    V& d = F[en0.a + en0.b * LD];
+    d = csub(d, from64<V>(h0));
+  }
+  for (int64_t e = lane + 32; e < f.ent_cnt; e += 32) {
     const Entry en = J.entries[f.ent_off + e];
     double2 h = J.vals[en.q];
     if (en.conj) h.y = -h.y;
