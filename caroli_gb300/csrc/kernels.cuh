@@ -229,11 +229,21 @@ __device__ __forceinline__ void apply_entries(const JobDesc& J, const FrontDesc&
 // ---- Gauss-Jordan sweep -------------------------------------------------------------------------
 // Largest value of a warp, ties to the smaller index (the reference keeps the first maximum); NaN
 // never wins, so a column of NaN reports -1 and fails the pivot test.
+// v is a lane's largest |c|^2 (never NaN) or -1 for no candidate. In f32 two warp reductions do
+// it: the maximum of v's bits (non-negative floats order as unsigned integers; +1 so that 0 means
+// no candidate), then the minimum index among the lanes holding it.
 template <typename T> __device__ __forceinline__ void warp_argmax(T& v, int& i) {
-  for (int o = 16; o > 0; o >>= 1) {
-    const T v2 = __shfl_xor_sync(0xffffffffu, v, o);
-    const int i2 = __shfl_xor_sync(0xffffffffu, i, o);
-    if (v2 > v || (v2 == v && i2 < i)) { v = v2; i = i2; }
+  if constexpr (sizeof(T) == 4) {
+    const unsigned key = v >= 0 ? __float_as_uint((float)v) + 1u : 0u;
+    const unsigned top = __reduce_max_sync(0xffffffffu, key);
+    i = __reduce_min_sync(0xffffffffu, key == top ? i : 0x7fffffff);
+    v = top ? (T)__uint_as_float(top - 1u) : (T)-1;
+  } else {
+    for (int o = 16; o > 0; o >>= 1) {
+      const T v2 = __shfl_xor_sync(0xffffffffu, v, o);
+      const int i2 = __shfl_xor_sync(0xffffffffu, i, o);
+      if (v2 > v || (v2 == v && i2 < i)) { v = v2; i = i2; }
+    }
   }
 }
 

@@ -86,13 +86,13 @@ __global__ void __launch_bounds__(256) tiny_front_kernel(const JobDesc* __restri
     const double thresh = tol * tol * scale2;
     int mypiv = 0;  // lane k keeps piv[k]
     for (int k = 0; k < ne; ++k) {
-      T bt = (lane >= k && lane < ne) ? cnorm(F[lane + k * LD]) : (T)-1;
-      int bi = (lane >= k && lane < ne) ? lane : 0x7fffffff;
-      for (int o = 16; o > 0; o >>= 1) {
-        const T b2 = __shfl_xor_sync(0xffffffffu, bt, o);
-        const int i2 = __shfl_xor_sync(0xffffffffu, bi, o);
-        if (b2 > bt || (b2 == bt && i2 < bi)) { bt = b2; bi = i2; }
+      T bt = (T)-1;
+      int bi = 0x7fffffff;
+      if (lane >= k && lane < ne) {
+        const T m = cnorm(F[lane + k * LD]);
+        if (m > bt) { bt = m; bi = lane; }  // NaN is no candidate
       }
+      warp_argmax(bt, bi);
       const double best = (double)bt;
       int p = bi;
       if (!(best > thresh) || p >= ne) {
