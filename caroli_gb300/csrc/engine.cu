@@ -247,7 +247,7 @@ struct SectorRequest {
 struct RefineBufs {
   Buf rdesc, rx, rr, rd, rtb, rhb, rt, rerr, rdone, rgx, stasks;
   Buf gV, gZ, gH, gg, gcs, gsn, gy, gbeta, gcol, gflags;
-  Buf segs, ctasks, ccount, cjobs;  // task lists compacted to the solves still iterating
+  Buf segs, ctasks, ccount, cjobs, ojobs;  // task and job lists compacted to the solves still iterating
   Buf tg_fr, tg_tasks, tg_stage;    // tensor-core sweeps of many-column solves (tcgemm.cuh)
   // The vectors (one column per channel; the bulk of a mixed batch's memory besides the fronts).
   void release_vectors() {
@@ -754,21 +754,22 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
       });
     });
   };
-  // Launches the slice products of one set (all jobs); flops for the accounting.
-  auto slice_products = [&](size_t set, KClass cls) {
+  // Launches the slice products of one set for the `nl` jobs listed in `jl`; flops for the
+  // accounting (the set's flops over all jobs, in proportion to the jobs listed).
+  auto slice_products = [&](size_t set, KClass cls, const int32_t* jl, size_t nl) {
     double fl = 0.0;
     for (size_t j = 0; j < cj; ++j) fl += 8.0 * sth[set * per_set + j].m * (double)sth[set * per_set + j].m * sth[set * per_set + j].c;
-    if (fl == 0.0) return;
+    if (fl == 0.0 || nl == 0) return;
     const dim3 grid((unsigned)((slice_m + SG_ROWS - 1) / SG_ROWS), (unsigned)((std::max(1, cmax) + SG_COLS - 1) / SG_COLS));
     const unsigned rchunks = (unsigned)((slice_m + 127) / 128);
-    in_pieces(cj, [&](size_t f0, size_t c) {
+    in_pieces(nl, [&](size_t f0, size_t c) {
       launch(cls, fl * c / cj, 0.0, [&] {
-        const SliceTask* tk = dst_tasks + set * per_set + f0;
-        if (cmax <= 1) slice_rows_kernel<1><<<dim3(rchunks, (unsigned)c), 128, 0, s>>>(tk);
-        else if (cmax <= 2) slice_rows_kernel<2><<<dim3(rchunks, (unsigned)c), 128, 0, s>>>(tk);
-        else if (cmax <= 4) slice_rows_kernel<4><<<dim3(rchunks, (unsigned)c), 128, 0, s>>>(tk);
-        else if (cmax <= 8) slice_rows_kernel<8><<<dim3(rchunks, (unsigned)c), 128, 0, s>>>(tk);
-        else slice_gemm_kernel<<<dim3(grid.x, grid.y, (unsigned)c), 256, 0, s>>>(tk);
+        const SliceTask* tk = dst_tasks + set * per_set;
+        if (cmax <= 1) slice_rows_kernel<1><<<dim3(rchunks, (unsigned)c), 128, 0, s>>>(tk, jl + f0);
+        else if (cmax <= 2) slice_rows_kernel<2><<<dim3(rchunks, (unsigned)c), 128, 0, s>>>(tk, jl + f0);
+        else if (cmax <= 4) slice_rows_kernel<4><<<dim3(rchunks, (unsigned)c), 128, 0, s>>>(tk, jl + f0);
+        else if (cmax <= 8) slice_rows_kernel<8><<<dim3(rchunks, (unsigned)c), 128, 0, s>>>(tk, jl + f0);
+        else slice_gemm_kernel<<<dim3(grid.x, grid.y, (unsigned)c), 256, 0, s>>>(tk, jl + f0);
       });
     });
   };
@@ -798,21 +799,33 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
   Task* ctasks = static_cast<Task*>(rb.ctasks.get(std::max<size_t>(ntask_all, 1) * sizeof(Task)));
   int32_t* ccount = static_cast<int32_t*>(rb.ccount.get((nseg + 1) * sizeof(int32_t)));
   int32_t* cjobs = static_cast<int32_t*>(rb.cjobs.get(cj * sizeof(int32_t)));
+  int32_t* ojobs = static_cast<int32_t*>(rb.ojobs.get(cj * sizeof(int32_t)));
   CK(cudaMemcpyAsync(dsegs, segs.data(), nseg * sizeof(TaskSeg), cudaMemcpyHostToDevice, s));
   std::vector<int32_t> hcount(nseg + 1, 0);
   // Compacts the lists to the solves still iterating; the counts reach the host with the next
-  // synchronisation.
+  // synchronisation. The jobs not done go to `ojobs` (outer steps), those whose GMRES still runs
+  // to `cjobs` (inner steps); `jobs` is the list of the last compaction, `njobs_l` its length
+  // once synchronised.
+  const int32_t* jobs = ojobs;
   auto compact = [&](int inner) {
     CK(cudaMemsetAsync(ccount, 0, (nseg + 1) * sizeof(int32_t), s));
     const unsigned gx = (unsigned)std::max<int64_t>(1, (std::max<int64_t>(seg_max, (int64_t)cj) + 255) / 256);
+    int32_t* out = inner ? cjobs : ojobs;
     launch(K_REF_GMRES, 0.0, 0.0, [&] {
-      compact_kernel<<<dim3(gx, (unsigned)(nseg + 1)), 256, 0, s>>>(drd, (int)cj, dtasks, dsegs, nseg, ctasks, cjobs,
+      compact_kernel<<<dim3(gx, (unsigned)(nseg + 1)), 256, 0, s>>>(drd, (int)cj, dtasks, dsegs, nseg, ctasks, out,
                                                                   ccount, inner);
     });
     CK(cudaMemcpyAsync(hcount.data(), ccount, (nseg + 1) * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    jobs = out;
   };
   compact(0);
   CK(cudaStreamSynchronize(s));
+  size_t njobs_l = (size_t)hcount[nseg], nouter = njobs_l;
+  // Algorithmic bytes of the Arnoldi vectors of all jobs (one pass over every column); a GMRES
+  // step k reads and writes 6 k + 13 such passes (two Gram-Schmidt passes of k + 1 dot products
+  // and an axpy each, the norm and the scaling), accounted in proportion to the jobs listed.
+  double vec_pass = 0.0;
+  for (size_t j = 0; j < cj; ++j) vec_pass += 16.0 * (double)rdh[j].nblk * rdh[j].c;
   auto sweep_cb = [&](auto cbt, int src, int dst) {
     constexpr int CB = decltype(cbt)::value;
     // Warp-per-front launches over a segment, at most 65535 blocks of TINY_WARPS (grid y).
@@ -863,7 +876,7 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
       in_pieces((size_t)nj, [&](size_t f0, size_t c) {
         launch(K_REF_ROOT, 0.0, 0.0, [&] {
           sweep_root_kernel<CB><<<dim3(cchunks, (unsigned)c), 256, (size_t)max_root * CB * sizeof(float2), s>>>(
-              drd, cjobs + f0, src, dst);
+              drd, jobs + f0, src, dst);
         });
       });
     }
@@ -898,27 +911,35 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
     }
   };
   for (int it = 0; it < ctx->max_iters; ++it) {
-    in_pieces(cj, [&](size_t f0, size_t c) {
-      launch(K_REF_GMRES, 0.0, 0.0, [&] { gm_start_kernel<<<dim3((unsigned)c, cols), 256, 0, s>>>(drd + f0); });
+    // The outer step's jobs: those not done (the list of the last outer compaction).
+    const size_t no = nouter;
+    in_pieces(no, [&](size_t f0, size_t c) {
+      launch(K_REF_GMRES, 0.0, vec_pass * 2.0 * c / cj,
+             [&] { gm_start_kernel<<<dim3((unsigned)c, cols), 256, 0, s>>>(drd, ojobs + f0); });
     });
     for (int k = 0; k < GM_M; ++k) {
       sweep(k, k);
       ctx->refine_batch_steps += 1;
-      in_pieces(cj, [&](size_t f0, size_t c) {
+      // This inner step's jobs: the outer list at k = 0, else those whose GMRES still runs.
+      const int32_t* jl = k == 0 ? ojobs : cjobs;
+      const size_t nl = k == 0 ? no : njobs_l;
+      in_pieces(nl, [&](size_t f0, size_t c) {
         launch(K_REF_RES, resid_flops * c / cj, 0.0,
-               [&] { gm_matvec_kernel<<<dim3((unsigned)c, rows), 256, 0, s>>>(drd + f0, k); });
+               [&] { gm_matvec_kernel<<<dim3((unsigned)c, rows), 256, 0, s>>>(drd, jl + f0, k); });
       });
-      for (int side = 0; side < nsides; ++side) slice_products(set_mv + (size_t)k * nsides + side, K_REF_RES);
+      for (int side = 0; side < nsides; ++side) slice_products(set_mv + (size_t)k * nsides + side, K_REF_RES, jl, nl);
       for (int pass = 0; pass < 2; ++pass) {
-        in_pieces(cj, [&](size_t f0, size_t c) {
-          launch(K_REF_GMRES, 0.0, 0.0,
-                 [&] { gm_dot_kernel<<<dim3((unsigned)c, cols, (unsigned)(k + 1)), 256, 0, s>>>(drd + f0, k, pass); });
-          launch(K_REF_GMRES, 0.0, 0.0, [&] { gm_axpy_kernel<<<dim3((unsigned)c, rows), 256, 0, s>>>(drd + f0, k); });
+        in_pieces(nl, [&](size_t f0, size_t c) {
+          launch(K_REF_GMRES, 0.0, vec_pass * 2.0 * (k + 1) * c / cj, [&] {
+            gm_dot_kernel<<<dim3((unsigned)c, cols, (unsigned)(k + 1)), 256, 0, s>>>(drd, jl + f0, k, pass);
+          });
+          launch(K_REF_GMRES, 0.0, vec_pass * (k + 3.0) * c / cj,
+                 [&] { gm_axpy_kernel<<<dim3((unsigned)c, rows), 256, 0, s>>>(drd, jl + f0, k); });
         });
       }
-      in_pieces(cj, [&](size_t f0, size_t c) {
-        launch(K_REF_GMRES, 0.0, 0.0,
-               [&] { gm_norm_kernel<<<dim3((unsigned)c, cols), 256, 0, s>>>(drd + f0, k, ctx->inner_tol); });
+      in_pieces(nl, [&](size_t f0, size_t c) {
+        launch(K_REF_GMRES, 0.0, vec_pass * 3.0 * c / cj,
+               [&] { gm_norm_kernel<<<dim3((unsigned)c, cols), 256, 0, s>>>(drd, jl + f0, k, ctx->inner_tol); });
       });
       launch(K_REF_GMRES, 0.0, 0.0, [&] {
         gm_inner_check_kernel<<<(unsigned)((cj + 127) / 128), 128, 0, s>>>(drd, (int)cj, k, gflags);
@@ -926,31 +947,37 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
       compact(1);
       CK(cudaMemcpyAsync(dh.data(), gflags, cj * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
       CK(cudaStreamSynchronize(s));
+      njobs_l = (size_t)hcount[nseg];
       bool all = true;
       for (size_t j = 0; j < cj; ++j) all &= dh[j] != 0;
       if (all) break;
     }
-    launch(K_REF_GMRES, 0.0, 0.0, [&] {
-      gm_solve_kernel<<<(unsigned)cj, std::min(1024, std::max(32, ((cmax + 31) / 32) * 32)), 0, s>>>(drd, (int)cj);
+    // The correction and the new residual of every job of the outer step.
+    in_pieces(no, [&](size_t f0, size_t c) {
+      launch(K_REF_GMRES, 0.0, 0.0, [&] {
+        gm_solve_kernel<<<(unsigned)c, std::min(1024, std::max(32, ((cmax + 31) / 32) * 32)), 0, s>>>(drd, ojobs + f0);
+      });
     });
-    in_pieces(cj, [&](size_t f0, size_t c) {
-      launch(K_REF_GMRES, 0.0, 0.0, [&] { gm_update_kernel<<<dim3((unsigned)c, rows), 256, 0, s>>>(drd + f0); });
+    in_pieces(no, [&](size_t f0, size_t c) {
+      launch(K_REF_GMRES, 0.0, 0.0,
+             [&] { gm_update_kernel<<<dim3((unsigned)c, rows), 256, 0, s>>>(drd, ojobs + f0); });
     });
     launch(K_REF_GMRES, 0.0, 0.0, [&] {
       gm_residual_kernel<<<(unsigned)((cj + 127) / 128), 128, 0, s>>>(drd, (int)cj);
     });
-    in_pieces(cj, [&](size_t f0, size_t c) {
+    in_pieces(no, [&](size_t f0, size_t c) {
       launch(K_REF_RES, resid_flops * c / cj, 0.0,
-             [&] { refine_residual_kernel<<<dim3((unsigned)c, rows), 256, 0, s>>>(drd + f0); });
+             [&] { refine_residual_kernel<<<dim3((unsigned)c, rows), 256, 0, s>>>(drd, ojobs + f0); });
     });
-    for (int side = 0; side < nsides; ++side) slice_products(set_res + side, K_REF_RES);
-    slice_products(set_gam, K_REF_CHECK);
+    for (int side = 0; side < nsides; ++side) slice_products(set_res + side, K_REF_RES, ojobs, no);
+    slice_products(set_gam, K_REF_CHECK, ojobs, no);
     launch(K_REF_CHECK, 0.0, 0.0, [&] {
       refine_check_kernel<<<(unsigned)cj, 256, 0, s>>>(drd, ctx->refine_tol, ctx->max_iters, rt_out, rerr, rdone);
     });
     compact(0);
     CK(cudaMemcpyAsync(dh.data(), rdone, cj * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
+    njobs_l = nouter = (size_t)hcount[nseg];
     size_t active = 0;
     for (size_t j = 0; j < cj; ++j) active += (dh[j] == 0 && rdh[j].c != 0) ? 1 : 0;
     if (active == 0) break;

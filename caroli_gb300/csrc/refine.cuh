@@ -115,8 +115,9 @@ __global__ void __launch_bounds__(256) refine_update_kernel(RefineDesc* __restri
   }
 }
 
-__global__ void __launch_bounds__(256) refine_residual_kernel(RefineDesc* __restrict__ rd) {
-  const RefineDesc& R = rd[blockIdx.x];
+__global__ void __launch_bounds__(256) refine_residual_kernel(RefineDesc* __restrict__ rd,
+                                                              const int32_t* __restrict__ jl) {
+  const RefineDesc& R = rd[jl[blockIdx.x]];
   if (R.done) return;
   const int i = blockIdx.y * 256 + threadIdx.x;
   if (i >= R.nblk) return;
@@ -249,10 +250,13 @@ __device__ __forceinline__ double2 cconj_mul(double2 a, double2 b) {  // conj(a)
   return make_double2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
 }
 
+// The GMRES kernels run over a list of jobs `jl` (the solves still iterating, compacted on the
+// device): grid x indexes the list, so finished solves cost no blocks.
+
 // beta_j = |r_j|, V_0 = r / beta, g = (beta, 0, ...). grid (jobs, columns).
-__global__ void __launch_bounds__(256) gm_start_kernel(RefineDesc* __restrict__ rd) {
+__global__ void __launch_bounds__(256) gm_start_kernel(RefineDesc* __restrict__ rd, const int32_t* __restrict__ jl) {
   __shared__ double red[32];
-  RefineDesc& R = rd[blockIdx.x];
+  RefineDesc& R = rd[jl[blockIdx.x]];
   const int j = blockIdx.y;
   if (R.done || j >= R.c) return;
   const double2* r = R.r + (int64_t)j * R.nblk;
@@ -276,8 +280,9 @@ __global__ void __launch_bounds__(256) gm_start_kernel(RefineDesc* __restrict__ 
 
 // w = A z_k into V_{k+1}, A = z - H - Σ_L - Σ_R in FP64: z - H here, grid (jobs, row chunks of
 // 256); the dense Σ blocks of the slices follow as slice_gemm_kernel launches.
-__global__ void __launch_bounds__(256) gm_matvec_kernel(RefineDesc* __restrict__ rd, int k) {
-  const RefineDesc& R = rd[blockIdx.x];
+__global__ void __launch_bounds__(256) gm_matvec_kernel(RefineDesc* __restrict__ rd, const int32_t* __restrict__ jl,
+                                                        int k) {
+  const RefineDesc& R = rd[jl[blockIdx.x]];
   if (R.done || R.inner_done) return;
   const int i = blockIdx.y * 256 + threadIdx.x;
   if (i >= R.nblk) return;
@@ -296,9 +301,10 @@ __global__ void __launch_bounds__(256) gm_matvec_kernel(RefineDesc* __restrict__
 
 // Gram-Schmidt coefficients c_i = V_i^† w (i <= k) into y (pass 0 stores them in H, pass 1 adds).
 // grid (jobs, columns, k + 1).
-__global__ void __launch_bounds__(256) gm_dot_kernel(RefineDesc* __restrict__ rd, int k, int pass) {
+__global__ void __launch_bounds__(256) gm_dot_kernel(RefineDesc* __restrict__ rd, const int32_t* __restrict__ jl,
+                                                     int k, int pass) {
   __shared__ double red[32];
-  RefineDesc& R = rd[blockIdx.x];
+  RefineDesc& R = rd[jl[blockIdx.x]];
   const int j = blockIdx.y, i = blockIdx.z;
   if (R.done || R.inner_done || j >= R.c || R.col_done[j] != 0) return;
   const double2* v = R.V + (int64_t)i * R.nblk * R.c + (int64_t)j * R.nblk;
@@ -320,8 +326,9 @@ __global__ void __launch_bounds__(256) gm_dot_kernel(RefineDesc* __restrict__ rd
 }
 
 // w -= Σ_i c_i V_i. grid (jobs, row chunks).
-__global__ void __launch_bounds__(256) gm_axpy_kernel(RefineDesc* __restrict__ rd, int k) {
-  const RefineDesc& R = rd[blockIdx.x];
+__global__ void __launch_bounds__(256) gm_axpy_kernel(RefineDesc* __restrict__ rd, const int32_t* __restrict__ jl,
+                                                      int k) {
+  const RefineDesc& R = rd[jl[blockIdx.x]];
   if (R.done || R.inner_done) return;
   const int q = blockIdx.y * 256 + threadIdx.x;
   if (q >= R.nblk) return;
@@ -337,9 +344,10 @@ __global__ void __launch_bounds__(256) gm_axpy_kernel(RefineDesc* __restrict__ r
 
 // h_{k+1,k} = |w|, V_{k+1} = w / |w|, then the Givens rotations of column k and the residual
 // estimate |g_{k+1}|; a column converges when it is below tol * beta. grid (jobs, columns).
-__global__ void __launch_bounds__(256) gm_norm_kernel(RefineDesc* __restrict__ rd, int k, double tol) {
+__global__ void __launch_bounds__(256) gm_norm_kernel(RefineDesc* __restrict__ rd, const int32_t* __restrict__ jl,
+                                                      int k, double tol) {
   __shared__ double red[32];
-  RefineDesc& R = rd[blockIdx.x];
+  RefineDesc& R = rd[jl[blockIdx.x]];
   const int j = blockIdx.y;
   if (R.done || R.inner_done || j >= R.c || R.col_done[j] != 0) return;
   double2* w = R.V + (int64_t)(k + 1) * R.nblk * R.c + (int64_t)j * R.nblk;
@@ -419,17 +427,15 @@ __device__ __forceinline__ void gm_solve_column(RefineDesc& R, int j) {
   for (int t = kc; t < GM_M; ++t) y[t] = make_double2(0.0, 0.0);
 }
 
-// The coefficients of every column of every job: grid (jobs), a thread per column.
-__global__ void gm_solve_kernel(RefineDesc* __restrict__ rd, int njobs) {
-  const int job = blockIdx.x;
-  if (job >= njobs) return;
-  RefineDesc& R = rd[job];
+// The coefficients of every column of the listed jobs: grid (jobs), a thread per column.
+__global__ void gm_solve_kernel(RefineDesc* __restrict__ rd, const int32_t* __restrict__ jl) {
+  RefineDesc& R = rd[jl[blockIdx.x]];
   if (R.done) return;
   for (int j = threadIdx.x; j < R.c; j += blockDim.x) gm_solve_column(R, j);
 }
 
-__global__ void __launch_bounds__(256) gm_update_kernel(RefineDesc* __restrict__ rd) {
-  const RefineDesc& R = rd[blockIdx.x];
+__global__ void __launch_bounds__(256) gm_update_kernel(RefineDesc* __restrict__ rd, const int32_t* __restrict__ jl) {
+  const RefineDesc& R = rd[jl[blockIdx.x]];
   if (R.done) return;
   const int q = blockIdx.y * 256 + threadIdx.x;
   if (q >= R.nblk) return;
@@ -496,10 +502,12 @@ struct SliceTask {
 
 constexpr int SG_ROWS = 64, SG_COLS = 32, SG_K = 16;
 
-__global__ void __launch_bounds__(256) slice_gemm_kernel(const SliceTask* __restrict__ tasks) {
+// Both slice kernels take the tasks of the jobs in `jl` (a job's task is tasks[job]).
+__global__ void __launch_bounds__(256) slice_gemm_kernel(const SliceTask* __restrict__ tasks,
+                                                         const int32_t* __restrict__ jl) {
   __shared__ double2 As[SG_K][SG_ROWS];
   __shared__ double2 Bs[SG_K][SG_COLS];
-  const SliceTask t = tasks[blockIdx.z];
+  const SliceTask t = tasks[jl[blockIdx.z]];
   const RefineDesc& R = *t.rd;
   if (R.done || (t.mode == 0 && R.inner_done)) return;
   const int i0 = blockIdx.x * SG_ROWS, j0 = blockIdx.y * SG_COLS;
@@ -593,10 +601,11 @@ __global__ void __launch_bounds__(256) slice_gemm_kernel(const SliceTask* __rest
 // output row holding its CB sums, the input rows of a K step staged in shared memory. A 64 x 32
 // tile would leave most of its columns empty there. grid (row chunks of 128, tasks), 128 threads.
 template <int CB>
-__global__ void __launch_bounds__(128) slice_rows_kernel(const SliceTask* __restrict__ tasks) {
+__global__ void __launch_bounds__(128) slice_rows_kernel(const SliceTask* __restrict__ tasks,
+                                                         const int32_t* __restrict__ jl) {
   constexpr int KS = 64;
   __shared__ double2 Xs[KS][CB];
-  const SliceTask t = tasks[blockIdx.y];
+  const SliceTask t = tasks[jl[blockIdx.y]];
   const RefineDesc& R = *t.rd;
   if (R.done || (t.mode == 0 && R.inner_done)) return;
   const int i0 = blockIdx.x * 128;
