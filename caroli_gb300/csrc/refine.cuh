@@ -227,7 +227,7 @@ namespace caroli {
 
 // ---- GMRES for the correction of an outer step ---------------------------------------------------
 // Right preconditioning: A M^-1 u = r, d = M^-1 (V y) = Z y. Arnoldi vectors in FP64, classical
-// Gram-Schmidt applied twice, complex Givens rotations (c real), per right-hand-side column.
+// Gram-Schmidt (one pass), complex Givens rotations (c real), per right-hand-side column.
 
 __device__ __forceinline__ double block_sum(double v, double* red) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
