@@ -30,6 +30,8 @@ transmissions and against Lopez-Sancho decimation.
 """
 from __future__ import annotations
 
+import threading
+
 import numpy as np
 import scipy.linalg as sla
 
@@ -87,6 +89,9 @@ class LeadSolver:
             if r < n:
                 root = np.sqrt(sv[:r])
                 self.uv = (uu[:, :r] * root[None, :], vh[:r].conj().T * root[None, :])
+        # The modes of the last general or reduced solve, per thread: energies may be solved on
+        # several host threads at once (NestedTwoTerminal.self_energies_many).
+        self._tls = threading.local()
         self.cell = None
         if n and np.abs(self.h01).max() > 0 and _hermitian(self.h00) and _hermitian(self.h01):
             c = self.h01[0, 0].real
@@ -146,7 +151,7 @@ class LeadSolver:
                     flux = y[:, prop] / np.sqrt(c) / np.sqrt(2.0 * np.abs(lam_r.imag[prop]))[None, :]
                     return flux, lam_r[prop], flux.copy(), lam_l[prop], sig[1], e
                 sig = self._reduced(e) if self.uv is not None else self._general(e)
-                (rm, rl), (lm, ll) = self._last_modes
+                (rm, rl), (lm, ll) = self._tls.last_modes
                 return rm, rl, lm, ll, sig[1], e
             except GreenError as err:
                 last = err
@@ -250,7 +255,7 @@ class LeadSolver:
                 return np.zeros((n, 0), np.complex128), np.zeros(0, np.complex128)
             return np.array([m[0] for m in ms]).T, np.array([m[1] for m in ms])
 
-        self._last_modes = (stack(right_modes), stack(left_modes))
+        self._tls.last_modes = (stack(right_modes), stack(left_modes))
         nr = int(right_ev.sum()) + len(right_vecs)
         nl = int(left_ev.sum()) + len(left_vecs)
         if nr != n or nl != n:
@@ -365,7 +370,7 @@ class LeadSolver:
                 return np.zeros((n, 0), np.complex128), np.zeros(0, np.complex128)
             return np.array([m[0] for m in ms]).T, np.array([m[1] for m in ms])
 
-        self._last_modes = (stack(right_modes), stack(left_modes))
+        self._tls.last_modes = (stack(right_modes), stack(left_modes))
         nr = int(right_ev.sum()) + len(right_x)
         nl = int(left_ev.sum()) + len(left_x)
         if nr != r or nl != r:

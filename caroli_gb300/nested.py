@@ -27,7 +27,10 @@ raises ``GreenError("Singular", …)`` as ``GreenError::Singular`` (nested.rs:79
 """
 from __future__ import annotations
 
+import contextlib
 import math
+import os
+from concurrent.futures import ThreadPoolExecutor
 from dataclasses import dataclass
 
 import numpy as np
@@ -188,6 +191,37 @@ class NestedTwoTerminal:
             blocks.append((sl, sr))
         return LeadSelfEnergies(float(energy), blocks)
 
+    def self_energies_many(self, energies, threads=None, errors=False):
+        """``self_energies`` at many energies, spread over host threads (the reference maps its
+        energies in parallel, ``NestedTwoTerminal::transmissions``, nested.rs:622-626): each
+        energy's eigenproblems run in LAPACK, which releases the interpreter lock, with the BLAS
+        limited to one thread per worker so that the workers do not oversubscribe the cores.
+        ``threads`` defaults to the host's cores when ``threadpoolctl`` can set that limit, else to
+        one (multithreaded BLAS under several workers was measured slower than one worker). With
+        ``errors`` an energy whose modes fail gives its ``GreenError`` in place instead of raising."""
+        energies = list(energies)
+        try:
+            from threadpoolctl import threadpool_limits
+        except ImportError:
+            threadpool_limits = None
+
+        def one(e):
+            try:
+                return self.self_energies(e)
+            except GreenError as err:
+                if errors:
+                    return err
+                raise
+
+        if threads is None:
+            threads = (os.cpu_count() or 1) if threadpool_limits is not None else 1
+        threads = max(1, min(int(threads), len(energies)))
+        if threads == 1:
+            return [one(e) for e in energies]
+        limit = threadpool_limits(1) if threadpool_limits is not None else contextlib.nullcontext()
+        with limit, ThreadPoolExecutor(max_workers=threads) as pool:
+            return list(pool.map(one, energies))
+
     def self_energies_broadened(self, energy, eta) -> LeadSelfEnergies:
         """Σ at E + iη with the device at the real E (``SelfEnergyMethod::ModesBroadened``,
         caroli-green/src/lib.rs:49-66): no propagating lead mode, as the thesis codes compute it."""
@@ -327,10 +361,16 @@ class NestedTwoTerminal:
         return out
 
     def transmissions(self, energies, config=0, precision=Precision.DOUBLE):
-        sigmas = []
-        for e in energies:
-            sigmas.append(self.self_energies(e))
-        return self.transmissions_with(sigmas, [config] * len(sigmas), precision)
+        """T at many energies (``NestedTwoTerminal::transmissions``, nested.rs:622-626): the lead
+        self-energies on host threads, the solves in one GPU batch; an energy whose self-energies
+        or solve fail is a ``GreenError`` in its place."""
+        sigmas = self.self_energies_many(energies, errors=True)
+        ok = [i for i, s in enumerate(sigmas) if not isinstance(s, GreenError)]
+        out = list(sigmas)
+        if ok:
+            for i, r in zip(ok, self.transmissions_with([sigmas[i] for i in ok], [config] * len(ok), precision)):
+                out[i] = r
+        return out
 
     def set_parameter_derivatives(self, derivs):
         """dH/dp for gradient parameters: ``derivs[c][k]`` = values of dH/dp_k of configuration c

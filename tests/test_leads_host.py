@@ -91,3 +91,83 @@ def test_reduced_pencil_solves_the_dyson_equation(width):
         rr = sr - ls.h01 @ np.linalg.solve(e * eye - ls.h00 - sr, ls.h01.conj().T)
         rl = sl - ls.h01.conj().T @ np.linalg.solve(e * eye - ls.h00 - sl, ls.h01)
         assert max(np.abs(rr).max(), np.abs(rl).max()) < 1e-11, e
+
+
+def test_self_energies_many_matches_serial_and_keeps_failures_in_place(monkeypatch):
+    """Σ of many energies on host threads (as the reference's parallel map over energies,
+    nested.rs:622-626) equals the serial Σ bit for bit; with errors=True a failing energy (made to
+    fail on the host) is a GreenError in its place, the others unaffected; without it, it raises."""
+    from caroli_gb300 import GreenError
+
+    m = bhz()
+    s = NestedTwoTerminal.from_model(m, m, Region.cuboid(m.lattice, [6, 12, 0]), 0)
+    es = list(np.linspace(-0.3, 0.3, 9))
+    serial = [s.self_energies(e) for e in es]
+    par = s.self_energies_many(es, threads=4)
+    for a, b in zip(serial, par):
+        assert a.energy == b.energy
+        for (al, ar), (bl, br) in zip(a.blocks, b.blocks):
+            assert np.array_equal(al, bl) and np.array_equal(ar, br)
+    orig = s.self_energies
+
+    def flaky(e):
+        if e == es[3]:
+            raise GreenError("Eigen", "made to fail")
+        return orig(e)
+
+    monkeypatch.setattr(s, "self_energies", flaky)
+    out = s.self_energies_many(es, threads=4, errors=True)
+    assert isinstance(out[3], GreenError)
+    for i, o in enumerate(out):
+        if i != 3:
+            assert not isinstance(o, GreenError)
+            assert np.array_equal(o.blocks[0][0], serial[i].blocks[0][0])
+    with pytest.raises(GreenError):
+        s.self_energies_many(es, threads=4)
+
+
+def test_lead_modes_are_per_thread():
+    """The modes of the reduced pencil (graphene's zigzag lead) computed on several threads at
+    once equal those computed one after another: each thread keeps its own last modes."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    ls = _lead(graphene(), 24)
+    assert ls.uv is not None
+    es = [-1.2, -0.7, -0.2, 0.4, 0.9, 1.3]
+    serial = [ls.modes(e) for e in es]
+    with ThreadPoolExecutor(max_workers=4) as pool:
+        par = list(pool.map(ls.modes, es))
+    for a, b in zip(serial, par):
+        assert a[0].shape == b[0].shape and a[2].shape == b[2].shape
+        for x, y in zip(a[:5], b[:5]):
+            assert np.array_equal(x, y)
+
+
+def test_transmissions_places_failed_energies(monkeypatch):
+    """NestedTwoTerminal.transmissions (nested.rs:622-626): an energy whose self-energies fail is a
+    GreenError in its place and the others are solved in one batch, in order (the batch call is
+    replaced by a stand-in that returns each energy, so no GPU is needed)."""
+    from caroli_gb300 import GreenError
+
+    m = bhz()
+    s = NestedTwoTerminal.from_model(m, m, Region.cuboid(m.lattice, [6, 12, 0]), 0)
+    es = [-0.2, -0.1, 0.0, 0.1, 0.2]
+    orig = s.self_energies
+
+    def flaky(e):
+        if e == 0.0:
+            raise GreenError("Eigen", "made to fail")
+        return orig(e)
+
+    seen = {}
+
+    def batch(sigmas, configs, precision):
+        seen["configs"] = list(configs)
+        return [sg.energy for sg in sigmas]
+
+    monkeypatch.setattr(s, "self_energies", flaky)
+    monkeypatch.setattr(s, "transmissions_with", batch)
+    out = s.transmissions(es, config=3)
+    assert isinstance(out[2], GreenError)
+    assert [out[i] for i in (0, 1, 3, 4)] == [es[i] for i in (0, 1, 3, 4)]
+    assert seen["configs"] == [3, 3, 3, 3]
