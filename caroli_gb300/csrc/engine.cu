@@ -928,18 +928,16 @@ RefineDesc* refine(caroli_ctx* ctx, System* sys, const std::vector<JobSpec>& spe
                [&] { gm_matvec_kernel<<<dim3((unsigned)c, rows), 256, 0, s>>>(drd, jl + f0, k); });
       });
       for (int side = 0; side < nsides; ++side) slice_products(set_mv + (size_t)k * nsides + side, K_REF_RES, jl, nl);
-      // Classical Gram-Schmidt, one pass: right-preconditioned by the f32 factors, A M^-1 is close
-      // to the identity and its few Krylov vectors stay orthogonal to working accuracy; the outer
-      // step checks the true FP64 residual either way.
-      for (int pass = 0; pass < 1; ++pass) {
-        in_pieces(nl, [&](size_t f0, size_t c) {
-          launch(K_REF_GMRES, 0.0, vec_pass * 2.0 * (k + 1) * c / cj, [&] {
-            gm_dot_kernel<<<dim3((unsigned)c, cols, (unsigned)(k + 1)), 256, 0, s>>>(drd, jl + f0, k, pass);
-          });
-          launch(K_REF_GMRES, 0.0, vec_pass * (k + 3.0) * c / cj,
-                 [&] { gm_axpy_kernel<<<dim3((unsigned)c, rows), 256, 0, s>>>(drd, jl + f0, k); });
+      // Classical Gram-Schmidt, one pass (gm_dot_kernel pass 0): right-preconditioned by the f32
+      // factors, A M^-1 is close to the identity and its few Krylov vectors stay orthogonal to
+      // working accuracy; the outer step checks the true FP64 residual either way.
+      in_pieces(nl, [&](size_t f0, size_t c) {
+        launch(K_REF_GMRES, 0.0, vec_pass * 2.0 * (k + 1) * c / cj, [&] {
+          gm_dot_kernel<<<dim3((unsigned)c, cols, (unsigned)(k + 1)), 256, 0, s>>>(drd, jl + f0, k, 0);
         });
-      }
+        launch(K_REF_GMRES, 0.0, vec_pass * (k + 3.0) * c / cj,
+               [&] { gm_axpy_kernel<<<dim3((unsigned)c, rows), 256, 0, s>>>(drd, jl + f0, k); });
+      });
       in_pieces(nl, [&](size_t f0, size_t c) {
         launch(K_REF_GMRES, 0.0, vec_pass * 3.0 * c / cj,
                [&] { gm_norm_kernel<<<dim3((unsigned)c, cols), 256, 0, s>>>(drd, jl + f0, k, ctx->inner_tol); });
